@@ -1,0 +1,305 @@
+"""Benchmark of the fix-eph hot path on GB300: fix-eph atom-steps/s.
+
+Workload (the plain FP64 cascade at scale): fcc Ni 80x80x80 cells (2,048,000
+atoms) at 300 K, a 10 keV primary knock-on atom at the box centre, dt 0.5 fs,
+the synthetic beta file (rho(r) = exp(-r/0.6) cut at 4.6 A, beta(rho) = 0.05
++ 0.02 tanh(rho - 2), 2,000 knots each), flags 7 (friction + random + FDM),
+model 4, FDM grid 64^3 with C_e 3.5e-6, kappa 0.1, T_e 300 K.  Seeded synthetic
+inputs stand in for the reference's LAMMPS decks; no pair potential (the metric
+excludes pair forces: external force zero).
+
+One step = one engine step through the fix: initial_integrate, position wrap
+check, binning + in-cutoff pair list, density, friction pre-vector, friction +
+random forces, final_integrate, energy deposition, FDM substeps.  `value` is
+device-resident (CUDA events on the fix's stream); `e2e` drives the same
+step through the C ABI hooks with host buffers (positions, velocities, forces
+copied in and out every step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "user-eph_gb300"))
+sys.path.insert(0, REPO)
+
+CELLS = 80
+GRID = (64, 64, 64)
+DT = 0.0005
+PKA_EV = 10000.0
+SEED = 4242
+WORKLOAD = "fcc Ni 80^3 cells (2,048,000 atoms), 10 keV PKA, dt 0.5 fs, FDM 64^3, flags 7, model 4"
+METRIC = "fix-eph atom-steps/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_system(workdir, cells=CELLS, grid=GRID):
+    from ephgb import workloads as W
+
+    bf = W.write_beta_file(os.path.join(workdir, "synth.beta"))
+    atoms = W.fcc_lattice(cells, seed=SEED)
+    W.add_pka(atoms, PKA_EV, seed=SEED + 1)
+    words = W.fix_args(bf, seed=SEED, flags=7, model=4, grid=grid, T_out=os.path.join(workdir, "Te_out"))
+    return words, atoms
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def forces_bytes(n_atoms, n_pairs):
+    """Algorithmic HBM bytes of one launch of the force sweep (k_forces):
+    per atom A_i, Bw_i (64 B), pair count (4), T_e at the atom (8), f read and
+    written (64), f_EPH and f_RNG written (64); per in-cutoff pair the cached
+    index (4), e_ij with rho_j(r^2)/r^2 (32) and rho_i(r^2)/r^2 (16).  The
+    neighbours' records are L2 hits and not counted."""
+    return 204 * n_atoms + 52 * n_pairs
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import ephgb
+
+    dev = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(dev)
+    out = {}
+    with tempfile.TemporaryDirectory() as wd:
+        words, atoms = make_system(wd)
+        n = atoms.n
+        fix = ephgb.FixEPH(words, atoms, dt=DT, mode=ephgb.MODE_FAST, device=dev)
+        stream = torch.cuda.current_stream()
+        fix.set_stream(stream.cuda_stream)
+        # ---------------------------------------------- device-resident value
+        fix.step(args.warmup)
+        fix.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        fix.set_profiling(True)
+        clocks = ClockSampler(dev)
+        clocks.start()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fix.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        clock = clocks.stop()
+        fix.synchronize()
+        phases = fix.phase_times()
+        launches = fix.launch_count()
+        fix.set_profiling(False)
+        n_pairs = fix.pair_count()
+        out.update(ms=ms, phases=phases, launches=launches, n_pairs=n_pairs, clocks=clock, n=n,
+                   rebuilds=fix.counter("wrap"))
+        # ------------------------------------------------ end to end (host)
+        x = torch.empty((n, 3), dtype=torch.float64).pin_memory()
+        v = torch.empty((n, 3), dtype=torch.float64).pin_memory()
+        f = torch.zeros((n, 3), dtype=torch.float64).pin_memory()
+        x.numpy()[:] = fix.get("x")
+        v.numpy()[:] = fix.get("v")
+        e2e_steps = max(1, min(args.steps, 20))
+
+        def host_step():
+            fix.put("x", x.numpy())
+            fix.put("v", v.numpy())
+            fix.put("f", f.numpy())
+            fix.initial_integrate()
+            fix.put("f", f.numpy())  # the pair force of this step (none)
+            fix.post_force()
+            fix.final_integrate()
+            fix.end_of_step()
+            fix.get("x", out=x.numpy())
+            fix.get("v", out=v.numpy())
+            fix.get("f", out=f.numpy())
+            f.numpy()[:] = 0.0
+            return fix.compute_vector(0)
+
+        for _ in range(2):
+            host_step()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            host_step()
+        torch.cuda.synchronize()
+        t_e2e = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([t_e2e], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        out.update(t_e2e=t_e2e, e2e_steps=e2e_steps, h2d=3 * 3 * 8 * n, d2h=3 * 3 * 8 * n + 8)
+    return out
+
+
+def cpu_baseline(threads, steps=1, warm=1):
+    """The CPU restatement (oracle port) on the same workload: `steps` steps
+    of the full system after `warm` warm-up steps; time of the fix's own hooks
+    (integrator, post_force, end_of_step), neighbour builds excluded as in
+    LAMMPS's Modify timer."""
+    from oracle.bindings import OracleFix
+
+    with tempfile.TemporaryDirectory() as wd:
+        words, atoms = make_system(wd)
+        fix = OracleFix(words, atoms, DT, threads=threads)
+        for _ in range(warm):
+            fix.step(None)
+        t0 = fix.seconds(0)
+        for _ in range(steps):
+            fix.step(None)
+        t = fix.seconds(0) - t0
+        return {"value": atoms.n * steps / t, "unit": METRIC, "cores": threads, "kind": "port",
+                "sample": f"{steps} step(s) of the full {atoms.n}-atom workload after {warm} warm-up step(s); "
+                          f"fix hooks only (neighbour builds excluded), OpenMP over atoms, {threads} threads",
+                "seconds": t}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        # the reference algorithm on the host cores (the oracle port: the
+        # reference's own sources need its engine and are not on this host)
+        if rank != 0:
+            return
+        k = max(1, min(args.steps, 3))
+        cb = cpu_baseline(threads, steps=k, warm=1)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": 0,
+                "steps": k, "warmup": 1, "ms_per_step": 1000.0 * cb["seconds"] / k, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "steps_timed": k},
+                "cpu_baseline": {k2: cb[k2] for k2 in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    res = run_gpu(args, rank, world)
+    n = res["n"]
+    value = world * n * args.steps / (res["ms"] / 1000.0)
+    e2e = world * n * res["e2e_steps"] / res["t_e2e"]
+    ms_f, nl_f = res["phases"]["forces"]
+    hbm, peak_src = peaks()
+    t_launch = ms_f / max(nl_f, 1) / 1000.0
+    achieved = forces_bytes(n, res["n_pairs"]) / t_launch / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "atoms_per_gpu": n, "grid": list(GRID), "dt_ps": DT,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 52 // 2 ** 20),
+                   "mode": "fast", "xi": "device Philox4x32-10"},
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
+                "steps": res["e2e_steps"]},
+        "gpu_launches": res["launches"],
+        "roofline": {"bound": "hbm", "kernel": "k_forces", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
+                     "note": "FP64-issue bound: GB300 issues ~0.5e12 FP64 instructions/s"},
+        "phases_ms": {k: round(v[0], 3) for k, v in res["phases"].items()},
+        "clocks": res["clocks"],
+        "pairs_per_atom": res["n_pairs"] / n,
+        "wraps": res["rebuilds"],
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(threads, steps=1, warm=1).items() if k != "seconds"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

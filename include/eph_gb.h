@@ -1,0 +1,197 @@
+/*
+ * eph_gb.h -- C ABI of the GB300 electron-phonon (`fix eph`) hot path.
+ *
+ * Drop-in boundary for the LAMMPS fix `eph` of USER-EPH (fix_eph.h:11-12,
+ * `FixStyle(eph,FixEPH)`): a context is built from the fix command's own words
+ * and then driven through the four hooks the reference fix registers
+ * (fix_eph.cpp:293-302: INITIAL_INTEGRATE, POST_FORCE, FINAL_INTEGRATE,
+ * END_OF_STEP).  All per-step work runs as sm_103a CUDA kernels on one GPU in
+ * FP64; there is no CPU fallback.  Plain C types only; every call returns an
+ * EPH_OK / EPH_ERR_* status and never throws.
+ *
+ * Ownership: the context owns all device memory; the caller owns every buffer
+ * it passes.  Host buffers use the engine's layout (x[n][3] etc.).  All device
+ * work is ordered on the context's CUDA stream; calls that hand data back to
+ * the host synchronise that stream.
+ */
+#ifndef EPH_GB_H
+#define EPH_GB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define EPH_OK 0
+#define EPH_ERR_ARG 1               /* bad argument (fix_eph.cpp:64, :140, :182, :196 error->all) */
+#define EPH_ERR_FILE 2              /* beta or grid file unreadable (eph_beta.h:42, eph_fdm.h:50 asserts) */
+#define EPH_ERR_UNSUPPORTED_MODEL 3 /* model other than 4 (fix_eph.cpp:888 throws) */
+#define EPH_ERR_CAPACITY 4          /* a bin or pair list overflowed its capacity */
+#define EPH_ERR_TIMEOUT 5           /* a bounded device wait gave up */
+#define EPH_ERR_CUDA 6              /* CUDA runtime error (no device, launch failure) */
+#define EPH_ERR_STATE 7             /* call out of order (e.g. hooks before eph_set_atoms) */
+#define EPH_ERR_RANGE 8             /* an input outside the tables / box the kernels index */
+
+/* arithmetic of the per-pair sweeps */
+#define EPH_MODE_EXACT 0 /* the reference's expression order, no FMA: bit-identical forces */
+#define EPH_MODE_FAST 1  /* per-atom alpha/rho and per-pair rho(r^2)/r^2 factored out, FMA */
+
+/* where a buffer lives */
+#define EPH_HOST 0
+#define EPH_DEVICE 1
+
+/* source of the Gaussian deviates xi of the random force */
+#define EPH_XI_DEVICE_RNG 0 /* counter-based Philox4x32-10 on the device, seeded by the fix seed */
+#define EPH_XI_GIVEN 1      /* the deviates last passed with eph_put(EPH_FIELD_XI) */
+
+/* per-atom and grid fields for eph_put / eph_get */
+#define EPH_FIELD_X 0       /* positions, n x 3 (put/get) */
+#define EPH_FIELD_V 1       /* velocities, n x 3 (put/get) */
+#define EPH_FIELD_F 2       /* total force, n x 3 (put/get) */
+#define EPH_FIELD_XI 3      /* Gaussian deviates for the next post_force, n x 3 (put) */
+#define EPH_FIELD_F_EPH 4   /* friction force of the last post_force, n x 3 (get) */
+#define EPH_FIELD_F_RNG 5   /* random force of the last post_force, n x 3 (get) */
+#define EPH_FIELD_RHO 6     /* site density rho_i, n (get) */
+#define EPH_FIELD_W 7       /* friction pre-vector w_i, n x 3 (get) */
+#define EPH_FIELD_PERATOM 8 /* the fix's per-atom array, n x 8: rho, beta(rho), f_EPH, f_RNG (get) */
+#define EPH_FIELD_T_E 9     /* electronic temperature grid, ncells (put/get) */
+#define EPH_FIELD_F_EXT 10  /* external force applied by eph_step as the pair force, n x 3 (put) */
+
+/* splines of a beta file, for eph_beta_eval / eph_beta_table */
+#define EPH_SPLINE_RHO_R 0    /* rho(r) */
+#define EPH_SPLINE_RHO_R_SQ 1 /* rho(r^2) */
+#define EPH_SPLINE_BETA 2     /* beta(rho) */
+#define EPH_SPLINE_ALPHA 3    /* alpha(rho), spline of sqrt(beta) knots */
+
+typedef struct eph_ctx eph_ctx;
+
+/* What the fix reads from the engine besides its own words. */
+typedef struct eph_md {
+  int ntypes;         /* atom->ntypes */
+  const double *mass; /* atom->mass, ntypes + 1 entries, index 1..ntypes */
+  double boxlo[3];    /* domain->boxlo (orthogonal, periodic, 3-D: fix_eph.cpp:263-271) */
+  double boxhi[3];    /* domain->boxhi */
+  double dt;          /* update->dt */
+  double boltz;       /* force->boltz */
+  double ftm2v;       /* force->ftm2v */
+  double skin;        /* neighbor->skin: eph_step wraps positions when an atom moved > skin/2 */
+  int groupbit;       /* the fix group's bit */
+  int device;         /* CUDA device ordinal */
+  int mode;           /* EPH_MODE_EXACT or EPH_MODE_FAST */
+} eph_md;
+
+/* Build a context from the words of the fix command: arg[0] fix ID, arg[1]
+ * group, arg[2] style ("eph"), then seed flags model rho_e C_e kappa_e T_e NX
+ * NY NZ T_infile freq T_out beta_file and one element name per atom type.
+ * Replaces FixEPH::FixEPH (fix_eph.cpp:61-241) and FixEPH::init
+ * (fix_eph.cpp:263-287).  Only model 4 (PRL) is accepted. */
+int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out);
+void eph_destroy(eph_ctx *ctx);
+const char *eph_last_error(const eph_ctx *ctx);
+const char *eph_status_string(int status);
+
+/* Set (or reset) the atoms: n locals with positions, velocities, types
+ * 1..ntypes and group masks (mask may be NULL: all in the group).  Host
+ * buffers.  Replaces FixEPH::grow_arrays (fix_eph.cpp:918-938) plus the
+ * engine's atom storage. */
+int eph_set_atoms(eph_ctx *ctx, int n, const double *x, const double *v, const int *type, const int *mask);
+
+/* Copy a field in or out (where = EPH_HOST or EPH_DEVICE pointer). */
+int eph_put(eph_ctx *ctx, int field, const double *src, int where);
+int eph_get(eph_ctx *ctx, int field, double *dst, int where);
+
+/* The hooks.  FixEPH::initial_integrate (fix_eph.cpp:305-328). */
+int eph_initial_integrate(eph_ctx *ctx);
+/* FixEPH::post_force (fix_eph.cpp:841-907) with force_prl
+ * (fix_eph.cpp:687-837) and calculate_environment (fix_eph.cpp:431-466):
+ * adds f_EPH and f_RNG to the force held by the context. */
+int eph_post_force(eph_ctx *ctx, int xi_source);
+/* FixEPH::final_integrate (fix_eph.cpp:330-348). */
+int eph_final_integrate(eph_ctx *ctx);
+/* FixEPH::end_of_step (fix_eph.cpp:350-429): energy deposition onto the
+ * grid, EPH_FDM::solve (eph_fdm.h:267-400), temperature output every freq
+ * steps, Ee accumulation. */
+int eph_end_of_step(eph_ctx *ctx);
+
+/* nsteps engine steps on the device (Verlet::run order): initial_integrate,
+ * position wrap when an atom moved > skin/2, force = external force,
+ * post_force, final_integrate, end_of_step.  Device-resident; with
+ * EPH_XI_GIVEN every step reuses the deviates last put. */
+int eph_step(eph_ctx *ctx, int nsteps, int xi_source);
+
+/* FixEPH::compute_vector (fix_eph.cpp:940-948): 0 -> cumulative energy
+ * transferred to the electrons, 1 -> mean electronic temperature
+ * (eph_fdm.h:189-196). */
+int eph_compute_vector(eph_ctx *ctx, int i, double *out);
+/* FixEPH::reset_dt (fix_eph.cpp:909-916). */
+int eph_reset_dt(eph_ctx *ctx, double dt);
+/* EPH_FDM::save_state (eph_fdm.h:226-265) and save_temperature
+ * (eph_fdm.h:198-224) of the current grid. */
+int eph_save_state(eph_ctx *ctx, const char *path);
+int eph_save_temperature(eph_ctx *ctx, const char *path, int n);
+/* FixEPH::post_run (fix_eph.cpp:1019-1021): writes T.restart or
+ * <T_infile>.restart. */
+int eph_post_run(eph_ctx *ctx);
+/* The current engine step number (update->ntimestep as the context counts it). */
+int eph_set_timestep(eph_ctx *ctx, long ntimestep);
+/* Order the context's work on a caller's CUDA stream (cudaStream_t), or 0. */
+int eph_set_stream(eph_ctx *ctx, void *stream);
+/* Wait for the context's work and report any device-side error. */
+int eph_synchronize(eph_ctx *ctx);
+/* Device-side counters: 0 atoms with rho > rho_cutoff (the reference warns
+ * once, eph_beta.h:174-180), 1 grid cells clamped at T = 0 (eph_fdm.h:391-394),
+ * 2 neighbour-list builds, 3 position wraps. */
+int eph_get_counter(eph_ctx *ctx, int which, long *out);
+/* Capacity of a spatial bin and of a per-atom pair list (0 keeps a value). */
+int eph_set_capacity(eph_ctx *ctx, int bin_capacity, int pair_capacity);
+
+/* Timing of the step's phases with CUDA events on the context's stream
+ * (no reference counterpart; the reference relies on gprof, lib/Makefile:25-28).
+ * Phases: */
+#define EPH_PHASE_INTEGRATE 0  /* initial + final integrate */
+#define EPH_PHASE_BIN 1        /* spatial binning */
+#define EPH_PHASE_DENSITY 2    /* neighbour pairs + rho_i (calculate_environment) */
+#define EPH_PHASE_FRICTION_W 3 /* force_prl stage 1 */
+#define EPH_PHASE_FORCES 4     /* force_prl stages 2 + 3 and the force update */
+#define EPH_PHASE_DEPOSIT 5    /* energy deposition + energy total */
+#define EPH_PHASE_FDM 6        /* EPH_FDM::solve substeps */
+#define EPH_NPHASES 7
+/* on != 0 starts recording (and zeroes the totals); off stops. */
+int eph_set_profiling(eph_ctx *ctx, int on);
+/* milliseconds and kernel launches per phase since profiling was switched on
+ * (arrays of EPH_NPHASES; either may be NULL). */
+int eph_phase_times(eph_ctx *ctx, double *ms, long *launches);
+/* kernels this context launched since profiling was last switched */
+int eph_launch_count(eph_ctx *ctx, long *out);
+/* in-cutoff pairs (directed) of the last post_force */
+int eph_pair_count(eph_ctx *ctx, long *out);
+
+/* Host-side parametrisation (no GPU needed): the beta file reader and the
+ * splines it builds (eph_beta.h:39-128, eph_spline.h:31-142). */
+typedef struct eph_beta eph_beta;
+int eph_beta_load(const char *path, eph_beta **out);
+void eph_beta_free(eph_beta *b);
+int eph_beta_info(const eph_beta *b, int *n_elements, double *r_cutoff, double *rho_cutoff);
+/* value of one spline (which = EPH_SPLINE_*) of element elem at x */
+double eph_beta_eval(const eph_beta *b, int which, int elem, double x);
+/* copy the coefficient table (a, b, c, d per knot) into out (may be NULL);
+ * returns the number of knots */
+long eph_beta_table(const eph_beta *b, int which, int elem, double *out);
+
+/* Host-side grid (no GPU needed): uniform grid or grid file
+ * (eph_fdm.h:28-119), stability substeps (eph_fdm.h:275-313), writers. */
+typedef struct eph_grid eph_grid;
+int eph_grid_create(long nx, long ny, long nz, const double *lo, const double *hi, double T_e, double C_e,
+                    double rho_e, double kappa_e, eph_grid **out);
+int eph_grid_load(const char *path, eph_grid **out);
+void eph_grid_free(eph_grid *g);
+long eph_grid_ncells(const eph_grid *g);
+/* number of substeps solve() takes for time step dt, and their length */
+unsigned eph_grid_substeps(const eph_grid *g, double dt, double *inner_dt);
+int eph_grid_save_state(const eph_grid *g, const char *path);
+int eph_grid_save_temperature(const eph_grid *g, const char *path, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,529 @@
+/*
+ * Parity harness around the reference `fix eph` (USER-EPH fix_eph.cpp,
+ * fix_eph.h, eph_beta.h, eph_spline.h, eph_fdm.h, eph_linear.h compiled
+ * UNCHANGED from the reference tree) running inside the engine stand-in of
+ * lammps_mock/.  TEST INFRASTRUCTURE ONLY: built by oracle/Makefile into
+ * oracle/_ref/ when the reference sources are present, loaded by tests to pin
+ * the CPU restatement (eph_oracle.c) and to write the golden fixtures.
+ *
+ * Engine behaviour reproduced here (LAMMPS Verlet::run order, see
+ * fix_eph.cpp:293-302 for the hooks the fix registers):
+ *   setup : wrap positions, make ghosts, build the full list, f = f_ext
+ *   step  : ntimestep += 1; initial_integrate (fix_eph.cpp:305-328);
+ *           rebuild if any atom moved > skin/2 (wrap, ghosts, list) else
+ *           copy owner x, v to ghosts; f = f_ext; post_force (:841-907);
+ *           final_integrate (:330-348); end_of_step (:350-429)
+ * The Gaussian deviates the fix draws with RanMars::gaussian() are injected.
+ */
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "atom.h"
+#include "comm.h"
+#include "domain.h"
+#include "error.h"
+#include "fix.h"
+#include "force.h"
+#include "memory.h"
+#include "neigh_list.h"
+#include "neighbor.h"
+#include "random_mars.h"
+#include "update.h"
+
+#include "fix_eph.h"
+
+using namespace LAMMPS_NS;
+
+namespace {
+
+// The reference fix with read access to its per-atom arrays.
+class FixEPHProbe : public FixEPH {
+ public:
+  FixEPHProbe(LAMMPS *l, int narg, char **arg) : FixEPH(l, narg, arg) {}
+  double *rho() { return rho_i; }
+  double **feph() { return f_EPH; }
+  double **frng() { return f_RNG; }
+  double **w() { return w_i; }
+  double **xi() { return xi_i; }
+  double **arr() { return array; }
+  RanMars *rng() { return random; }
+  double T_at(double x, double y, double z) const { return fdm.get_T(x, y, z); }
+  void save_T(const char *path, int n) const { fdm.save_temperature(path, n); }
+  void save_state(const char *path) const { fdm.save_state(path); }
+};
+
+struct Sim {
+  LAMMPS lmp;
+  Atom atom;
+  Domain domain;
+  Neighbor neighbor;
+  Memory memory;
+  Force force;
+  Update update;
+  Comm comm;
+  Error error;
+  NeighList list;
+  FixEPHProbe *fix = nullptr;
+
+  double skin = 1.0, cutneigh = 0.0;
+  std::vector<int> ghost_owner;
+  std::vector<int> ghost_shift;  // 3 per ghost, values -1, 0, +1
+  std::vector<double> xhold;
+  std::vector<double> fext;
+  std::vector<int> numneigh;
+  std::vector<int *> firstneigh;
+  std::vector<std::vector<int>> neigh;
+  std::vector<double> commbuf;
+  long nbuild = 0;
+
+  Sim() {
+    lmp.atom = &atom;
+    lmp.domain = &domain;
+    lmp.neighbor = &neighbor;
+    lmp.memory = &memory;
+    lmp.force = &force;
+    lmp.update = &update;
+    lmp.comm = &comm;
+    lmp.error = &error;
+  }
+  ~Sim() {
+    delete fix;
+    memory.destroy(atom.x);
+    memory.destroy(atom.v);
+    memory.destroy(atom.f);
+    memory.destroy(atom.type);
+    memory.destroy(atom.mask);
+    memory.destroy(atom.mass);
+  }
+
+  void grow_atoms(int n) {
+    if (n <= atom.nmax) return;
+    atom.nmax = n;
+    memory.grow(atom.x, n, 3, "x");
+    memory.grow(atom.v, n, 3, "v");
+    memory.grow(atom.f, n, 3, "f");
+    memory.grow(atom.type, n, "type");
+    memory.grow(atom.mask, n, "mask");
+    commbuf.resize((size_t)3 * n);
+    comm.buf = commbuf.data();
+    if (fix) fix->grow_arrays(n);
+  }
+
+  // Domain::pbc for an orthogonal periodic box.
+  void pbc() {
+    for (int i = 0; i < atom.nlocal; ++i)
+      for (int k = 0; k < 3; ++k) {
+        double &c = atom.x[i][k];
+        if (c < domain.boxlo[k]) c += domain.prd[k];
+        if (c >= domain.boxhi[k]) {
+          c -= domain.prd[k];
+          c = std::max(c, domain.boxlo[k]);
+        }
+      }
+  }
+
+  // Ghosts: every periodic image of a local atom that falls inside the box
+  // grown by the neighbour cutoff on each side.
+  void borders() {
+    const int nlocal = atom.nlocal;
+    ghost_owner.clear();
+    ghost_shift.clear();
+    std::vector<double> gx;
+    for (int i = 0; i < nlocal; ++i)
+      for (int sz = -1; sz <= 1; ++sz)
+        for (int sy = -1; sy <= 1; ++sy)
+          for (int sx = -1; sx <= 1; ++sx) {
+            if (!sx && !sy && !sz) continue;
+            const int s[3] = {sx, sy, sz};
+            double c[3];
+            bool inside = true;
+            for (int k = 0; k < 3; ++k) {
+              c[k] = atom.x[i][k];
+              if (s[k] > 0) c[k] = atom.x[i][k] + domain.prd[k];
+              if (s[k] < 0) c[k] = atom.x[i][k] + (-domain.prd[k]);
+              if (!(c[k] >= domain.boxlo[k] - cutneigh && c[k] < domain.boxhi[k] + cutneigh)) inside = false;
+            }
+            if (!inside) continue;
+            ghost_owner.push_back(i);
+            ghost_shift.insert(ghost_shift.end(), s, s + 3);
+            gx.insert(gx.end(), c, c + 3);
+          }
+    const int ng = (int)ghost_owner.size();
+    grow_atoms(nlocal + ng + 1);
+    atom.nghost = ng;
+    for (int g = 0; g < ng; ++g) {
+      const int j = nlocal + g, o = ghost_owner[g];
+      for (int k = 0; k < 3; ++k) {
+        atom.x[j][k] = gx[3 * g + k];
+        atom.v[j][k] = atom.v[o][k];
+      }
+      atom.type[j] = atom.type[o];
+      atom.mask[j] = atom.mask[o];
+    }
+    comm.ghost_owner = ghost_owner.data();
+    comm.nghost = ng;
+    comm.nlocal = nlocal;
+  }
+
+  // Owner x, v to ghosts (forward communication with ghost_velocity = 1).
+  void forward_xv() {
+    const int nlocal = atom.nlocal;
+    for (int g = 0; g < atom.nghost; ++g) {
+      const int j = nlocal + g, o = ghost_owner[g];
+      for (int k = 0; k < 3; ++k) {
+        const int s = ghost_shift[3 * g + k];
+        double c = atom.x[o][k];
+        if (s > 0) c = atom.x[o][k] + domain.prd[k];
+        if (s < 0) c = atom.x[o][k] + (-domain.prd[k]);
+        atom.x[j][k] = c;
+        atom.v[j][k] = atom.v[o][k];
+      }
+    }
+  }
+
+  int owner(int j) const { return j < atom.nlocal ? j : ghost_owner[j - atom.nlocal]; }
+
+  // Full list of every local atom, neighbours ordered by owner index.
+  void build_list() {
+    const int nlocal = atom.nlocal, ntot = nlocal + atom.nghost;
+    const double cutsq = cutneigh * cutneigh;
+    // bin all atoms (local + ghost) on a grid of cells of edge >= cutneigh
+    double lo[3], w[3];
+    int nb[3];
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = domain.boxlo[k] - cutneigh;
+      const double ext = domain.prd[k] + 2.0 * cutneigh;
+      nb[k] = std::max(1, (int)(ext / cutneigh));
+      w[k] = ext / nb[k];
+    }
+    auto bin_of = [&](const double *c, int *b) {
+      for (int k = 0; k < 3; ++k) {
+        int v = (int)std::floor((c[k] - lo[k]) / w[k]);
+        b[k] = std::min(std::max(v, 0), nb[k] - 1);
+      }
+    };
+    std::vector<std::vector<int>> bins((size_t)nb[0] * nb[1] * nb[2]);
+    for (int j = 0; j < ntot; ++j) {
+      int b[3];
+      bin_of(atom.x[j], b);
+      bins[(size_t)b[0] + (size_t)nb[0] * (b[1] + (size_t)nb[1] * b[2])].push_back(j);
+    }
+    neigh.assign(nlocal, {});
+    numneigh.assign(nlocal, 0);
+    firstneigh.assign(nlocal, nullptr);
+    for (int i = 0; i < nlocal; ++i) {
+      int b[3];
+      bin_of(atom.x[i], b);
+      std::vector<std::pair<int, int>> cand;
+      for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int c0 = b[0] + dx, c1 = b[1] + dy, c2 = b[2] + dz;
+            if (c0 < 0 || c1 < 0 || c2 < 0 || c0 >= nb[0] || c1 >= nb[1] || c2 >= nb[2]) continue;
+            for (int j : bins[(size_t)c0 + (size_t)nb[0] * (c1 + (size_t)nb[1] * c2)]) {
+              if (j == i) continue;
+              const double ex = atom.x[j][0] - atom.x[i][0];
+              const double ey = atom.x[j][1] - atom.x[i][1];
+              const double ez = atom.x[j][2] - atom.x[i][2];
+              const double rsq = ex * ex + ey * ey + ez * ez;
+              if (rsq < cutsq) cand.emplace_back(owner(j), j);
+            }
+          }
+      std::sort(cand.begin(), cand.end());
+      for (size_t c = 1; c < cand.size(); ++c)
+        if (cand[c].first == cand[c - 1].first)
+          throw std::runtime_error("two images of one atom in a list: box narrower than 2*(rc+skin)");
+      for (auto &p : cand) neigh[i].push_back(p.second);
+      numneigh[i] = (int)neigh[i].size();
+      firstneigh[i] = neigh[i].data();
+    }
+    list.inum = nlocal;
+    list.numneigh = numneigh.data();
+    list.firstneigh = firstneigh.data();
+    xhold.assign((size_t)3 * nlocal, 0.0);
+    for (int i = 0; i < nlocal; ++i)
+      for (int k = 0; k < 3; ++k) xhold[3 * (size_t)i + k] = atom.x[i][k];
+    ++nbuild;
+  }
+
+  bool decide() const {
+    const double triggersq = 0.25 * skin * skin;
+    for (int i = 0; i < atom.nlocal; ++i) {
+      const double dx = atom.x[i][0] - xhold[3 * (size_t)i + 0];
+      const double dy = atom.x[i][1] - xhold[3 * (size_t)i + 1];
+      const double dz = atom.x[i][2] - xhold[3 * (size_t)i + 2];
+      if (dx * dx + dy * dy + dz * dz > triggersq) return true;
+    }
+    return false;
+  }
+
+  void reneighbor() {
+    pbc();
+    borders();
+    build_list();
+  }
+
+  void clear_forces() {
+    const int ntot = atom.nlocal + atom.nghost;
+    for (int i = 0; i < ntot; ++i)
+      for (int k = 0; k < 3; ++k) atom.f[i][k] = 0.0;
+    if (!fext.empty())
+      for (int i = 0; i < atom.nlocal; ++i)
+        for (int k = 0; k < 3; ++k) atom.f[i][k] = fext[3 * (size_t)i + k];
+  }
+};
+
+void copy_err(const char *msg, char *errbuf, int errlen) {
+  if (errbuf && errlen > 0) {
+    std::strncpy(errbuf, msg, (size_t)errlen - 1);
+    errbuf[errlen - 1] = 0;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Build the engine with `nlocal` atoms and construct the reference fix from
+ * the fix command's words (arg[0] = fix ID, arg[1] = group, arg[2] = "eph",
+ * then the reference's positional arguments, fix_eph.cpp:36-58).
+ * mass[1..ntypes] are per-type masses.  Returns NULL on error. */
+void *ref_create(int narg, const char **arg, int nlocal, const double *x, const double *v, const int *type,
+                 const int *mask, int ntypes, const double *mass, const double *lo, const double *hi, double dt,
+                 double boltz, double ftm2v, double skin, char *errbuf, int errlen) {
+  Sim *s = new Sim();
+  try {
+    s->domain.set_box(lo, hi);
+    s->update.dt = dt;
+    s->force.boltz = boltz;
+    s->force.ftm2v = ftm2v;
+    s->skin = skin;
+    s->atom.ntypes = ntypes;
+    s->atom.natoms = nlocal;
+    s->atom.nlocal = nlocal;
+    s->memory.grow(s->atom.mass, ntypes + 1, "mass");
+    for (int t = 0; t <= ntypes; ++t) s->atom.mass[t] = mass[t];
+    s->grow_atoms(std::max(nlocal, 1));
+    for (int i = 0; i < nlocal; ++i) {
+      for (int k = 0; k < 3; ++k) {
+        s->atom.x[i][k] = x[3 * (size_t)i + k];
+        s->atom.v[i][k] = v[3 * (size_t)i + k];
+        s->atom.f[i][k] = 0.0;
+      }
+      s->atom.type[i] = type[i];
+      s->atom.mask[i] = mask ? mask[i] : 1;
+    }
+    std::vector<std::string> words(arg, arg + narg);
+    std::vector<char *> argv;
+    for (auto &w : words) argv.push_back(&w[0]);
+    s->fix = new FixEPHProbe(&s->lmp, narg, argv.data());
+    s->fix->init();
+    if (s->neighbor.nrequest != 1) throw std::runtime_error("fix did not request a neighbour list");
+    s->cutneigh = s->neighbor.request.cutoff + skin;
+    s->fix->init_list(0, &s->list);
+    // Verlet::setup
+    s->reneighbor();
+    s->fix->grow_arrays(s->atom.nmax);
+    s->clear_forces();
+  } catch (std::exception &e) {
+    copy_err(e.what(), errbuf, errlen);
+    delete s;
+    return nullptr;
+  }
+  return s;
+}
+
+void ref_destroy(void *h) { delete static_cast<Sim *>(h); }
+
+/* Per-atom constant external force (stands in for the pair style); NULL = 0. */
+int ref_set_fext(void *h, const double *fext) {
+  Sim *s = static_cast<Sim *>(h);
+  if (fext)
+    s->fext.assign(fext, fext + 3 * (size_t)s->atom.nlocal);
+  else
+    s->fext.clear();
+  s->clear_forces();
+  return 0;
+}
+
+/* One Verlet step.  `xi` holds the deviates RanMars::gaussian() returns this
+ * step, in draw order (nxi values); pass NULL when the fix draws none. */
+int ref_step(void *h, const double *xi, long nxi, char *errbuf, int errlen) {
+  Sim *s = static_cast<Sim *>(h);
+  try {
+    s->update.ntimestep += 1;
+    s->fix->initial_integrate(0);
+    if (s->decide())
+      s->reneighbor();
+    else
+      s->forward_xv();
+    s->clear_forces();
+    RanMars *r = s->fix->rng();
+    r->stream = xi;
+    r->count = xi ? nxi : 0;
+    r->pos = 0;
+    s->fix->post_force(0);
+    if (xi && r->pos != nxi) throw std::runtime_error("fix drew a different number of deviates than injected");
+    s->fix->final_integrate();
+    s->fix->end_of_step();
+  } catch (std::exception &e) {
+    copy_err(e.what(), errbuf, errlen);
+    return 1;
+  }
+  return 0;
+}
+
+/* Copy a per-atom quantity of the locals into out:
+ * "x","v","f","f_eph","f_rng","w","xi" (3 per atom), "rho" (1 per atom),
+ * "array" (8 per atom), "vector" (2 values: compute_vector(0), (1)). */
+int ref_get(void *h, const char *what, double *out) {
+  Sim *s = static_cast<Sim *>(h);
+  const int n = s->atom.nlocal;
+  auto rows3 = [&](double **a) {
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) out[3 * (size_t)i + k] = a[i][k];
+  };
+  const std::string w(what);
+  if (w == "x") rows3(s->atom.x);
+  else if (w == "v") rows3(s->atom.v);
+  else if (w == "f") rows3(s->atom.f);
+  else if (w == "f_eph") rows3(s->fix->feph());
+  else if (w == "f_rng") rows3(s->fix->frng());
+  else if (w == "w") rows3(s->fix->w());
+  else if (w == "xi") rows3(s->fix->xi());
+  else if (w == "rho") {
+    for (int i = 0; i < n; ++i) out[i] = s->fix->rho()[i];
+  } else if (w == "array") {
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 8; ++k) out[8 * (size_t)i + k] = s->fix->arr()[i][k];
+  } else if (w == "vector") {
+    out[0] = s->fix->compute_vector(0);
+    out[1] = s->fix->compute_vector(1);
+  } else
+    return 1;
+  return 0;
+}
+
+/* Electronic temperature of every grid cell, read at the cell centres of an
+ * nx*ny*nz grid spanning [lo, hi); index i + j*nx + k*nx*ny. */
+int ref_get_T(void *h, int nx, int ny, int nz, const double *lo, const double *hi, double *out) {
+  Sim *s = static_cast<Sim *>(h);
+  const double dx = (hi[0] - lo[0]) / nx, dy = (hi[1] - lo[1]) / ny, dz = (hi[2] - lo[2]) / nz;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        out[i + (size_t)nx * (j + (size_t)ny * k)] =
+            s->fix->T_at(lo[0] + (i + 0.5) * dx, lo[1] + (j + 0.5) * dy, lo[2] + (k + 0.5) * dz);
+  return 0;
+}
+
+/* The current full list: numneigh[i] and the owner index of each neighbour,
+ * row i at neigh[i*maxn ...].  Returns the largest count (fills nothing
+ * beyond maxn). */
+int ref_get_neigh(void *h, int *numneigh, int *owners, int maxn) {
+  Sim *s = static_cast<Sim *>(h);
+  int mx = 0;
+  for (int i = 0; i < s->atom.nlocal; ++i) {
+    const int c = s->numneigh[i];
+    mx = std::max(mx, c);
+    numneigh[i] = c;
+    for (int k = 0; k < c && k < maxn; ++k) owners[(size_t)i * maxn + k] = s->owner(s->neigh[i][k]);
+  }
+  return mx;
+}
+
+long ref_nbuild(void *h) { return static_cast<Sim *>(h)->nbuild; }
+
+int ref_save_temperature(void *h, const char *path, int n) {
+  static_cast<Sim *>(h)->fix->save_T(path, n);
+  return 0;
+}
+
+int ref_save_state(void *h, const char *path) {
+  static_cast<Sim *>(h)->fix->save_state(path);
+  return 0;
+}
+
+}  // extern "C"
+
+/* ----------------------------------------------------------------------
+ * The reference parametrisation and grid classes on their own
+ * (eph_beta.h, eph_spline.h, eph_fdm.h), for table-level comparisons.
+ * ---------------------------------------------------------------------- */
+namespace {
+// Read access to the protected coefficient tables (layout-identical views).
+struct SplineView : Spline {
+  static const std::vector<Coefficients> &coeffs(const Spline &s) { return static_cast<const SplineView &>(s).c; }
+  static size_t coeff_size() { return sizeof(Coefficients); }
+};
+struct BetaView : Beta {
+  static const Spline &table(const Beta &b, int which, int e) {
+    const BetaView &v = static_cast<const BetaView &>(b);
+    switch (which) {
+      case 0: return v.rho[e];
+      case 1: return v.rho_r_sq[e];
+      case 2: return v.beta[e];
+      default: return v.alpha[e];
+    }
+  }
+};
+}  // namespace
+
+extern "C" {
+
+void *refb_load(const char *path) { return new Beta(path); }
+void refb_free(void *b) { delete static_cast<Beta *>(b); }
+int refb_n_elements(void *b) { return (int)static_cast<Beta *>(b)->get_n_elements(); }
+double refb_r_cutoff(void *b) { return static_cast<Beta *>(b)->get_r_cutoff(); }
+double refb_rho_cutoff(void *b) { return static_cast<Beta *>(b)->get_rho_cutoff(); }
+
+/* which: 0 rho(r), 1 rho(r^2), 2 beta(rho) via get_beta, 3 alpha(rho) via get_alpha */
+double refb_eval(void *h, int which, int elem, double x) {
+  Beta *b = static_cast<Beta *>(h);
+  switch (which) {
+    case 0: return b->get_rho(elem, x);
+    case 1: return b->get_rho_r_sq(elem, x);
+    case 2: return b->get_beta(elem, x);
+    default: return b->get_alpha(elem, x);
+  }
+}
+
+long refb_table(void *h, int which, int elem, double *out) {
+  const Spline &s = BetaView::table(*static_cast<Beta *>(h), which, elem);
+  const auto &c = SplineView::coeffs(s);
+  if (out) std::memcpy(out, c.data(), c.size() * SplineView::coeff_size());
+  return (long)c.size();
+}
+
+void *refg_create(long nx, long ny, long nz, const double *lo, const double *hi, double T, double Ce, double rho,
+                  double kappa) {
+  EPH_FDM *g = new EPH_FDM(nx, ny, nz, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], T, Ce, rho, kappa);
+  g->set_comm(0, 0, 1);
+  return g;
+}
+void *refg_load(const char *path) {
+  EPH_FDM *g = new EPH_FDM(path);
+  g->set_comm(0, 0, 1);
+  return g;
+}
+void refg_free(void *g) { delete static_cast<EPH_FDM *>(g); }
+void refg_set_dt(void *g, double dt) { static_cast<EPH_FDM *>(g)->set_dt(dt); }
+void refg_insert_energy(void *g, double x, double y, double z, double E) {
+  static_cast<EPH_FDM *>(g)->insert_energy(x, y, z, E);
+}
+double refg_get_T(void *g, double x, double y, double z) { return static_cast<EPH_FDM *>(g)->get_T(x, y, z); }
+double refg_get_T_total(void *g) { return static_cast<EPH_FDM *>(g)->get_T_total(); }
+void refg_solve(void *g) { static_cast<EPH_FDM *>(g)->solve(); }
+void refg_save_state(void *g, const char *path) { static_cast<EPH_FDM *>(g)->save_state(path); }
+void refg_save_temperature(void *g, const char *path, int n) {
+  static_cast<EPH_FDM *>(g)->save_temperature(path, n);
+}
+
+}  // extern "C"

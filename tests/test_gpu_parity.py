@@ -1,0 +1,102 @@
+"""CUDA path (libephgb.so through the C ABI) against the CPU oracle on the
+same seeded inputs and the same injected deviates.
+
+EXACT mode keeps the reference's expression order without FMA: on the first
+step every per-atom array is bit-identical to the oracle; the grid sums its
+deposits exactly (fixed point) instead of in atom order, so T_e (and from the
+second step on everything that depends on T_e) agrees to rounding.  FAST mode
+factors alpha/rho and rho(r^2)/r^2 and uses FMA.  Tolerance for both: the
+spec bar, 1e-12 relative, norm-wise (max |a - b| / max |b|) per array."""
+import numpy as np
+import pytest
+
+import ephgb
+from ephgb import workloads as W
+from helpers import SCENARIOS, n_in_group, rel_err, scenario, xi_rows
+from oracle.bindings import OracleFix
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+ATOM_KEYS = ("rho", "w", "f_eph", "f_rng", "f", "x", "v", "array")
+
+
+def run_pair(words, at, dt, mode, steps, check, seed=5):
+    gpu = ephgb.FixEPH(words, at, dt=dt, mode=mode)
+    ref = OracleFix(words, at, dt)
+    ng = n_in_group(at)
+    rnd = int(words[4], 0) & 2
+    for s in range(steps):
+        stream = W.gaussian_stream(ng, seed, s) if rnd else None
+        if rnd:
+            gpu.step(1, xi=xi_rows(at, stream))
+        else:
+            gpu.step(1)
+        ref.step(stream)
+        check(s, gpu, ref)
+    gpu.synchronize()
+    return gpu, ref
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_exact_mode_bitwise_first_step(built, beta_file, beta_file_2el, name):
+    words, at, dt = scenario(name, beta_file, beta_file_2el)
+
+    def check(s, gpu, ref):
+        for k in ATOM_KEYS:
+            a, b = gpu.get(k), ref.get(k)
+            if s == 0:
+                assert np.array_equal(a, b), (k, rel_err(a, b))
+            else:
+                assert rel_err(a, b) <= TOL, (s, k, rel_err(a, b))
+        assert rel_err(gpu.get("T"), ref.get("T")) <= TOL
+        Ee_g, Ee_r = gpu.compute_vector(0), ref.get("vector")[0]
+        scale = max(abs(Ee_r), np.abs(ref.get("f_eph")).max() * 1e-3 + 1e-300)
+        assert abs(Ee_g - Ee_r) <= TOL * scale * at.n
+        assert abs(gpu.compute_vector(1) - ref.get("vector")[1]) <= TOL * abs(ref.get("vector")[1])
+
+    run_pair(words, at, dt, ephgb.MODE_EXACT, 6 if name != "pka" else 30, check)
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_fast_mode_within_tolerance(built, beta_file, beta_file_2el, name):
+    words, at, dt = scenario(name, beta_file, beta_file_2el)
+
+    def check(s, gpu, ref):
+        for k in ATOM_KEYS:
+            assert rel_err(gpu.get(k), ref.get(k)) <= TOL, (s, k, rel_err(gpu.get(k), ref.get(k)))
+        assert rel_err(gpu.get("T"), ref.get("T")) <= TOL
+
+    run_pair(words, at, dt, ephgb.MODE_FAST, 6 if name != "pka" else 30, check)
+
+
+def test_c1_config_fast_and_exact(built, beta_file):
+    """BASELINE configs[0] (4,000 atoms, 10^3 grid) for 20 steps."""
+    words, at, dt = scenario("c1", beta_file)
+    for mode in (ephgb.MODE_EXACT, ephgb.MODE_FAST):
+        def check(s, gpu, ref):
+            if s in (0, 9, 19):
+                for k in ATOM_KEYS:
+                    assert rel_err(gpu.get(k), ref.get(k)) <= TOL, (mode, s, k)
+                assert rel_err(gpu.get("T"), ref.get("T")) <= TOL
+
+        run_pair(words, at, dt, mode, 20, check)
+
+
+def test_hook_sequence_matches_step(built, beta_file):
+    """Driving the four hooks one by one equals eph_step (no wrap needed at
+    300 K over a few steps)."""
+    words, at, dt = scenario("c1_small", beta_file)
+    a = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_EXACT)
+    b = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_EXACT)
+    for s in range(3):
+        xi = xi_rows(at, W.gaussian_stream(at.n, 9, s))
+        a.step(1, xi=xi)
+        b.set_timestep(s + 1)
+        b.initial_integrate()
+        b.put("f", np.zeros((at.n, 3)))
+        b.post_force(xi=xi)
+        b.final_integrate()
+        b.end_of_step()
+        for k in ATOM_KEYS:
+            assert np.array_equal(a.get(k), b.get(k)), (s, k)
+        assert np.array_equal(a.get("T"), b.get("T"))

@@ -1,0 +1,989 @@
+// Context, launches and the C ABI (include/eph_gb.h) of the GB300 fix-eph
+// path.  One context = one fix instance on one GPU; all its work is ordered
+// on one CUDA stream.  Device layout (n atoms, K = pair capacity):
+//   x, v, f, xhold, f_eph, f_rng, xi   D4[n]       (x.w holds the element index)
+//   A, Bw                              D4[n]       per-atom records read by neighbours
+//   pj, pe, pg                         [K][n]      in-cutoff pairs of the step
+//   bins                               [nbins][bcap] BinEntry
+//   grid T (two buffers), kappa, rho_e*C_e, S, flag, dT, fixed-point deposits
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "eph_gb.h"
+#include "eph_host.hpp"
+#include "eph_kernels.cuh"
+
+using namespace ephgb;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, sizeof(T) * count);
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DevBuf() { free(); }
+};
+
+constexpr int BLOCK = 128;
+inline int nblocks(long n, int b = BLOCK) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+struct eph_ctx {
+  std::string err;
+  int device = 0;
+  cudaStream_t stream = 0;
+  bool own_stream = false;
+
+  FixArgs args;
+  Beta beta;
+  Grid grid;  // host copy: geometry and parameters (T lives on the device)
+  int ntypes = 0;
+  std::vector<double> mass;
+  std::vector<int> type_map;  // by LAMMPS type 1..ntypes
+  double boxlo[3], boxhi[3], prd[3];
+  double dt = 0, boltz = 0, ftm2v = 0, skin = 0;
+  int groupbit = 1, mode = EPH_MODE_FAST;
+  long ntimestep = 0;
+  unsigned long long rng_step = 0;
+
+  StepParams P{};
+  bool multi = false;
+
+  int n = 0;
+  DevBuf<D4> x, v, f, xhold, f_eph, f_rng, xi, fext, A, Bw;
+  bool have_fext = false, have_xi = false;
+  DevBuf<int> type, mask, nshort, cell, tmap;
+  DevBuf<double> rho, beta_i, Te_i, stage;
+  DevBuf<int> bin_count;
+  DevBuf<BinEntry> bins;
+  DevBuf<int4> atom_bin;
+  DevBuf<float4> atom_off;
+  DevBuf<unsigned> pj;
+  DevBuf<D4> pe;
+  DevBuf<double2> pg;
+  int nbins = 0, bcap = 0, kcap = 0;
+
+  DevBuf<D4> tab_rho_r_sq, tab_beta, tab_alpha;
+
+  DevBuf<double> T0, T1, kappa, rhoC, S, dT;
+  DevBuf<signed char> gflag;
+  DevBuf<U128> acc, part, gsum;
+  unsigned nsub = 1;
+  double inner_dt = 0;
+
+  // per-phase CUDA-event timing (eph_set_profiling) and launch counts
+  bool profiling = false;
+  struct Mark {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> event_pool;
+  double phase_ms[EPH_NPHASES] = {0};
+  long phase_launches[EPH_NPHASES] = {0};
+  long launches = 0;
+
+  DevBuf<double> scal;  // 0 Ee, 1 E_local, 2 T_total
+  DevBuf<unsigned> d_err;
+  DevBuf<unsigned long long> counters;
+  DevBuf<int> wrapflag;
+  unsigned *h_err = nullptr;  // pinned
+};
+
+namespace {
+
+int fail(eph_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                           \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess) return fail((ctx), EPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int upload_tables(eph_ctx *c) {
+  const Beta &b = c->beta;
+  auto up = [&](DevBuf<D4> &dst, int which, long nk) -> cudaError_t {
+    std::vector<double> h((size_t)b.n_elements * nk * 4);
+    for (int e = 0; e < b.n_elements; ++e) {
+      const Spline &s = b.table(which, e);
+      std::memcpy(&h[(size_t)e * nk * 4], s.c.data(), sizeof(double) * 4 * nk);
+    }
+    cudaError_t r = dst.alloc((size_t)b.n_elements * nk);
+    if (r != cudaSuccess) return r;
+    return cudaMemcpy(dst.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  };
+  CUDA_TRY(c, up(c->tab_rho_r_sq, EPH_SPLINE_RHO_R_SQ, b.n_rho));
+  CUDA_TRY(c, up(c->tab_beta, EPH_SPLINE_BETA, b.n_beta));
+  CUDA_TRY(c, up(c->tab_alpha, EPH_SPLINE_ALPHA, b.n_beta));
+  return EPH_OK;
+}
+
+int upload_grid(eph_ctx *c) {
+  Grid &g = c->grid;
+  const size_t nc = (size_t)g.ntotal;
+  CUDA_TRY(c, c->T0.alloc(nc));
+  CUDA_TRY(c, c->T1.alloc(nc));
+  CUDA_TRY(c, c->kappa.alloc(nc));
+  CUDA_TRY(c, c->rhoC.alloc(nc));
+  CUDA_TRY(c, c->S.alloc(nc));
+  CUDA_TRY(c, c->dT.alloc(nc));
+  CUDA_TRY(c, c->gflag.alloc(nc));
+  CUDA_TRY(c, c->acc.alloc(nc));
+  std::vector<double> rc(nc);
+  std::vector<signed char> fl(nc);
+  for (size_t i = 0; i < nc; ++i) {
+    rc[i] = g.rho[i] * g.C[i];  // eph_fdm.h:372 prescaler
+    fl[i] = (signed char)g.flag[i];
+  }
+  CUDA_TRY(c, cudaMemcpy(c->T0.p, g.T.data(), nc * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->kappa.p, g.kappa.data(), nc * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->rhoC.p, rc.data(), nc * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->S.p, g.S.data(), nc * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->gflag.p, fl.data(), nc, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemset(c->dT.p, 0, nc * 8));
+  CUDA_TRY(c, cudaMemset(c->acc.p, 0, nc * sizeof(U128)));
+  return EPH_OK;
+}
+
+void set_time_params(eph_ctx *c) {
+  // fix_eph.cpp:200-205 and reset_dt (:909-916)
+  c->P.eta = std::sqrt(2.0 * c->boltz / c->dt);
+  c->P.dtv = c->dt;
+  c->P.dt = c->dt;
+  const double dtf = 0.5 * c->dt * c->ftm2v;
+  for (int t = 1; t <= c->ntypes; ++t) c->P.dtfm[t] = dtf / c->mass[t];
+  c->grid.dt = c->dt;  // EPH_FDM::set_dt
+  c->nsub = c->grid.substeps(&c->inner_dt);
+  c->P.prescale = c->grid.dV * c->dt;
+}
+
+// read back the device error word; returns EPH_OK or the matching status
+int check_device(eph_ctx *c) {
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_err, c->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const unsigned e = *c->h_err;
+  if (!e) return EPH_OK;
+  cudaMemsetAsync(c->d_err.p, 0, sizeof(unsigned), c->stream);
+  if (e & (ERR_BIN_OVERFLOW | ERR_PAIR_OVERFLOW))
+    return fail(c, EPH_ERR_CAPACITY,
+                std::string("device: ") + ((e & ERR_BIN_OVERFLOW) ? "bin capacity exceeded " : "") +
+                    ((e & ERR_PAIR_OVERFLOW) ? "pair capacity exceeded" : ""));
+  if (e & ERR_TIMEOUT) return fail(c, EPH_ERR_TIMEOUT, "device: a bounded wait gave up");
+  if (e & ERR_DRIFT) return fail(c, EPH_ERR_RANGE, "device: an atom drifted more than one bin outside the box");
+  if (e & ERR_SPLINE_RANGE) return fail(c, EPH_ERR_RANGE, "device: spline argument outside its table");
+  return fail(c, EPH_ERR_RANGE, "device: energy deposit outside the fixed-point range");
+}
+
+cudaEvent_t take_event(eph_ctx *c) {
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets the launches of one phase with CUDA events on the context's
+// stream when profiling is on; counts the kernel launches either way.
+struct PhaseScope {
+  eph_ctx *c;
+  int phase;
+  cudaEvent_t b = nullptr;
+  PhaseScope(eph_ctx *ctx, int ph) : c(ctx), phase(ph) {
+    if (c->profiling) {
+      b = take_event(c);
+      cudaEventRecord(b, c->stream);
+    }
+  }
+  void launched(int k = 1) {
+    c->launches += k;
+    c->phase_launches[phase] += k;
+  }
+  ~PhaseScope() {
+    if (c->profiling && b) {
+      cudaEvent_t e = take_event(c);
+      cudaEventRecord(e, c->stream);
+      c->marks.push_back({phase, b, e});
+    }
+  }
+};
+
+void collect_marks(eph_ctx *c) {
+  for (auto &m : c->marks) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, m.a, m.b) == cudaSuccess) c->phase_ms[m.phase] += ms;
+    c->event_pool.push_back(m.a);
+    c->event_pool.push_back(m.b);
+  }
+  c->marks.clear();
+}
+
+int require_atoms(eph_ctx *c) {
+  if (c->n <= 0) return fail(c, EPH_ERR_STATE, "no atoms: call eph_set_atoms first");
+  return EPH_OK;
+}
+
+// --------------------------------------------------------------- launches
+
+int launch_initial(eph_ctx *c, int check_wrap) {
+  PhaseScope ps(c, EPH_PHASE_INTEGRATE);
+  ps.launched();
+  const int nb = nblocks(c->n);
+  if (c->mode == EPH_MODE_FAST)
+    k_initial_integrate<true><<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->v.p, c->f.p, c->type.p, c->mask.p,
+                                                           c->xhold.p, check_wrap, c->wrapflag.p);
+  else
+    k_initial_integrate<false><<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->v.p, c->f.p, c->type.p, c->mask.p,
+                                                            c->xhold.p, check_wrap, c->wrapflag.p);
+  CUDA_TRY(c, cudaGetLastError());
+  return EPH_OK;
+}
+
+int launch_final(eph_ctx *c) {
+  PhaseScope ps(c, EPH_PHASE_INTEGRATE);
+  ps.launched();
+  const int nb = nblocks(c->n);
+  if (c->mode == EPH_MODE_FAST)
+    k_final_integrate<true><<<nb, BLOCK, 0, c->stream>>>(c->P, c->v.p, c->f.p, c->type.p, c->mask.p);
+  else
+    k_final_integrate<false><<<nb, BLOCK, 0, c->stream>>>(c->P, c->v.p, c->f.p, c->type.p, c->mask.p);
+  CUDA_TRY(c, cudaGetLastError());
+  return EPH_OK;
+}
+
+template <bool FAST, bool MULTI>
+void launch_density_t(eph_ctx *c, int xi_mode) {
+  k_density<FAST, MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+      c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p,
+      c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,
+      c->wrapflag.p, c->d_err.p, c->counters.p);
+}
+
+template <bool FAST, bool MULTI, bool FRIC, bool RAND>
+void launch_forces_t(eph_ctx *c) {
+  k_forces<FAST, MULTI, FRIC, RAND><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+      c->P, c->mask.p, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->Te_i.p, c->f.p, c->f_eph.p,
+      c->f_rng.p);
+}
+
+template <bool FAST, bool MULTI>
+void launch_forces_m(eph_ctx *c) {
+  const bool fr = c->P.flags & FLAG_FRICTION, ra = c->P.flags & FLAG_RANDOM;
+  if (fr && ra) launch_forces_t<FAST, MULTI, true, true>(c);
+  else if (fr) launch_forces_t<FAST, MULTI, true, false>(c);
+  else if (ra) launch_forces_t<FAST, MULTI, false, true>(c);
+  else launch_forces_t<FAST, MULTI, false, false>(c);
+}
+
+// post_force: bins, density, friction pre-vector, forces
+int launch_post_force(eph_ctx *c, int xi_mode) {
+  const int nb = nblocks(c->n);
+  c->P.step = c->rng_step;
+  {
+    PhaseScope ps(c, EPH_PHASE_BIN);
+    ps.launched();
+    CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
+    k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
+                                       c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p);
+  }
+  const bool fast = c->mode == EPH_MODE_FAST;
+  {
+    PhaseScope ps(c, EPH_PHASE_DENSITY);
+    ps.launched();
+    if (fast) {
+      if (c->multi) launch_density_t<true, true>(c, xi_mode);
+      else launch_density_t<true, false>(c, xi_mode);
+    } else {
+      if (c->multi) launch_density_t<false, true>(c, xi_mode);
+      else launch_density_t<false, false>(c, xi_mode);
+    }
+  }
+  if (c->P.flags & FLAG_FRICTION) {
+    PhaseScope ps(c, EPH_PHASE_FRICTION_W);
+    ps.launched();
+    if (fast)
+      k_friction_w<true><<<nb, BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
+                                                      c->nshort.p, c->A.p, c->Bw.p);
+    else
+      k_friction_w<false><<<nb, BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
+                                                       c->nshort.p, c->A.p, c->Bw.p);
+  }
+  {
+    PhaseScope ps(c, EPH_PHASE_FORCES);
+    ps.launched();
+    if (fast) {
+      if (c->multi) launch_forces_m<true, true>(c);
+      else launch_forces_m<true, false>(c);
+    } else {
+      if (c->multi) launch_forces_m<false, true>(c);
+      else launch_forces_m<false, false>(c);
+    }
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  c->rng_step += 1;
+  return EPH_OK;
+}
+
+template <bool FRIC, bool RAND, bool GRID>
+void launch_deposit_t(eph_ctx *c) {
+  k_deposit<FRIC, RAND, GRID><<<nblocks(c->n, 256), 256, 0, c->stream>>>(
+      c->P, c->mask.p, c->v.p, c->f_eph.p, c->f_rng.p, c->cell.p, c->acc.p, c->part.p, c->d_err.p);
+}
+
+// end_of_step: deposits, FDM substeps, energy total
+int launch_end_of_step(eph_ctx *c) {
+  const bool fr = c->P.flags & FLAG_FRICTION, ra = c->P.flags & FLAG_RANDOM, gr = c->P.flags & FLAG_FDM;
+  if (fr || ra) {
+    PhaseScope ps(c, EPH_PHASE_DEPOSIT);
+    ps.launched(2);
+    if (fr && ra) {
+      if (gr) launch_deposit_t<true, true, true>(c);
+      else launch_deposit_t<true, true, false>(c);
+    } else if (fr) {
+      if (gr) launch_deposit_t<true, false, true>(c);
+      else launch_deposit_t<true, false, false>(c);
+    } else {
+      if (gr) launch_deposit_t<false, true, true>(c);
+      else launch_deposit_t<false, true, false>(c);
+    }
+    k_energy_total<<<1, 1024, 0, c->stream>>>(c->part.p, nblocks(c->n, 256), c->scal.p + 1, c->scal.p + 0);
+  }
+  if (gr) {
+    PhaseScope ps(c, EPH_PHASE_FDM);
+    ps.launched((int)c->nsub);
+    const Grid &g = c->grid;
+    double *src = c->T0.p, *dst = c->T1.p;
+    for (unsigned s = 0; s < c->nsub; ++s) {
+      k_fdm_substep<<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt,
+                                                                 src, dst, c->kappa.p, c->rhoC.p, c->S.p,
+                                                                 c->gflag.p, c->dT.p, c->acc.p, s == 0,
+                                                                 c->counters.p);
+      std::swap(src, dst);
+    }
+    if (src != c->T0.p)
+      CUDA_TRY(c, cudaMemcpyAsync(c->T0.p, src, sizeof(double) * (size_t)g.ntotal, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  return EPH_OK;
+}
+
+int download_grid(eph_ctx *c) {
+  CUDA_TRY(c, cudaMemcpyAsync(c->grid.T.data(), c->T0.p, sizeof(double) * (size_t)c->grid.ntotal,
+                              cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return EPH_OK;
+}
+
+int write_T_output(eph_ctx *c) {
+  // end_of_step (fix_eph.cpp:397-399): every T_freq steps
+  if (c->args.T_freq > 0 && (c->ntimestep % c->args.T_freq) == 0) {
+    int r = download_grid(c);
+    if (r) return r;
+    if (c->grid.save_temperature(c->args.T_out.c_str(), (int)(c->ntimestep / c->args.T_freq)))
+      return fail(c, EPH_ERR_FILE, "cannot write " + c->args.T_out);
+  }
+  return EPH_OK;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+
+extern "C" {
+
+const char *eph_status_string(int s) {
+  switch (s) {
+    case EPH_OK: return "ok";
+    case EPH_ERR_ARG: return "bad argument";
+    case EPH_ERR_FILE: return "file error";
+    case EPH_ERR_UNSUPPORTED_MODEL: return "unsupported model";
+    case EPH_ERR_CAPACITY: return "capacity exceeded";
+    case EPH_ERR_TIMEOUT: return "device wait timed out";
+    case EPH_ERR_CUDA: return "CUDA error";
+    case EPH_ERR_STATE: return "call out of order";
+    case EPH_ERR_RANGE: return "input out of range";
+    default: return "unknown status";
+  }
+}
+
+const char *eph_last_error(const eph_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out) {
+  if (!out || !md || !arg) return EPH_ERR_ARG;
+  *out = nullptr;
+  eph_ctx *c = new (std::nothrow) eph_ctx();
+  if (!c) return EPH_ERR_ARG;
+  std::string why;
+  int r = parse_fix_args(narg, arg, &c->args, &why);
+  if (r) {
+    *out = c;
+    return fail(c, r, why);
+  }
+  *out = c;
+  if (c->args.model != 4)
+    return fail(c, EPH_ERR_UNSUPPORTED_MODEL, "only model 4 (PRL 120, 185501) runs on the GPU path");
+  if (md->ntypes < 1 || md->ntypes > 64 || !md->mass) return fail(c, EPH_ERR_ARG, "ntypes must be 1..64 with masses");
+  if (!(md->dt > 0)) return fail(c, EPH_ERR_ARG, "dt must be positive");
+  c->ntypes = md->ntypes;
+  c->mass.assign(md->mass, md->mass + md->ntypes + 1);
+  for (int k = 0; k < 3; ++k) {
+    c->boxlo[k] = md->boxlo[k];
+    c->boxhi[k] = md->boxhi[k];
+    c->prd[k] = md->boxhi[k] - md->boxlo[k];
+    if (!(c->prd[k] > 0)) return fail(c, EPH_ERR_ARG, "empty box");
+  }
+  c->dt = md->dt;
+  c->boltz = md->boltz;
+  c->ftm2v = md->ftm2v;
+  c->skin = md->skin;
+  c->groupbit = md->groupbit;
+  c->device = md->device;
+  c->mode = md->mode == EPH_MODE_EXACT ? EPH_MODE_EXACT : EPH_MODE_FAST;
+  // grid (fix_eph.cpp:131-161)
+  if (c->args.T_infile == "NULL") {
+    c->grid.create(c->args.nx, c->args.ny, c->args.nz, c->boxlo[0], c->boxhi[0], c->boxlo[1], c->boxhi[1],
+                   c->boxlo[2], c->boxhi[2], c->args.T_e, c->args.C_e, c->args.rho_e, c->args.kappa_e);
+  } else {
+    std::string e = c->grid.load(c->args.T_infile.c_str());
+    if (!e.empty()) return fail(c, EPH_ERR_FILE, e);
+  }
+  // element map (fix_eph.cpp:168-198), including its check type_map > types
+  if (c->ntypes > narg - 17) return fail(c, EPH_ERR_ARG, "Fix eph: number of types larger than provided in fix");
+  {
+    std::string e = c->beta.load(c->args.beta_file.c_str());
+    if (!e.empty()) return fail(c, EPH_ERR_FILE, e);
+  }
+  c->type_map.assign(c->ntypes + 1, 0);
+  for (int t = 0; t < c->ntypes; ++t) {
+    long m = 2147483647L;
+    for (int j = 0; j < c->beta.n_elements; ++j)
+      if (c->beta.names[j] == c->args.elements[t]) m = j;
+    if (m > c->ntypes) return fail(c, EPH_ERR_ARG, "Fix eph: elements not found in input file");
+    c->type_map[t + 1] = (int)m;
+  }
+  int used[64] = {0}, nused = 0;
+  for (int t = 1; t <= c->ntypes; ++t)
+    if (!used[c->type_map[t]]) used[c->type_map[t]] = 1, ++nused;
+  c->multi = nused > 1;
+  // device
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  c->own_stream = true;
+  CUDA_TRY(c, cudaMallocHost(&c->h_err, sizeof(unsigned)));
+  CUDA_TRY(c, c->d_err.alloc(1));
+  CUDA_TRY(c, c->counters.alloc(NCOUNTERS));
+  CUDA_TRY(c, c->wrapflag.alloc(1));
+  CUDA_TRY(c, c->scal.alloc(4));
+  CUDA_TRY(c, c->gsum.alloc(1));
+  CUDA_TRY(c, cudaMemset(c->d_err.p, 0, sizeof(unsigned)));
+  CUDA_TRY(c, cudaMemset(c->counters.p, 0, sizeof(unsigned long long) * NCOUNTERS));
+  CUDA_TRY(c, cudaMemset(c->wrapflag.p, 0, sizeof(int)));
+  CUDA_TRY(c, cudaMemset(c->scal.p, 0, sizeof(double) * 4));
+  r = upload_tables(c);
+  if (r) return r;
+  r = upload_grid(c);
+  if (r) return r;
+  // step constants
+  StepParams &P = c->P;
+  P.flags = c->args.flags;
+  P.groupbit = c->groupbit;
+  P.nelem = c->beta.n_elements;
+  for (int k = 0; k < 3; ++k) {
+    P.lo[k] = c->boxlo[k];
+    P.hi[k] = c->boxhi[k];
+    P.prd[k] = c->prd[k];
+  }
+  P.rc2 = c->beta.r_cutoff_sq;
+  P.rc2_band = (float)(c->beta.r_cutoff_sq * (1.0 + 1e-4));
+  P.tab_rho_r_sq = c->tab_rho_r_sq.p;
+  P.tab_beta = c->tab_beta.p;
+  P.tab_alpha = c->tab_alpha.p;
+  P.inv_dr_sq = c->beta.rho_r_sq[0].inv_dx;
+  P.inv_drho = c->beta.beta[0].inv_dx;
+  P.n_rho = (int)c->beta.n_rho;
+  P.n_beta = (int)c->beta.n_beta;
+  P.rho_cutoff = c->beta.rho_cutoff;
+  P.triggersq = 0.25 * c->skin * c->skin;
+  for (int t = 0; t <= 64; ++t) P.type_map[t] = t <= c->ntypes ? c->type_map[t] : 0;
+  const Grid &g = c->grid;
+  P.gnx = g.nx;
+  P.gny = g.ny;
+  P.gnz = g.nz;
+  P.ncells = g.ntotal;
+  P.gx0 = g.x0;
+  P.gy0 = g.y0;
+  P.gz0 = g.z0;
+  P.gdx = g.dx;
+  P.gdy = g.dy;
+  P.gdz = g.dz;
+  P.seed = (unsigned)c->args.seed;
+  set_time_params(c);
+  // bins: edge >= rc (1 + 5e-5), at least 3 per axis
+  for (int k = 0; k < 3; ++k) {
+    const int nb = (int)(c->prd[k] / (c->beta.r_cutoff * (1.0 + 5e-5)));
+    if (nb < 3) return fail(c, EPH_ERR_ARG, "box edge shorter than three r_cutoff: too small for minimum-image bins");
+    P.nb[k] = nb;
+    P.w[k] = c->prd[k] / nb;
+    P.inv_w[k] = 1.0 / P.w[k];
+    P.wf[k] = (float)P.w[k];
+  }
+  c->nbins = P.nb[0] * P.nb[1] * P.nb[2];
+  return EPH_OK;
+}
+
+void eph_destroy(eph_ctx *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  collect_marks(c);
+  for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  delete c;
+}
+
+int eph_set_capacity(eph_ctx *c, int bin_capacity, int pair_capacity) {
+  if (!c) return EPH_ERR_ARG;
+  if (pair_capacity > KMAX) return fail(c, EPH_ERR_ARG, "pair capacity above the compiled maximum");
+  if (bin_capacity > 0) c->bcap = bin_capacity;
+  if (pair_capacity > 0) c->kcap = pair_capacity;
+  if (c->n > 0) {
+    c->P.bcap = c->bcap;
+    c->P.kcap = c->kcap;
+    CUDA_TRY(c, c->bins.alloc((size_t)c->nbins * c->bcap));
+    CUDA_TRY(c, c->pj.alloc((size_t)c->kcap * c->n));
+    CUDA_TRY(c, c->pe.alloc((size_t)c->kcap * c->n));
+    CUDA_TRY(c, c->pg.alloc((size_t)c->kcap * c->n));
+  }
+  return EPH_OK;
+}
+
+int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const int *htype, const int *hmask) {
+  if (!c) return EPH_ERR_ARG;
+  if (n < 1) return fail(c, EPH_ERR_ARG, "fix_eph: error no atoms in simulation");
+  if ((unsigned)n > IDX_MASK) return fail(c, EPH_ERR_ARG, "too many atoms for one context");
+  if (!hx || !hv || !htype) return fail(c, EPH_ERR_ARG, "null atom buffer");
+  for (int i = 0; i < n; ++i)
+    if (htype[i] < 1 || htype[i] > c->ntypes) return fail(c, EPH_ERR_ARG, "atom type outside 1..ntypes");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->n = n;
+  c->P.n = n;
+  const size_t N = (size_t)n;
+  for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw})
+    CUDA_TRY(c, b->alloc(N));
+  CUDA_TRY(c, c->type.alloc(N));
+  CUDA_TRY(c, c->mask.alloc(N));
+  CUDA_TRY(c, c->nshort.alloc(N));
+  CUDA_TRY(c, c->cell.alloc(N));
+  CUDA_TRY(c, c->rho.alloc(N));
+  CUDA_TRY(c, c->beta_i.alloc(N));
+  CUDA_TRY(c, c->Te_i.alloc(N));
+  CUDA_TRY(c, c->stage.alloc(8 * N));
+  CUDA_TRY(c, c->atom_bin.alloc(N));
+  CUDA_TRY(c, c->atom_off.alloc(N));
+  CUDA_TRY(c, c->tmap.alloc(65));
+  CUDA_TRY(c, c->part.alloc((size_t)nblocks(n, 256)));
+  CUDA_TRY(c, c->bin_count.alloc((size_t)c->nbins));
+  // capacities from the number density: a bin holds ~density*w^3 atoms, the
+  // cutoff sphere ~density*4/3 pi rc^3
+  const double vol = c->prd[0] * c->prd[1] * c->prd[2];
+  const double dens = n / vol;
+  const double per_bin = dens * c->P.w[0] * c->P.w[1] * c->P.w[2];
+  const double rc = c->beta.r_cutoff;
+  const double per_sphere = dens * 4.18879020478639 * rc * rc * rc;
+  if (c->bcap <= 0) c->bcap = ((int)std::ceil(2.0 * per_bin + 16.0) + 7) / 8 * 8;
+  if (c->kcap <= 0) c->kcap = std::min(KMAX, ((int)std::ceil(2.0 * per_sphere + 24.0) + 7) / 8 * 8);
+  c->P.bcap = c->bcap;
+  c->P.kcap = c->kcap;
+  CUDA_TRY(c, c->bins.alloc((size_t)c->nbins * c->bcap));
+  CUDA_TRY(c, c->pj.alloc((size_t)c->kcap * N));
+  CUDA_TRY(c, c->pe.alloc((size_t)c->kcap * N));
+  CUDA_TRY(c, c->pg.alloc((size_t)c->kcap * N));
+  // atoms
+  std::vector<int> m(N, 1);
+  if (hmask) std::memcpy(m.data(), hmask, sizeof(int) * N);
+  CUDA_TRY(c, cudaMemcpy(c->type.p, htype, sizeof(int) * N, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->mask.p, m.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->tmap.p, c->P.type_map, sizeof(int) * 65, cudaMemcpyHostToDevice));
+  for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw})
+    CUDA_TRY(c, cudaMemset(b->p, 0, sizeof(D4) * N));
+  int r = eph_put(c, EPH_FIELD_X, hx, EPH_HOST);
+  if (r) return r;
+  r = eph_put(c, EPH_FIELD_V, hv, EPH_HOST);
+  if (r) return r;
+  k_set_elem<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->type.p, c->tmap.p, c->x.p);
+  CUDA_TRY(c, cudaMemcpyAsync(c->xhold.p, c->x.p, sizeof(D4) * N, cudaMemcpyDeviceToDevice, c->stream));
+  // the engine wraps positions at set-up (Verlet::setup)
+  CUDA_TRY(c, cudaMemsetAsync(c->wrapflag.p, 0xff, sizeof(int), c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
+  k_bin<<<nblocks(n), BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
+                                             c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p);
+  CUDA_TRY(c, cudaMemsetAsync(c->wrapflag.p, 0, sizeof(int), c->stream));
+  c->have_fext = false;
+  CUDA_TRY(c, cudaGetLastError());
+  return check_device(c);
+}
+
+int eph_put(eph_ctx *c, int field, const double *src, int where) {
+  if (!c || !src) return EPH_ERR_ARG;
+  if (field == EPH_FIELD_T_E) {
+    const size_t nc = (size_t)c->grid.ntotal;
+    CUDA_TRY(c, cudaMemcpyAsync(c->T0.p, src, nc * 8,
+                                where == EPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+    return EPH_OK;
+  }
+  int r = require_atoms(c);
+  if (r) return r;
+  DevBuf<D4> *dst = nullptr;
+  switch (field) {
+    case EPH_FIELD_X: dst = &c->x; break;
+    case EPH_FIELD_V: dst = &c->v; break;
+    case EPH_FIELD_F: dst = &c->f; break;
+    case EPH_FIELD_XI: dst = &c->xi; c->have_xi = true; break;
+    case EPH_FIELD_F_EXT:
+      if (!c->fext.p) CUDA_TRY(c, c->fext.alloc((size_t)c->n));
+      dst = &c->fext;
+      c->have_fext = true;
+      break;
+    default: return fail(c, EPH_ERR_ARG, "field cannot be written");
+  }
+  const double *s = src;
+  if (where == EPH_HOST) {
+    CUDA_TRY(c, cudaMemcpyAsync(c->stage.p, src, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyHostToDevice,
+                                c->stream));
+    s = c->stage.p;
+  }
+  k_pack3<<<nblocks(c->n), BLOCK, 0, c->stream>>>(c->n, s, dst->p);
+  CUDA_TRY(c, cudaGetLastError());
+  if (where == EPH_HOST) CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // src may be reused at return
+  return EPH_OK;
+}
+
+int eph_get(eph_ctx *c, int field, double *dst, int where) {
+  if (!c || !dst) return EPH_ERR_ARG;
+  if (field == EPH_FIELD_T_E) {
+    CUDA_TRY(c, cudaMemcpyAsync(dst, c->T0.p, sizeof(double) * (size_t)c->grid.ntotal,
+                                where == EPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+    return check_device(c);
+  }
+  int r = require_atoms(c);
+  if (r) return r;
+  const int n = c->n;
+  double *d = where == EPH_HOST ? c->stage.p : dst;
+  size_t count = 3 * (size_t)n;
+  switch (field) {
+    case EPH_FIELD_X: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->x.p, d); break;
+    case EPH_FIELD_V: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->v.p, d); break;
+    case EPH_FIELD_F: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->f.p, d); break;
+    case EPH_FIELD_XI: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->xi.p, d); break;
+    case EPH_FIELD_F_EPH: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->f_eph.p, d); break;
+    case EPH_FIELD_F_RNG: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->f_rng.p, d); break;
+    case EPH_FIELD_W: k_get_w<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->Bw.p, d); break;
+    case EPH_FIELD_RHO:
+      count = (size_t)n;
+      CUDA_TRY(c, cudaMemcpyAsync(d, c->rho.p, sizeof(double) * count, cudaMemcpyDeviceToDevice, c->stream));
+      break;
+    case EPH_FIELD_PERATOM:
+      count = 8 * (size_t)n;
+      k_peratom<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->groupbit, c->mask.p, c->rho.p, c->beta_i.p, c->f_eph.p,
+                                                     c->f_rng.p, d);
+      break;
+    default: return fail(c, EPH_ERR_ARG, "field cannot be read");
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  if (where == EPH_HOST)
+    CUDA_TRY(c, cudaMemcpyAsync(dst, c->stage.p, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+  return check_device(c);
+}
+
+int eph_initial_integrate(eph_ctx *c) {
+  if (!c) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r) return r;
+  return launch_initial(c, 0);
+}
+
+int eph_post_force(eph_ctx *c, int xi_source) {
+  if (!c) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r) return r;
+  if (xi_source == EPH_XI_GIVEN && !c->have_xi && (c->P.flags & FLAG_RANDOM))
+    return fail(c, EPH_ERR_STATE, "EPH_XI_GIVEN without eph_put(EPH_FIELD_XI)");
+  r = launch_post_force(c, xi_source == EPH_XI_GIVEN ? 1 : 0);
+  if (r) return r;
+  return EPH_OK;
+}
+
+int eph_final_integrate(eph_ctx *c) {
+  if (!c) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r) return r;
+  return launch_final(c);
+}
+
+int eph_end_of_step(eph_ctx *c) {
+  if (!c) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r) return r;
+  r = launch_end_of_step(c);
+  if (r) return r;
+  return write_T_output(c);
+}
+
+int eph_step(eph_ctx *c, int nsteps, int xi_source) {
+  if (!c || nsteps < 0) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r) return r;
+  if (xi_source == EPH_XI_GIVEN && !c->have_xi && (c->P.flags & FLAG_RANDOM))
+    return fail(c, EPH_ERR_STATE, "EPH_XI_GIVEN without eph_put(EPH_FIELD_XI)");
+  for (int s = 0; s < nsteps; ++s) {
+    c->ntimestep += 1;
+    if ((r = launch_initial(c, 1))) return r;
+    // force clear + the external (pair) force
+    if (c->have_fext)
+      CUDA_TRY(c, cudaMemcpyAsync(c->f.p, c->fext.p, sizeof(D4) * (size_t)c->n, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+    else
+      CUDA_TRY(c, cudaMemsetAsync(c->f.p, 0, sizeof(D4) * (size_t)c->n, c->stream));
+    if ((r = launch_post_force(c, xi_source == EPH_XI_GIVEN ? 1 : 0))) return r;
+    if ((r = launch_final(c))) return r;
+    if ((r = launch_end_of_step(c))) return r;
+    if ((r = write_T_output(c))) return r;
+  }
+  return EPH_OK;
+}
+
+int eph_synchronize(eph_ctx *c) {
+  if (!c) return EPH_ERR_ARG;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device(c);
+}
+
+int eph_compute_vector(eph_ctx *c, int i, double *out) {
+  if (!c || !out) return EPH_ERR_ARG;
+  if (i == 1) {
+    CUDA_TRY(c, cudaMemsetAsync(c->gsum.p, 0, sizeof(U128), c->stream));
+    k_grid_sum<<<std::min(nblocks(c->grid.ntotal, 256), 1024), 256, 0, c->stream>>>(c->T0.p, c->grid.ntotal,
+                                                                                    c->gsum.p, c->d_err.p);
+    k_from_fixed<<<1, 1, 0, c->stream>>>(c->gsum.p, c->scal.p + 2);
+    double s;
+    CUDA_TRY(c, cudaMemcpyAsync(&s, c->scal.p + 2, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    int r = check_device(c);
+    if (r) return r;
+    *out = s / (double)(size_t)c->grid.ntotal;
+    return EPH_OK;
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(out, c->scal.p + 0, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return check_device(c);
+}
+
+int eph_reset_dt(eph_ctx *c, double dt) {
+  if (!c || !(dt > 0)) return EPH_ERR_ARG;
+  c->dt = dt;
+  set_time_params(c);
+  return EPH_OK;
+}
+
+int eph_save_state(eph_ctx *c, const char *path) {
+  if (!c || !path) return EPH_ERR_ARG;
+  int r = download_grid(c);
+  if (r) return r;
+  if (c->grid.save_state(path)) return fail(c, EPH_ERR_FILE, std::string("cannot write ") + path);
+  return EPH_OK;
+}
+
+int eph_save_temperature(eph_ctx *c, const char *path, int n) {
+  if (!c || !path) return EPH_ERR_ARG;
+  int r = download_grid(c);
+  if (r) return r;
+  if (c->grid.save_temperature(path, n)) return fail(c, EPH_ERR_FILE, std::string("cannot write ") + path);
+  return EPH_OK;
+}
+
+int eph_post_run(eph_ctx *c) {
+  if (!c) return EPH_ERR_ARG;
+  return eph_save_state(c, c->args.T_state.c_str());
+}
+
+int eph_set_timestep(eph_ctx *c, long ntimestep) {
+  if (!c) return EPH_ERR_ARG;
+  c->ntimestep = ntimestep;
+  return EPH_OK;
+}
+
+int eph_set_stream(eph_ctx *c, void *stream) {
+  if (!c) return EPH_ERR_ARG;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  c->own_stream = false;
+  c->stream = (cudaStream_t)stream;
+  return EPH_OK;
+}
+
+int eph_set_profiling(eph_ctx *c, int on) {
+  if (!c) return EPH_ERR_ARG;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  collect_marks(c);
+  for (int k = 0; k < EPH_NPHASES; ++k) {
+    c->phase_ms[k] = 0.0;
+    c->phase_launches[k] = 0;
+  }
+  c->launches = 0;
+  c->profiling = on != 0;
+  return EPH_OK;
+}
+
+int eph_phase_times(eph_ctx *c, double *ms, long *launches) {
+  if (!c) return EPH_ERR_ARG;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  collect_marks(c);
+  for (int k = 0; k < EPH_NPHASES; ++k) {
+    if (ms) ms[k] = c->phase_ms[k];
+    if (launches) launches[k] = c->phase_launches[k];
+  }
+  return EPH_OK;
+}
+
+int eph_launch_count(eph_ctx *c, long *out) {
+  if (!c || !out) return EPH_ERR_ARG;
+  *out = c->launches;
+  return EPH_OK;
+}
+
+int eph_pair_count(eph_ctx *c, long *out) {
+  if (!c || !out) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r) return r;
+  std::vector<int> h((size_t)c->n);
+  CUDA_TRY(c, cudaMemcpyAsync(h.data(), c->nshort.p, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  long t = 0;
+  for (int v : h) t += v;
+  *out = t;
+  return EPH_OK;
+}
+
+int eph_get_counter(eph_ctx *c, int which, long *out) {
+  if (!c || !out || which < 0 || which >= NCOUNTERS) return EPH_ERR_ARG;
+  unsigned long long v = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&v, c->counters.p + which, sizeof(v), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  *out = (long)v;
+  return EPH_OK;
+}
+
+// ------------------------------------------------------ host-side helpers
+
+struct eph_beta {
+  Beta b;
+};
+
+int eph_beta_load(const char *path, eph_beta **out) {
+  if (!path || !out) return EPH_ERR_ARG;
+  eph_beta *b = new (std::nothrow) eph_beta();
+  if (!b) return EPH_ERR_ARG;
+  if (!b->b.load(path).empty()) {
+    delete b;
+    *out = nullptr;
+    return EPH_ERR_FILE;
+  }
+  *out = b;
+  return EPH_OK;
+}
+
+void eph_beta_free(eph_beta *b) { delete b; }
+
+int eph_beta_info(const eph_beta *b, int *n_elements, double *r_cutoff, double *rho_cutoff) {
+  if (!b) return EPH_ERR_ARG;
+  if (n_elements) *n_elements = b->b.n_elements;
+  if (r_cutoff) *r_cutoff = b->b.r_cutoff;
+  if (rho_cutoff) *rho_cutoff = b->b.rho_cutoff;
+  return EPH_OK;
+}
+
+double eph_beta_eval(const eph_beta *b, int which, int elem, double x) {
+  if (!b || elem < 0 || elem >= b->b.n_elements) return NAN;
+  return b->b.table(which, elem)(x);
+}
+
+long eph_beta_table(const eph_beta *b, int which, int elem, double *out) {
+  if (!b || elem < 0 || elem >= b->b.n_elements) return -1;
+  const Spline &s = b->b.table(which, elem);
+  if (out) std::memcpy(out, s.c.data(), sizeof(double) * 4 * (size_t)s.n);
+  return s.n;
+}
+
+struct eph_grid {
+  Grid g;
+};
+
+int eph_grid_create(long nx, long ny, long nz, const double *lo, const double *hi, double T_e, double C_e,
+                    double rho_e, double kappa_e, eph_grid **out) {
+  if (!out || !lo || !hi || nx < 1 || ny < 1 || nz < 1) return EPH_ERR_ARG;
+  eph_grid *g = new (std::nothrow) eph_grid();
+  if (!g) return EPH_ERR_ARG;
+  g->g.create(nx, ny, nz, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], T_e, C_e, rho_e, kappa_e);
+  *out = g;
+  return EPH_OK;
+}
+
+int eph_grid_load(const char *path, eph_grid **out) {
+  if (!path || !out) return EPH_ERR_ARG;
+  eph_grid *g = new (std::nothrow) eph_grid();
+  if (!g) return EPH_ERR_ARG;
+  if (!g->g.load(path).empty()) {
+    delete g;
+    *out = nullptr;
+    return EPH_ERR_FILE;
+  }
+  *out = g;
+  return EPH_OK;
+}
+
+void eph_grid_free(eph_grid *g) { delete g; }
+long eph_grid_ncells(const eph_grid *g) { return g ? g->g.ntotal : -1; }
+
+unsigned eph_grid_substeps(const eph_grid *g, double dt, double *inner_dt) {
+  if (!g) return 0;
+  Grid t = g->g;
+  t.dt = dt;
+  double idt = 0;
+  const unsigned s = t.substeps(&idt);
+  if (inner_dt) *inner_dt = idt;
+  return s;
+}
+
+int eph_grid_save_state(const eph_grid *g, const char *path) {
+  if (!g || !path) return EPH_ERR_ARG;
+  return g->g.save_state(path) ? EPH_ERR_FILE : EPH_OK;
+}
+
+int eph_grid_save_temperature(const eph_grid *g, const char *path, int n) {
+  if (!g || !path) return EPH_ERR_ARG;
+  return g->g.save_temperature(path, n) ? EPH_ERR_FILE : EPH_OK;
+}
+
+}  // extern "C"

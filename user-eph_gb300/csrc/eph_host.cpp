@@ -1,0 +1,316 @@
+// Host side of the GB300 fix-eph path (see eph_host.hpp).  Compiled with
+// -ffp-contract=off: the spline construction and the grid constants follow
+// the reference's expressions term by term, so the device tables are the
+// reference's tables bit for bit.
+#include "eph_host.hpp"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "eph_gb.h"
+
+namespace ephgb {
+
+void Spline::build(double dx, const std::vector<double> &y) {
+  const size_t points = y.size();
+  inv_dx = 1. / dx;
+  n = (long)points;
+  // One zero knot past the end: at i = points-1 the slope loop below reads the
+  // slope of knot `points`, one past the table (eph_spline.h:79-81 reads
+  // c[i+1].b there); a zero slope reproduces the reference's choice in every
+  // case except when that stray value equals z2 exactly.
+  c.assign((points + 1) * 4, 0.0);
+  auto A = [&](size_t i) -> double & { return c[4 * i + 0]; };
+  auto B = [&](size_t i) -> double & { return c[4 * i + 1]; };
+  auto C = [&](size_t i) -> double & { return c[4 * i + 2]; };
+  auto D = [&](size_t i) -> double & { return c[4 * i + 3]; };
+  double z0, z1, z2, z3;
+  for (size_t i = 0; i < points - 1; ++i) B(i) = (y[i + 1] - y[i]) / dx;
+  z1 = 2.0 * B(0) - B(1);
+  z0 = 2.0 * z1 - B(0);
+  z2 = 2.0 * B(points - 2) - B(points - 1);
+  z3 = 2.0 * z2 - B(points - 1);
+  B(points - 1) = z2;
+  for (size_t i = 2; i < points - 2; ++i) {
+    C(i) = std::fabs(B(i + 1) - B(i));
+    D(i) = std::fabs(B(i - 1) - B(i - 2));
+  }
+  C(0) = std::fabs(B(1) - B(0));
+  D(0) = std::fabs(z1 - z0);
+  C(1) = std::fabs(B(2) - B(1));
+  D(1) = std::fabs(B(0) - z1);
+  C(points - 2) = std::fabs(z2 - B(points - 2));
+  D(points - 2) = std::fabs(B(points - 3) - B(points - 4));
+  C(points - 1) = std::fabs(z3 - z2);
+  D(points - 1) = std::fabs(B(points - 2) - B(points - 3));
+  for (size_t i = 0; i < points; ++i) {
+    double d_2, d_1, d0, d1;
+    if (i == 0) {
+      d_2 = z0;
+      d_1 = z1;
+    } else if (i == 1) {
+      d_2 = z1;
+      d_1 = B(i - 1);
+    } else {
+      d_2 = B(i - 2);
+      d_1 = B(i - 1);
+    }
+    d1 = B(i + 1);
+    d0 = B(i);
+    const double w1 = C(i), w0 = D(i);
+    if (d_2 == d_1 && d0 != d1)
+      A(i) = d_1;
+    else if (d0 == d1 && d_2 == d_1)
+      A(i) = d0;
+    else if (d_1 == d0)
+      A(i) = d0;
+    else if (d_2 == d_1 && d0 == d1 && d0 != d_1)
+      A(i) = 0.5 * (d_1 + d0);
+    else
+      A(i) = (d_1 * w1 + d0 * w0) / (w1 + w0);
+  }
+  for (size_t i = 0; i < points - 1; ++i) {
+    const double fi = (double)i, fi1 = (double)(i + 1);
+    const double dx3 = dx * dx * dx;
+    const double x0_1 = fi * dx, x0_2 = fi * dx * x0_1, x0_3 = fi * dx * x0_2;
+    const double x1_1 = fi1 * dx, x1_2 = fi1 * dx * x1_1, x1_3 = fi1 * dx * x1_2;
+    D(i) = (-A(i) * x0_1 - A(i + 1) * x0_1 + A(i) * x1_1 + A(i + 1) * x1_1 + 2.0 * y[i] - 2.0 * y[i + 1]) / dx3;
+    C(i) = (-A(i) + A(i + 1) + 3.0 * D(i) * x0_2 - 3.0 * D(i) * x1_2) / 2.0 / dx;
+    B(i) = (C(i) * x0_2 + D(i) * x0_3 - C(i) * x1_2 - D(i) * x1_3 - y[i] + y[i + 1]) / dx;
+    A(i) = y[i] - B(i) * x0_1 - C(i) * x0_2 - D(i) * x0_3;
+  }
+  A(points - 1) = y[points - 1];
+  B(points - 1) = 0.0;
+  C(points - 1) = 0.0;
+  D(points - 1) = 0.0;
+  c.resize(points * 4);
+}
+
+double Spline::operator()(double x) const {
+  size_t index = (size_t)(x * inv_dx);
+  if (!(x >= 0.0) || index >= (size_t)n) return NAN;
+  const double *k = &c[4 * index];
+  return k[0] + x * (k[1] + x * (k[2] + x * k[3]));
+}
+
+std::string Beta::load(const char *path) {
+  std::ifstream fd(path);
+  if (!fd.is_open()) return std::string("cannot open beta file ") + path;
+  std::string line;
+  for (int k = 0; k < 3; ++k)
+    if (!std::getline(fd, line)) return "beta file: missing comment lines";
+  if (!std::getline(fd, line)) return "beta file: missing element line";
+  {
+    std::istringstream ss(line);
+    if (!(ss >> n_elements) || n_elements < 1) return "beta file: no elements found";
+    names.resize(n_elements);
+    for (int i = 0; i < n_elements; ++i)
+      if (!(ss >> names[i])) return "beta file: fewer element names than elements";
+  }
+  if (!(fd >> n_rho >> dr >> n_beta >> drho >> r_cutoff)) return "beta file: bad spline header";
+  if (n_rho < 5 || n_beta < 5 || !(dr > 0) || !(drho > 0) || !(r_cutoff > 0)) return "beta file: bad spline header";
+  r_cutoff_sq = r_cutoff * r_cutoff;
+  rho_cutoff = drho * (double)(size_t)(n_beta - 1);
+  dr_sq = r_cutoff_sq / (double)(size_t)(n_rho - 1);
+  numbers.resize(n_elements);
+  rho.resize(n_elements);
+  rho_r_sq.resize(n_elements);
+  beta.resize(n_elements);
+  alpha.resize(n_elements);
+  std::vector<double> buf;
+  for (int e = 0; e < n_elements; ++e) {
+    unsigned short z;
+    if (!(fd >> z)) return "beta file: missing element number";
+    numbers[e] = (uint8_t)z;
+    buf.assign(n_rho, 0.0);
+    for (long j = 0; j < n_rho; ++j)
+      if (!(fd >> buf[j])) return "beta file: too few rho(r) knots";
+    rho[e].build(dr, buf);
+    for (long j = 0; j < n_rho; ++j) buf[j] = rho[e](std::sqrt((double)(size_t)j * dr_sq));
+    rho_r_sq[e].build(dr_sq, buf);
+    buf.assign(n_beta, 0.0);
+    for (long j = 0; j < n_beta; ++j)
+      if (!(fd >> buf[j])) return "beta file: too few beta(rho) knots";
+    beta[e].build(drho, buf);
+    for (long j = 0; j < n_beta; ++j) buf[j] = std::sqrt(buf[j]);
+    alpha[e].build(drho, buf);
+  }
+  return "";
+}
+
+const Spline &Beta::table(int which, int elem) const {
+  switch (which) {
+    case EPH_SPLINE_RHO_R: return rho[elem];
+    case EPH_SPLINE_RHO_R_SQ: return rho_r_sq[elem];
+    case EPH_SPLINE_BETA: return beta[elem];
+    default: return alpha[elem];
+  }
+}
+
+double Beta::get_beta(int elem, double r) const { return r > rho_cutoff ? 0. : beta[elem](r); }
+double Beta::get_alpha(int elem, double r) const { return r > rho_cutoff ? 0. : alpha[elem](r); }
+
+void Grid::set_box(double a0, double a1, double b0, double b1, double c0, double c1) {
+  x0 = a0; x1 = a1; y0 = b0; y1 = b1; z0 = c0; z1 = c1;
+  dx = (x1 - x0) / (double)(size_t)nx;
+  dy = (y1 - y0) / (double)(size_t)ny;
+  dz = (z1 - z0) / (double)(size_t)nz;
+  dV = dx * dy * dz;
+}
+
+void Grid::create(long inx, long iny, long inz, double a0, double a1, double b0, double b1, double c0, double c1,
+                  double T_e, double C_e, double rho_e, double kappa_e) {
+  nx = inx; ny = iny; nz = inz;
+  ntotal = nx * ny * nz;
+  T.assign(ntotal, T_e);
+  S.assign(ntotal, 0.0);
+  rho.assign(ntotal, rho_e);
+  C.assign(ntotal, C_e);
+  kappa.assign(ntotal, kappa_e);
+  flag.assign(ntotal, GRID_DYNAMIC);
+  T_dynamic.assign(ntotal, 0);
+  set_box(a0, a1, b0, b1, c0, c1);
+  steps = 1;
+  dt = 1;
+  parameter_filename = "NULL";
+}
+
+std::string Grid::load(const char *path) {
+  std::ifstream fd(path);
+  if (!fd) return std::string("cannot open grid file ") + path;
+  std::string line;
+  for (int k = 0; k < 3; ++k)
+    if (!std::getline(fd, line) || line.empty() || line[0] != '#') return "grid file: three '#' comment lines expected";
+  if (!(fd >> nx >> ny >> nz >> steps) || nx < 1 || ny < 1 || nz < 1) return "grid file: bad size line";
+  ntotal = nx * ny * nz;
+  double b[6];
+  for (double &v : b)
+    if (!(fd >> v)) return "grid file: bad box lines";
+  if (!(fd >> parameter_filename)) return "grid file: missing parameter-file line";
+  if (parameter_filename != "NULL")
+    return "grid file: temperature-dependent parameter files (C_e(T), kappa(T)) are not supported";
+  T.assign(ntotal, 0.0);
+  S.assign(ntotal, 0.0);
+  rho.assign(ntotal, 0.0);
+  C.assign(ntotal, 0.0);
+  kappa.assign(ntotal, 0.0);
+  flag.assign(ntotal, GRID_DYNAMIC);
+  T_dynamic.assign(ntotal, 0);
+  set_box(b[0], b[1], b[2], b[3], b[4], b[5]);
+  for (long c = 0; c < ntotal; ++c) {
+    long lx, ly, lz;
+    int fl, td;
+    double t, s, r, ce, k;
+    if (!(fd >> lx >> ly >> lz >> t >> s >> r >> ce >> k >> fl >> td)) return "grid file: too few cell lines";
+    const long index = lx + ly * nx + lz * nx * ny;
+    if (lx < 0 || ly < 0 || lz < 0 || index >= ntotal) return "grid file: cell index outside the grid";
+    if (td != 0) return "grid file: temperature-dependent cells are not supported";
+    T[index] = t;
+    S[index] = s;
+    rho[index] = r;
+    C[index] = ce;
+    kappa[index] = k;
+    flag[index] = (int16_t)fl;
+    T_dynamic[index] = (uint16_t)td;
+  }
+  dt = 1;
+  return "";
+}
+
+unsigned Grid::substeps(double *inner_dt_out) const {
+  double inner_dt = dt / (double)(size_t)steps;
+  const double dtdxdydz = inner_dt * (1.0 / dx / dx + 1.0 / dy / dy + 1.0 / dz / dz);
+  double c_min = C[0], rho_min = rho[0], kappa_max = kappa[0];
+  for (long i = 1; i < ntotal; ++i)
+    if (flag[i] != GRID_CONSTANT) {
+      if (C[i] < c_min) c_min = C[i];
+      if (rho[i] < rho_min) rho_min = rho[i];
+      if (kappa[i] > kappa_max) kappa_max = kappa[i];
+    }
+  const double r = dtdxdydz / c_min / rho_min * kappa_max;
+  unsigned new_steps = (unsigned)steps;
+  if (r > 0.4) {
+    inner_dt = 0.4 * inner_dt / r;
+    const unsigned s = (unsigned)(dt / inner_dt);
+    new_steps = s > 1u ? s : 1u;
+    inner_dt = dt / new_steps;
+  }
+  *inner_dt_out = inner_dt;
+  return new_steps;
+}
+
+int Grid::save_state(const char *path) const {
+  FILE *fd = std::fopen(path, "w");
+  if (!fd) return 1;
+  std::fprintf(fd, "# A comment\n#\n#\n");
+  std::fprintf(fd, "%ld %ld %ld %ld\n", nx, ny, nz, steps);
+  std::fprintf(fd, "%.6e %.6e\n", x0, x1);
+  std::fprintf(fd, "%.6e %.6e\n", y0, y1);
+  std::fprintf(fd, "%.6e %.6e\n", z0, z1);
+  std::fprintf(fd, "%s\n", parameter_filename.c_str());
+  for (long k = 0; k < nz; ++k)
+    for (long j = 0; j < ny; ++j)
+      for (long i = 0; i < nx; ++i) {
+        const long index = i + j * nx + k * nx * ny;
+        std::fprintf(fd, "%d %d %d %.6e %.6e %.6e %.6e %.6e %d %d\n", (int)i, (int)j, (int)k, T[index], S[index],
+                     rho[index], C[index], kappa[index], (int)flag[index], (int)T_dynamic[index]);
+      }
+  std::fclose(fd);
+  return 0;
+}
+
+int Grid::save_temperature(const char *path, int n) const {
+  char fn[4096];
+  std::snprintf(fn, sizeof fn, "%s_%06d", path, n);
+  FILE *fd = std::fopen(fn, "w");
+  if (!fd) return 1;
+  std::fprintf(fd, "x y z Te\n");
+  for (long k = 0; k < nz; ++k)
+    for (long j = 0; j < ny; ++j)
+      for (long i = 0; i < nx; ++i) {
+        const long index = i + j * nx + k * nx * ny;
+        const double x = x0 + (int)i * dx, y = y0 + (int)j * dy, z = z0 + (int)k * dz;
+        std::fprintf(fd, "%.6e %.6e %.6e %.6e\n", x, y, z, T[index]);
+      }
+  std::fclose(fd);
+  return 0;
+}
+
+int parse_fix_args(int narg, const char *const *arg, FixArgs *a, std::string *why) {
+  if (narg < 18) {
+    *why = "Illegal fix eph command: too few arguments";
+    return EPH_ERR_ARG;
+  }
+  a->seed = std::atoi(arg[3]);
+  a->flags = (int)std::strtol(arg[4], nullptr, 0);
+  a->model = std::atoi(arg[5]);
+  a->rho_e = std::atof(arg[6]);
+  a->C_e = std::atof(arg[7]);
+  a->kappa_e = std::atof(arg[8]);
+  a->T_e = std::atof(arg[9]);
+  a->nx = std::atoi(arg[10]);
+  a->ny = std::atoi(arg[11]);
+  a->nz = std::atoi(arg[12]);
+  a->T_infile = arg[13];
+  if (a->T_infile == "NULL") {
+    if (a->nx < 1 || a->ny < 1 || a->nz < 1) {
+      *why = "FixEPH: non-positive grid values";
+      return EPH_ERR_ARG;
+    }
+    a->T_state = "T.restart";
+  } else {
+    a->T_state = a->T_infile + ".restart";
+  }
+  a->T_freq = std::atoi(arg[14]);
+  if (a->T_freq > 0) a->T_out = arg[15];
+  a->beta_file = arg[16];
+  a->elements.clear();
+  for (int i = 17; i < narg; ++i) a->elements.emplace_back(arg[i]);
+  return EPH_OK;
+}
+
+}  // namespace ephgb

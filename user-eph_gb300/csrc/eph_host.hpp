@@ -1,0 +1,93 @@
+// Host side of the GB300 fix-eph path: the beta(rho) parametrisation, the
+// electronic-temperature grid and the fix argument parser.  Everything here
+// runs on the CPU once per set-up (or per file write); the per-step work is in
+// eph_kernels.cuh.  Compiled without floating-point contraction so that the
+// spline tables and grid constants are the reference's to the last bit.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace ephgb {
+
+// Cubic spline of eph_spline.h (Akima-type slopes, coefficients in absolute x,
+// evaluated as a + x(b + x(c + x d)) with index floor(x / dx)).
+struct Spline {
+  double inv_dx = 0.0;
+  std::vector<double> c;  // a, b, c, d per knot
+  long n = 0;
+  // eph_spline.h:31-132
+  void build(double dx, const std::vector<double> &y);
+  // eph_spline.h:134-142
+  double operator()(double x) const;
+};
+
+// beta(rho) file of eph_beta.h:39-128: per element rho(r), rho(r^2) (re-spline
+// of rho(r) sampled at sqrt(j dr^2)), beta(rho) and alpha(rho) = spline of
+// sqrt(beta) knots.
+struct Beta {
+  int n_elements = 0;
+  std::vector<std::string> names;
+  std::vector<int> numbers;
+  double r_cutoff = 0, r_cutoff_sq = 0, rho_cutoff = 0;
+  long n_rho = 0, n_beta = 0;
+  double dr = 0, dr_sq = 0, drho = 0;
+  std::vector<Spline> rho, rho_r_sq, beta, alpha;
+  // returns an empty string on success, else the reason
+  std::string load(const char *path);
+  const Spline &table(int which, int elem) const;
+  // eph_beta.h:174-197 (zero above rho_cutoff)
+  double get_beta(int elem, double r) const;
+  double get_alpha(int elem, double r) const;
+};
+
+enum : int { GRID_CONSTANT = 0, GRID_DYNAMIC = 1, GRID_ZERO_DERIVATIVE = 2 };
+
+// Electronic grid of eph_fdm.h: uniform (constructor :28-46) or read from a
+// grid file (:48-119); index i + j nx + k nx ny.
+struct Grid {
+  long nx = 1, ny = 1, nz = 1, ntotal = 1;
+  double x0 = 0, x1 = 1, y0 = 0, y1 = 1, z0 = 0, z1 = 1, dx = 1, dy = 1, dz = 1, dV = 1;
+  std::vector<double> T, S, rho, C, kappa;
+  std::vector<int16_t> flag;
+  std::vector<uint16_t> T_dynamic;
+  std::string parameter_filename = "NULL";
+  long steps = 1;
+  double dt = 1;
+
+  void create(long nx, long ny, long nz, double x0, double x1, double y0, double y1, double z0, double z1,
+              double T_e, double C_e, double rho_e, double kappa_e);
+  std::string load(const char *path);
+  void set_box(double x0, double x1, double y0, double y1, double z0, double z1);
+  // eph_fdm.h:275-313: number and length of the stability substeps of solve()
+  unsigned substeps(double *inner_dt) const;
+  // eph_fdm.h:226-265 and :198-224, same text format
+  int save_state(const char *path) const;
+  int save_temperature(const char *path, int n) const;
+};
+
+// Parsed `fix ID group eph seed flags model rho_e C_e kappa_e T_e NX NY NZ
+// T_infile freq T_out beta_file A B ...` (fix_eph.cpp:36-58, :61-241).
+struct FixArgs {
+  int seed = 0, flags = 0, model = 0;
+  double rho_e = 0, C_e = 0, kappa_e = 0, T_e = 0;
+  int nx = 0, ny = 0, nz = 0;
+  std::string T_infile, T_out, beta_file, T_state;
+  int T_freq = 0;
+  std::vector<std::string> elements;
+};
+
+enum : int {
+  FLAG_FRICTION = 0x01,
+  FLAG_RANDOM = 0x02,
+  FLAG_FDM = 0x04,
+  FLAG_NOINT = 0x08,
+  FLAG_NOFRICTION = 0x10,
+  FLAG_NORANDOM = 0x20
+};
+
+// Returns 0 or an EPH_ERR_* code with `why` filled.
+int parse_fix_args(int narg, const char *const *arg, FixArgs *out, std::string *why);
+
+}  // namespace ephgb

@@ -1,0 +1,842 @@
+// sm_103a kernels of the fix-eph hot path.
+//
+// One thread per atom for every per-atom sweep.  The FP64 pipe of GB300
+// issues about two instructions per clock per SM, so these kernels are bound
+// by FP64 instruction issue, not by HBM: the design removes FP64 work
+// (in-cutoff pairs compacted per step so the warps sweep them in lockstep,
+// pair geometry and rho(r^2) cached once per step, alpha/beta per atom once)
+// and keeps integer/FP32 work (binning, candidate tests, sorting) off the
+// FP64 pipe.
+//
+// This translation unit is compiled with -fmad=false: in EXACT mode every
+// product and sum rounds separately, in the reference's order, so forces and
+// densities equal the reference's bit for bit; FAST mode writes its FMAs
+// explicitly.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ephgb {
+
+struct __align__(32) D4 {
+  double x, y, z, w;
+};
+
+struct __align__(16) BinEntry {
+  unsigned idx;  // atom index | wrap code << 27
+  float ox, oy, oz;  // offset of the atom inside its unwrapped bin
+};
+
+struct __align__(16) U128 {
+  unsigned long long lo, hi;  // two's-complement 128-bit fixed point, 2^-64 units
+};
+
+constexpr int KMAX = 128;  // local candidate array of one atom
+constexpr unsigned IDX_BITS = 27;
+constexpr unsigned IDX_MASK = (1u << IDX_BITS) - 1u;
+constexpr unsigned CODE_NOSHIFT = 13;  // (0,0,0) image of the 3x3x3 code
+
+enum : unsigned {
+  ERR_BIN_OVERFLOW = 1u,
+  ERR_PAIR_OVERFLOW = 2u,
+  ERR_DRIFT = 4u,
+  ERR_Q_RANGE = 8u,
+  ERR_SPLINE_RANGE = 16u,
+  ERR_TIMEOUT = 32u
+};
+
+enum : int { CNT_RHO_CUTOFF = 0, CNT_T_CLAMP = 1, CNT_BUILD = 2, CNT_WRAP = 3, NCOUNTERS = 4 };
+
+// Everything a step's kernels read besides the big arrays.
+struct StepParams {
+  int n;
+  int flags;
+  int groupbit;
+  int nelem;
+  double lo[3], hi[3], prd[3];
+  double rc2;         // r_cutoff^2 (eph_beta.h:85)
+  float rc2_band;     // FP32 candidate threshold, rc^2 (1 + 1e-4)
+  int nb[3];          // bins per axis (>= 3), bin edge >= r_cutoff (1 + 5e-5)
+  double inv_w[3], w[3];
+  float wf[3];
+  int bcap, kcap;
+  // splines: tables of element e start at e * n_knots
+  const D4 *tab_rho_r_sq;
+  const D4 *tab_beta;
+  const D4 *tab_alpha;
+  double inv_dr_sq, inv_drho;
+  int n_rho, n_beta;
+  double rho_cutoff;
+  // integrator and forces
+  double dtv, dt, eta, triggersq;
+  double dtfm[65];  // dtf / mass[type], type 1..64 (fix_eph.cpp:314)
+  int type_map[65];  // LAMMPS type -> element
+  // grid
+  long gnx, gny, gnz, ncells;
+  double gx0, gy0, gz0, gdx, gdy, gdz;
+  double prescale;  // dV * dt (eph_fdm.h:176)
+  // random numbers
+  unsigned seed;
+  unsigned long long step;
+};
+
+// ------------------------------------------------------------------ helpers
+
+template <bool FAST>
+__device__ __forceinline__ double spline_eval(const D4 *__restrict__ tab, double inv_dx, int n, double x,
+                                              unsigned *err) {
+  // eph_spline.h:134-142: index floor(x/dx), value a + x(b + x(c + x d))
+  unsigned long long idx = (unsigned long long)(x * inv_dx);
+  if (idx >= (unsigned long long)n) {
+    atomicOr(err, ERR_SPLINE_RANGE);
+    idx = (unsigned long long)(n - 1);
+  }
+  const D4 c = tab[idx];
+  if (FAST) return fma(x, fma(x, fma(x, c.w, c.z), c.y), c.x);
+  return c.x + x * (c.y + x * (c.z + x * c.w));
+}
+
+__device__ __forceinline__ double dot3(double ax, double ay, double az, double bx, double by, double bz) {
+  return ax * bx + ay * by + az * bz;  // ((ax bx + ay by) + az bz), fix_eph.h:160-163
+}
+
+__device__ __forceinline__ double dot3_fma(double ax, double ay, double az, double bx, double by, double bz) {
+  return fma(az, bz, fma(ay, by, ax * bx));
+}
+
+// eph_fdm.h:494-509: cell of a position, floor-wrapped into the grid
+__device__ __forceinline__ long grid_index(const StepParams &P, double x, double y, double z) {
+  int lx = (int)floor((x - P.gx0) / P.gdx);
+  int px = (int)floor(((double)lx) / (double)P.gnx);
+  lx -= px * (int)P.gnx;
+  int ly = (int)floor((y - P.gy0) / P.gdy);
+  int py = (int)floor(((double)ly) / (double)P.gny);
+  ly -= py * (int)P.gny;
+  int lz = (int)floor((z - P.gz0) / P.gdz);
+  int pz = (int)floor(((double)lz) / (double)P.gnz);
+  lz -= pz * (int)P.gnz;
+  return (long)lx + (long)ly * P.gnx + (long)lz * P.gnx * P.gny;
+}
+
+// ---------------------------------------------------- fixed-point deposits
+
+// Round t * 2^64 to the nearest integer as a 128-bit two's-complement value.
+// Integer work only.  |t| must stay below 2^62.
+__device__ __forceinline__ U128 to_fixed(double t, unsigned *err) {
+  U128 r{0ull, 0ull};
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(t);
+  const int e = (int)((bits >> 52) & 0x7ffu);
+  if (e == 0) return r;  // zero or subnormal: far below one unit
+  const unsigned long long m = (bits & ((1ull << 52) - 1ull)) | (1ull << 52);
+  const int sh = e - 1011;  // value * 2^64 = m * 2^(e - 1075 + 64)
+  unsigned long long lo, hi;
+  if (sh >= 74) {
+    atomicOr(err, ERR_Q_RANGE);
+    return r;
+  } else if (sh >= 64) {
+    lo = 0ull;
+    hi = m << (sh - 64);
+  } else if (sh > 11) {
+    lo = m << sh;
+    hi = m >> (64 - sh);
+  } else if (sh >= 0) {
+    lo = m << sh;
+    hi = 0ull;
+  } else if (sh > -54) {
+    const int s = -sh;
+    lo = (m + (1ull << (s - 1))) >> s;  // round half up on the magnitude
+    hi = 0ull;
+  } else {
+    return r;
+  }
+  if ((long long)bits < 0) {  // negate: ~v + 1
+    lo = ~lo;
+    hi = ~hi;
+    lo += 1ull;
+    if (lo == 0ull) hi += 1ull;
+  }
+  r.lo = lo;
+  r.hi = hi;
+  return r;
+}
+
+__device__ __forceinline__ U128 add128(U128 a, U128 b) {
+  U128 r;
+  r.lo = a.lo + b.lo;
+  r.hi = a.hi + b.hi + (r.lo < a.lo ? 1ull : 0ull);
+  return r;
+}
+
+__device__ __forceinline__ void atomic_add128(U128 *dst, U128 v) {
+  const unsigned long long old = atomicAdd(&dst->lo, v.lo);
+  const unsigned long long carry = (old + v.lo < old) ? 1ull : 0ull;
+  atomicAdd(&dst->hi, v.hi + carry);
+}
+
+__device__ __forceinline__ double from_fixed(U128 v) {
+  // v * 2^-64 = (signed hi) + lo * 2^-64
+  return (double)(long long)v.hi + (double)v.lo * 5.421010862427522170037264e-20;
+}
+
+__device__ __forceinline__ U128 shfl_down128(U128 v, int d) {
+  U128 r;
+  r.lo = __shfl_down_sync(0xffffffffu, v.lo, d);
+  r.hi = __shfl_down_sync(0xffffffffu, v.hi, d);
+  return r;
+}
+
+// ------------------------------------------------------------ random numbers
+
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11): ten rounds of two
+// 32x32->64 multiplies with a Weyl-sequence key schedule.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+  const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k.x += W0;
+      k.y += W1;
+    }
+    const unsigned hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const unsigned hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+  }
+  return c;
+}
+
+// Three standard normal deviates for atom i at step s (Box-Muller on 32-bit
+// uniforms in (0, 1)).
+__device__ __forceinline__ void gaussian3(unsigned seed, unsigned long long step, unsigned i, double *g) {
+  const uint4 r = philox4x32_10(make_uint4(i, (unsigned)step, (unsigned)(step >> 32), 0x45504847u),
+                                make_uint2(seed, 0x9e3779b9u));
+  const float u0 = ((float)r.x + 0.5f) * 2.3283064365386963e-10f;
+  const float u1 = ((float)r.y + 0.5f) * 2.3283064365386963e-10f;
+  const float u2 = ((float)r.z + 0.5f) * 2.3283064365386963e-10f;
+  const float u3 = ((float)r.w + 0.5f) * 2.3283064365386963e-10f;
+  const float ra = sqrtf(-2.0f * logf(u0)), rb = sqrtf(-2.0f * logf(u2));
+  float sa, ca, sb, cb;
+  sincospif(2.0f * u1, &sa, &ca);
+  sincospif(2.0f * u3, &sb, &cb);
+  g[0] = (double)(ra * ca);
+  g[1] = (double)(ra * sa);
+  g[2] = (double)(rb * cb);
+}
+
+// ------------------------------------------------------------- integrator
+
+// FixEPH::initial_integrate (fix_eph.cpp:305-328) and the engine's rebuild
+// test (an atom moved more than skin/2 since the last wrap).
+template <bool FAST>
+__global__ void k_initial_integrate(StepParams P, D4 *__restrict__ x, D4 *__restrict__ v,
+                                    const D4 *__restrict__ f, const int *__restrict__ type,
+                                    const int *__restrict__ mask, const D4 *__restrict__ xhold, int check_wrap,
+                                    int *__restrict__ wrapflag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool moved = false;
+  if (i < P.n) {
+    D4 xi = x[i];
+    if (!(P.flags & 0x08) && (mask[i] & P.groupbit)) {
+      D4 vi = v[i];
+      const D4 fi = f[i];
+      const double dtfm = P.dtfm[type[i]];
+      if (FAST) {
+        vi.x = fma(dtfm, fi.x, vi.x);
+        vi.y = fma(dtfm, fi.y, vi.y);
+        vi.z = fma(dtfm, fi.z, vi.z);
+        xi.x = fma(P.dtv, vi.x, xi.x);
+        xi.y = fma(P.dtv, vi.y, xi.y);
+        xi.z = fma(P.dtv, vi.z, xi.z);
+      } else {
+        vi.x += dtfm * fi.x;
+        vi.y += dtfm * fi.y;
+        vi.z += dtfm * fi.z;
+        xi.x += P.dtv * vi.x;
+        xi.y += P.dtv * vi.y;
+        xi.z += P.dtv * vi.z;
+      }
+      v[i] = vi;
+      x[i] = xi;
+    }
+    if (check_wrap) {
+      const D4 h = xhold[i];
+      const double dx = xi.x - h.x, dy = xi.y - h.y, dz = xi.z - h.z;
+      moved = dx * dx + dy * dy + dz * dz > P.triggersq;
+    }
+  }
+  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(wrapflag, 1);
+}
+
+// FixEPH::final_integrate (fix_eph.cpp:330-348)
+template <bool FAST>
+__global__ void k_final_integrate(StepParams P, D4 *__restrict__ v, const D4 *__restrict__ f,
+                                  const int *__restrict__ type, const int *__restrict__ mask) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n || (P.flags & 0x08) || !(mask[i] & P.groupbit)) return;
+  D4 vi = v[i];
+  const D4 fi = f[i];
+  const double dtfm = P.dtfm[type[i]];
+  if (FAST) {
+    vi.x = fma(dtfm, fi.x, vi.x);
+    vi.y = fma(dtfm, fi.y, vi.y);
+    vi.z = fma(dtfm, fi.z, vi.z);
+  } else {
+    vi.x += dtfm * fi.x;
+    vi.y += dtfm * fi.y;
+    vi.z += dtfm * fi.z;
+  }
+  v[i] = vi;
+}
+
+// ------------------------------------------------------------------ binning
+
+// Wrap positions into [lo, hi) when the engine rebuilds (LAMMPS Domain::pbc
+// for an orthogonal box), then drop every atom into its spatial bin.  A bin
+// edge is at least the cutoff, so all pairs inside the cutoff are found in
+// the 27 bins around an atom.  Bins keep unwrapped coordinates: an atom that
+// drifted up to one bin outside the box carries a wrap code and the offset
+// from its own (unwrapped) bin corner.
+__global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, const int *__restrict__ wrapflag,
+                      int *__restrict__ bin_count, BinEntry *__restrict__ bins, int4 *__restrict__ atom_bin,
+                      float4 *__restrict__ atom_off, unsigned *__restrict__ err,
+                      unsigned long long *__restrict__ counters) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  D4 xi = x[i];
+  if (*wrapflag) {
+    double *c[3] = {&xi.x, &xi.y, &xi.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double q = *c[k];
+      if (q < P.lo[k]) q += P.prd[k];
+      if (q >= P.hi[k]) {
+        q -= P.prd[k];
+        q = q > P.lo[k] ? q : P.lo[k];
+      }
+      *c[k] = q;
+    }
+    x[i] = xi;
+    xhold[i] = xi;
+    if (i == 0) atomicAdd(&counters[CNT_WRAP], 1ull);
+  }
+  const double p[3] = {xi.x, xi.y, xi.z};
+  int B[3], t[3], wc[3];
+  float o[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double s = p[k] - P.lo[k];
+    int b = (int)floor(s * P.inv_w[k]);
+    if (b < -1 || b > P.nb[k]) {
+      atomicOr(err, ERR_DRIFT);
+      b = b < -1 ? -1 : P.nb[k];
+    }
+    B[k] = b;
+    t[k] = b < 0 ? b + P.nb[k] : (b >= P.nb[k] ? b - P.nb[k] : b);
+    wc[k] = (b - t[k]) / P.nb[k];
+    o[k] = (float)(s - (double)b * P.w[k]);
+  }
+  const int flat = t[0] + P.nb[0] * (t[1] + P.nb[1] * t[2]);
+  const unsigned code = (unsigned)((wc[0] + 1) + 3 * (wc[1] + 1) + 9 * (wc[2] + 1));
+  const int slot = atomicAdd(&bin_count[flat], 1);
+  if (slot < P.bcap) {
+    BinEntry be;
+    be.idx = (unsigned)i | (code << IDX_BITS);
+    be.ox = o[0];
+    be.oy = o[1];
+    be.oz = o[2];
+    bins[(size_t)flat * P.bcap + slot] = be;
+  } else {
+    atomicOr(err, ERR_BIN_OVERFLOW);
+  }
+  atom_bin[i] = make_int4(B[0], B[1], B[2], flat);
+  atom_off[i] = make_float4(o[0], o[1], o[2], 0.f);
+}
+
+// -------------------------------------------------------- density sweep
+
+// calculate_environment (fix_eph.cpp:431-466) plus everything per atom the
+// later sweeps need.  Per atom: (1) candidates from the 27 bins with an FP32
+// distance test padded by 1e-4 of rc^2, kept in ascending neighbour index
+// (the order of the reference's list, so sums round identically); (2) the
+// exact FP64 test r^2 < rc^2 with e = (x_j + image) - x_i, the density sum,
+// and the pair cache of the in-cutoff pairs for the force sweeps.
+//
+// Pair cache row k of atom i sits at k*n + i (coalesced across the warp):
+//   pj: neighbour index | image code << 27
+//   pe: e_ij and (EXACT) r^2 or (FAST) rho_j(r^2)/r^2
+//   pg: (EXACT) rho_j(r^2), rho_i(r^2); (FAST) rho_i(r^2)/r^2 in .x
+// A[i] = {rho_i, alpha_i (EXACT) | alpha_i/rho_i (FAST), xi_x, xi_y}
+// Bw[i] = {xi_z, w_i} (w written by the friction sweep)
+template <bool FAST, bool MULTI>
+__global__ void __launch_bounds__(128) k_density(
+    StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
+    const BinEntry *__restrict__ bins, const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
+    const D4 *__restrict__ xi_given, int xi_mode, const double *__restrict__ T_e, unsigned *__restrict__ pj,
+    D4 *__restrict__ pe, double2 *__restrict__ pg, int *__restrict__ nshort, D4 *__restrict__ A,
+    D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell,
+    double *__restrict__ Te_i, int *__restrict__ wrapflag, unsigned *__restrict__ err,
+    unsigned long long *__restrict__ counters) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *wrapflag = 0;  // the binning kernel has read it
+  if (i >= P.n) return;
+  const bool in_group = (mask[i] & P.groupbit) != 0;
+  const D4 xi = x[i];
+  const int ei = (int)xi.w;
+  double rho = 0.0;
+  int ns = 0;
+  if (in_group) {
+    unsigned cand[KMAX];
+    int nc = 0;
+    const int4 Bi = atom_bin[i];
+    const float4 oi = atom_off[i];
+    const int Bv[3] = {Bi.x, Bi.y, Bi.z};
+    // pass 1: candidates, FP32/integer work only
+    for (int dz = -1; dz <= 1; ++dz) {
+      int Tz = Bv[2] + dz, tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
+      const int kz = Tz < 0 ? -1 : (Tz >= P.nb[2] ? 1 : 0);
+      const float bz = (float)dz * P.wf[2] - oi.z;
+      for (int dy = -1; dy <= 1; ++dy) {
+        int Ty = Bv[1] + dy, ty = Ty < 0 ? Ty + P.nb[1] : (Ty >= P.nb[1] ? Ty - P.nb[1] : Ty);
+        const int ky = Ty < 0 ? -1 : (Ty >= P.nb[1] ? 1 : 0);
+        const float by = (float)dy * P.wf[1] - oi.y;
+        for (int dx = -1; dx <= 1; ++dx) {
+          int Tx = Bv[0] + dx, tx = Tx < 0 ? Tx + P.nb[0] : (Tx >= P.nb[0] ? Tx - P.nb[0] : Tx);
+          const int kx = Tx < 0 ? -1 : (Tx >= P.nb[0] ? 1 : 0);
+          const float bx = (float)dx * P.wf[0] - oi.x;
+          const int flat = tx + P.nb[0] * (ty + P.nb[1] * tz);
+          int cnt = bin_count[flat];
+          cnt = cnt < P.bcap ? cnt : P.bcap;
+          const BinEntry *be = bins + (size_t)flat * P.bcap;
+          for (int s = 0; s < cnt; ++s) {
+            const BinEntry b = be[s];
+            const unsigned j = b.idx & IDX_MASK;
+            if (j == (unsigned)i) continue;
+            const float ex = bx + b.ox, ey = by + b.oy, ez = bz + b.oz;
+            const float r2 = ex * ex + ey * ey + ez * ez;
+            if (r2 >= P.rc2_band) continue;
+            const unsigned wc = b.idx >> IDX_BITS;
+            const int mx = kx - ((int)(wc % 3u) - 1), my = ky - ((int)((wc / 3u) % 3u) - 1),
+                      mz = kz - ((int)(wc / 9u) - 1);
+            if (mx < -1 || mx > 1 || my < -1 || my > 1 || mz < -1 || mz > 1) {
+              atomicOr(err, ERR_DRIFT);
+              continue;
+            }
+            if (nc >= KMAX || nc >= P.kcap) {
+              atomicOr(err, ERR_PAIR_OVERFLOW);
+              continue;
+            }
+            const unsigned u = j | ((unsigned)((mx + 1) + 3 * (my + 1) + 9 * (mz + 1)) << IDX_BITS);
+            int pos = nc++;
+            while (pos > 0 && (cand[pos - 1] & IDX_MASK) > j) {
+              cand[pos] = cand[pos - 1];
+              --pos;
+            }
+            cand[pos] = u;
+          }
+        }
+      }
+    }
+    // pass 2: exact FP64 test, density and pair cache
+    for (int k = 0; k < nc; ++k) {
+      const unsigned u = cand[k];
+      const unsigned j = u & IDX_MASK, code = u >> IDX_BITS;
+      const D4 xj = x[j];
+      double cx = xj.x, cy = xj.y, cz = xj.z;
+      if (code != CODE_NOSHIFT) {
+        const int mx = (int)(code % 3u) - 1, my = (int)((code / 3u) % 3u) - 1, mz = (int)(code / 9u) - 1;
+        if (mx) cx = xj.x + (mx > 0 ? P.prd[0] : -P.prd[0]);
+        if (my) cy = xj.y + (my > 0 ? P.prd[1] : -P.prd[1]);
+        if (mz) cz = xj.z + (mz > 0 ? P.prd[2] : -P.prd[2]);
+      }
+      const double ex = cx - xi.x, ey = cy - xi.y, ez = cz - xi.z;
+      const double r2 = FAST ? dot3_fma(ex, ey, ez, ex, ey, ez) : dot3(ex, ey, ez, ex, ey, ez);
+      if (!(r2 < P.rc2)) continue;
+      const int ej = (int)xj.w;
+      const double rji = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+      double rij = rji;
+      if (MULTI && ej != ei)
+        rij = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+      rho += rji;
+      const size_t slot = (size_t)ns * P.n + i;
+      pj[slot] = u;
+      if (FAST) {
+        const double inv_r2 = 1.0 / r2;
+        pe[slot] = D4{ex, ey, ez, rji * inv_r2};
+        pg[slot] = make_double2(rij * inv_r2, 0.0);
+      } else {
+        pe[slot] = D4{ex, ey, ez, r2};
+        pg[slot] = make_double2(rji, rij);
+      }
+      ++ns;
+    }
+  }
+  nshort[i] = ns;
+  // per-atom quantities
+  double alpha = 0.0, beta = 0.0, xi3[3] = {0.0, 0.0, 0.0};
+  if (in_group) {
+    if (rho > P.rho_cutoff) {  // eph_beta.h:174-197
+      atomicAdd(&counters[CNT_RHO_CUTOFF], 1ull);
+    } else {
+      beta = spline_eval<FAST>(P.tab_beta + (size_t)ei * P.n_beta, P.inv_drho, P.n_beta, rho, err);
+      if (rho > 0) alpha = spline_eval<FAST>(P.tab_alpha + (size_t)ei * P.n_beta, P.inv_drho, P.n_beta, rho, err);
+    }
+    if (FAST && rho > 0) alpha = alpha / rho;
+    if (P.flags & 0x02) {
+      if (xi_mode == 0) {
+        gaussian3(P.seed, P.step, (unsigned)i, xi3);
+      } else {
+        const D4 g = xi_given[i];
+        xi3[0] = g.x;
+        xi3[1] = g.y;
+        xi3[2] = g.z;
+      }
+    }
+    const long c = grid_index(P, xi.x, xi.y, xi.z);
+    cell[i] = (int)c;
+    Te_i[i] = T_e[c];
+  }
+  A[i] = D4{rho, alpha, xi3[0], xi3[1]};
+  Bw[i] = D4{xi3[2], 0.0, 0.0, 0.0};
+  rho_out[i] = rho;
+  beta_out[i] = beta;
+}
+
+// -------------------------------------------------------- friction sweep 1
+
+// force_prl stage 1 (fix_eph.cpp:699-741):
+// w_i = sum_j p_ij [(e.v_i) - (e.v_j)] e,  p_ij = alpha_i rho_j(r^2) / (rho_i r^2)
+template <bool FAST>
+__global__ void __launch_bounds__(128) k_friction_w(StepParams P, const int *__restrict__ mask,
+                                                     const D4 *__restrict__ v, const unsigned *__restrict__ pj,
+                                                     const D4 *__restrict__ pe, const double2 *__restrict__ pg,
+                                                     const int *__restrict__ nshort, const D4 *__restrict__ A,
+                                                     D4 *__restrict__ Bw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const D4 Ai = A[i];
+  if (!(mask[i] & P.groupbit) || !(Ai.x > 0)) return;  // Bw[i].yzw stays 0
+  const D4 vi = v[i];
+  const int ns = nshort[i];
+  double wx = 0.0, wy = 0.0, wz = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    const size_t slot = (size_t)k * P.n + i;
+    const unsigned j = pj[slot] & IDX_MASK;
+    const D4 e = pe[slot];
+    const D4 vj = v[j];
+    if (FAST) {
+      const double c = Ai.y * e.w;  // alpha_i/rho_i * rho_j(r^2)/r^2
+      const double d = dot3_fma(e.x, e.y, e.z, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
+      const double s = c * d;
+      wx = fma(s, e.x, wx);
+      wy = fma(s, e.y, wy);
+      wz = fma(s, e.z, wz);
+    } else {
+      const double rji = pg[slot].x;
+      const double prescaler = Ai.y * rji / (Ai.x * e.w);
+      const double var1 = prescaler * dot3(e.x, e.y, e.z, vi.x, vi.y, vi.z);
+      const double var2 = prescaler * dot3(e.x, e.y, e.z, vj.x, vj.y, vj.z);
+      const double dvar = var1 - var2;
+      wx += dvar * e.x;
+      wy += dvar * e.y;
+      wz += dvar * e.z;
+    }
+  }
+  const double xiz = Bw[i].x;
+  Bw[i] = D4{xiz, wx, wy, wz};
+}
+
+// ------------------------------------------------ friction + random sweep
+
+// force_prl stages 2 and 3 (fix_eph.cpp:748-836) in one pass over the pairs,
+// then the force update of post_force (fix_eph.cpp:892-906):
+//   f_EPH_i -= sum_j [a_i rho_j(r^2) (e.w_i)/(rho_i r^2) - a_j rho_i(r^2) (e.w_j)/(rho_j r^2)] e
+//   f_RNG_i  = eta sqrt(T_e(x_i)) sum_j [same with xi] e
+template <bool FAST, bool MULTI, bool FRIC, bool RAND>
+__global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restrict__ mask,
+                                                const unsigned *__restrict__ pj, const D4 *__restrict__ pe,
+                                                const double2 *__restrict__ pg, const int *__restrict__ nshort,
+                                                const D4 *__restrict__ A, const D4 *__restrict__ Bw,
+                                                const double *__restrict__ Te_i, D4 *__restrict__ f,
+                                                D4 *__restrict__ f_eph, D4 *__restrict__ f_rng) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  double fex = 0.0, fey = 0.0, fez = 0.0, frx = 0.0, fry = 0.0, frz = 0.0;
+  const D4 Ai = A[i];
+  if ((mask[i] & P.groupbit) && Ai.x > 0) {
+    const D4 Bi = Bw[i];
+    const double xix = Ai.z, xiy = Ai.w, xiz = Bi.x;
+    const int ns = nshort[i];
+    for (int k = 0; k < ns; ++k) {
+      const size_t slot = (size_t)k * P.n + i;
+      const unsigned j = pj[slot] & IDX_MASK;
+      const D4 Aj = A[j];
+      if (!(Aj.x > 0)) continue;
+      const D4 e = pe[slot];
+      const double2 g = pg[slot];
+      const D4 Bj = Bw[j];
+      if (FAST) {
+        const double a = Ai.y * e.w;                  // alpha_i/rho_i * rho_j(r^2)/r^2
+        const double b = Aj.y * (MULTI ? g.x : e.w);  // alpha_j/rho_j * rho_i(r^2)/r^2
+        if (FRIC) {
+          const double di = dot3_fma(e.x, e.y, e.z, Bi.y, Bi.z, Bi.w);
+          const double dj = dot3_fma(e.x, e.y, e.z, Bj.y, Bj.z, Bj.w);
+          const double dvar = fma(a, di, -(b * dj));
+          fex = fma(-dvar, e.x, fex);
+          fey = fma(-dvar, e.y, fey);
+          fez = fma(-dvar, e.z, fez);
+        }
+        if (RAND) {
+          const double di = dot3_fma(e.x, e.y, e.z, xix, xiy, xiz);
+          const double dj = dot3_fma(e.x, e.y, e.z, Aj.z, Aj.w, Bj.x);
+          const double dvar = fma(a, di, -(b * dj));
+          frx = fma(dvar, e.x, frx);
+          fry = fma(dvar, e.y, fry);
+          frz = fma(dvar, e.z, frz);
+        }
+      } else {
+        const double r2 = e.w;
+        const double ai = Ai.y * g.x;                 // alpha_i * rho_j(r^2)
+        const double aj = Aj.y * (MULTI ? g.y : g.x);  // alpha_j * rho_i(r^2)
+        const double den_i = Ai.x * r2, den_j = Aj.x * r2;
+        if (FRIC) {
+          const double var1 = ai * dot3(e.x, e.y, e.z, Bi.y, Bi.z, Bi.w) / den_i;
+          const double var2 = aj * dot3(e.x, e.y, e.z, Bj.y, Bj.z, Bj.w) / den_j;
+          const double dvar = var1 - var2;
+          fex -= dvar * e.x;
+          fey -= dvar * e.y;
+          fez -= dvar * e.z;
+        }
+        if (RAND) {
+          const double var1 = ai * dot3(e.x, e.y, e.z, xix, xiy, xiz) / den_i;
+          const double var2 = aj * dot3(e.x, e.y, e.z, Aj.z, Aj.w, Bj.x) / den_j;
+          const double dvar = var1 - var2;
+          frx += dvar * e.x;
+          fry += dvar * e.y;
+          frz += dvar * e.z;
+        }
+      }
+    }
+    if (RAND) {
+      const double var = P.eta * sqrt(Te_i[i]);
+      frx *= var;
+      fry *= var;
+      frz *= var;
+    }
+  }
+  f_eph[i] = D4{fex, fey, fez, 0.0};
+  f_rng[i] = D4{frx, fry, frz, 0.0};
+  D4 fi = f[i];
+  if (FRIC && !(P.flags & 0x10)) {
+    fi.x += fex;
+    fi.y += fey;
+    fi.z += fez;
+  }
+  if (RAND && !(P.flags & 0x20)) {
+    fi.x += frx;
+    fi.y += fry;
+    fi.z += frz;
+  }
+  f[i] = fi;
+}
+
+// ------------------------------------------------------- energy deposition
+
+// end_of_step deposition (fix_eph.cpp:364-390, eph_fdm.h:172-179): per atom
+// dE = -f.v dt for the friction and the random force, dT_e[cell] += dE/(dV dt).
+// The grid sums are exact: every term becomes a 128-bit fixed-point integer
+// (2^-64 units) and integer addition is order-free, so the grid and the
+// energy total are the same whatever order the atoms arrive in; the block
+// totals of the energy go to `part` and are summed by k_energy_total.
+template <bool FRIC, bool RAND, bool GRID>
+__global__ void __launch_bounds__(256) k_deposit(StepParams P, const int *__restrict__ mask,
+                                                 const D4 *__restrict__ v, const D4 *__restrict__ f_eph,
+                                                 const D4 *__restrict__ f_rng, const int *__restrict__ cell,
+                                                 U128 *__restrict__ acc, U128 *__restrict__ part,
+                                                 unsigned *__restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  U128 e{0ull, 0ull};
+  if (i < P.n && (mask[i] & P.groupbit)) {
+    const D4 vi = v[i];
+    U128 g{0ull, 0ull};
+    if (FRIC) {
+      const D4 fe = f_eph[i];
+      double dE = 0.0;
+      dE -= fe.x * vi.x * P.dt;
+      dE -= fe.y * vi.y * P.dt;
+      dE -= fe.z * vi.z * P.dt;
+      e = add128(e, to_fixed(dE, err));
+      if (GRID) g = add128(g, to_fixed(dE / P.prescale, err));
+    }
+    if (RAND) {
+      const D4 fr = f_rng[i];
+      double dE = 0.0;
+      dE -= fr.x * vi.x * P.dt;
+      dE -= fr.y * vi.y * P.dt;
+      dE -= fr.z * vi.z * P.dt;
+      e = add128(e, to_fixed(dE, err));
+      if (GRID) g = add128(g, to_fixed(dE / P.prescale, err));
+    }
+    if (GRID && (g.lo | g.hi)) atomic_add128(acc + cell[i], g);
+  }
+  // block total of the energy, integer adds
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) e = add128(e, shfl_down128(e, d));
+  __shared__ U128 warp_tot[8];
+  if ((threadIdx.x & 31) == 0) warp_tot[threadIdx.x >> 5] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    U128 t{0ull, 0ull};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = add128(t, warp_tot[w]);
+    part[blockIdx.x] = t;
+  }
+}
+
+// Sum the block totals, add the step's exchange to Ee (fix_eph.cpp:402-404).
+__global__ void k_energy_total(const U128 *__restrict__ part, int nparts, double *__restrict__ E_local,
+                               double *__restrict__ Ee) {
+  U128 t{0ull, 0ull};
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) t = add128(t, part[b]);
+  for (int d = 16; d > 0; d >>= 1) t = add128(t, shfl_down128(t, d));
+  __shared__ U128 warp_tot[32];
+  if ((threadIdx.x & 31) == 0) warp_tot[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    U128 s{0ull, 0ull};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = add128(s, warp_tot[w]);
+    const double e = from_fixed(s);
+    *E_local = e;
+    *Ee += e;
+  }
+}
+
+// ------------------------------------------------------------- FDM solve
+
+// One substep of EPH_FDM::solve (eph_fdm.h:315-396) with the reference's
+// expression order: the variable-kappa 7-point stencil with periodic wrap and
+// ZERO_DERIVATIVE walls, then T += (ddT + dT + S)/(rho_e C_e) dt' on DYNAMIC
+// cells and the clamp at T = 0.  Reads T_in, writes T_out.  The first
+// substep turns the fixed-point deposits into dT and clears them.
+__global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, double dz, double inner_dt,
+                              const double *__restrict__ T, double *__restrict__ Tout,
+                              const double *__restrict__ kappa, const double *__restrict__ rhoC,
+                              const double *__restrict__ S, const signed char *__restrict__ flag,
+                              double *__restrict__ dT, U128 *__restrict__ acc, int first,
+                              unsigned long long *__restrict__ counters) {
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long ntotal = nx * ny * nz;
+  if (r >= ntotal) return;
+  double dTr;
+  if (first) {
+    U128 a = acc[r];
+    dTr = from_fixed(a);
+    dT[r] = dTr;
+    acc[r] = U128{0ull, 0ull};
+  } else {
+    dTr = dT[r];
+  }
+  const long i = r % nx, j = (r / nx) % ny, k = r / (nx * ny);
+  double ddT = 0.0;
+  if (flag[r] != 2) {
+    long p, q;
+    p = (i > 0) ? r - 1 : r + (nx - 1);
+    q = (i < nx - 1) ? r + 1 : r - (nx - 1);
+    if (flag[q] == 2) q = r;
+    else if (flag[p] == 2) p = r;
+    ddT += (kappa[q] - kappa[p]) * (T[q] - T[p]) / dx / dx / 4.0;
+    ddT += kappa[r] * ((T[q] + T[p] - 2.0 * T[r]) / dx / dx);
+    p = (j > 0) ? r - nx : r + (ny - 1) * nx;
+    q = (j < ny - 1) ? r + nx : r - (ny - 1) * nx;
+    if (flag[q] == 2) q = r;
+    else if (flag[p] == 2) p = r;
+    ddT += (kappa[q] - kappa[p]) * (T[q] - T[p]) / dy / dy / 4.0;
+    ddT += kappa[r] * ((T[q] + T[p] - 2.0 * T[r]) / dy / dy);
+    p = (k > 0) ? r - nx * ny : r + (nz - 1) * nx * ny;
+    q = (k < nz - 1) ? r + nx * ny : r - (nz - 1) * nx * ny;
+    if (flag[q] == 2) q = r;
+    else if (flag[p] == 2) p = r;
+    ddT += (kappa[q] - kappa[p]) * (T[q] - T[p]) / dz / dz / 4.0;
+    ddT += kappa[r] * ((T[q] + T[p] - 2.0 * T[r]) / dz / dz);
+  }
+  double t = T[r];
+  if (flag[r] == 1) t += (ddT + dTr + S[r]) / rhoC[r] * inner_dt;
+  if (t < 0.0) {
+    t = 0.0;
+    atomicAdd(&counters[CNT_T_CLAMP], 1ull);
+  }
+  Tout[r] = t;
+}
+
+// Exact sum of the grid temperatures (EPH_FDM::get_T_total, eph_fdm.h:189-196).
+__global__ void k_grid_sum(const double *__restrict__ T, long ncells, U128 *__restrict__ out,
+                           unsigned *__restrict__ err) {
+  U128 t{0ull, 0ull};
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < ncells; r += (long)gridDim.x * blockDim.x)
+    t = add128(t, to_fixed(T[r], err));
+  for (int d = 16; d > 0; d >>= 1) t = add128(t, shfl_down128(t, d));
+  if ((threadIdx.x & 31) == 0 && (t.lo | t.hi)) atomic_add128(out, t);
+}
+
+__global__ void k_from_fixed(const U128 *__restrict__ in, double *__restrict__ out) { *out = from_fixed(*in); }
+
+// ------------------------------------------------------------ layout moves
+
+// engine layout (n x 3) <-> padded device layout; w is kept
+__global__ void k_pack3(int n, const double *__restrict__ src, D4 *__restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  D4 d = dst[i];
+  d.x = src[3 * (size_t)i + 0];
+  d.y = src[3 * (size_t)i + 1];
+  d.z = src[3 * (size_t)i + 2];
+  dst[i] = d;
+}
+
+__global__ void k_unpack3(int n, const D4 *__restrict__ src, double *__restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const D4 s = src[i];
+  dst[3 * (size_t)i + 0] = s.x;
+  dst[3 * (size_t)i + 1] = s.y;
+  dst[3 * (size_t)i + 2] = s.z;
+}
+
+// per-atom array of the fix (fix_eph.cpp:406-428): rho, beta(rho), f_EPH, f_RNG
+__global__ void k_peratom(int n, int groupbit, const int *__restrict__ mask, const double *__restrict__ rho,
+                          const double *__restrict__ beta, const D4 *__restrict__ f_eph,
+                          const D4 *__restrict__ f_rng, double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double *o = out + 8 * (size_t)i;
+  if (mask[i] & groupbit) {
+    const D4 a = f_eph[i], b = f_rng[i];
+    o[0] = rho[i];
+    o[1] = beta[i];
+    o[2] = a.x;
+    o[3] = a.y;
+    o[4] = a.z;
+    o[5] = b.x;
+    o[6] = b.y;
+    o[7] = b.z;
+  } else {
+    for (int k = 0; k < 8; ++k) o[k] = 0.0;
+  }
+}
+
+// rho and w in the engine layout
+__global__ void k_get_w(int n, const D4 *__restrict__ Bw, double *__restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const D4 b = Bw[i];
+  dst[3 * (size_t)i + 0] = b.y;
+  dst[3 * (size_t)i + 1] = b.z;
+  dst[3 * (size_t)i + 2] = b.w;
+}
+
+__global__ void k_set_elem(int n, const int *__restrict__ type, const int *__restrict__ type_map,
+                           D4 *__restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[i].w = (double)type_map[type[i]];
+}
+
+}  // namespace ephgb

@@ -1,0 +1,146 @@
+"""Synthetic inputs for the fix-eph hot path: fcc lattices, Maxwell-Boltzmann
+velocities, the synthetic beta(rho) file and the `fix eph` argument vector.
+
+The reference ships no dataset for this path; its benchmarks are LAMMPS decks
+on fcc Ni (TB_Bench/01_Profile/*/run.lmp).  These generators produce seeded
+inputs with the shapes and value distributions of those decks: fcc Ni with
+a = 3.52 A, Gaussian position jitter, velocities at a set temperature, and a
+beta file in the reference format (Doc/Beta/input.beta, read by
+eph_beta.h:39-128).  Units are LAMMPS metal units throughout.
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# LAMMPS metal units: Boltzmann constant in eV/K, and the conversion of
+# eV/A/amu into A/ps^2 (ftm2v) whose inverse converts amu*A^2/ps^2 into eV.
+BOLTZ = 8.617343e-5
+MVV2E = 1.0364269e-4
+FTM2V = 1.0 / MVV2E
+
+NI_MASS = 58.69
+NI_LATTICE = 3.52
+
+
+@dataclass
+class Atoms:
+    """Atoms of one periodic orthogonal box, arrays in LAMMPS layout."""
+
+    x: np.ndarray  # (n, 3) float64
+    v: np.ndarray  # (n, 3) float64
+    type: np.ndarray  # (n,) int32, LAMMPS types 1..ntypes
+    mask: np.ndarray  # (n,) int32, group bits
+    boxlo: np.ndarray  # (3,)
+    boxhi: np.ndarray  # (3,)
+    mass: np.ndarray = field(default_factory=lambda: np.array([0.0, NI_MASS]))  # index 1..ntypes
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+
+def fcc_lattice(cells: int | tuple, a: float = NI_LATTICE, jitter: float = 0.05, temperature: float = 300.0,
+                mass: float = NI_MASS, seed: int = 12345) -> Atoms:
+    """fcc crystal of cells^3 unit cells (4 atoms each), positions jittered by
+    a Gaussian of standard deviation `jitter` (A), velocities drawn from the
+    Maxwell-Boltzmann distribution at `temperature` with the centre-of-mass
+    velocity removed."""
+    if isinstance(cells, int):
+        cells = (cells, cells, cells)
+    nx, ny, nz = cells
+    rng = np.random.default_rng(seed)
+    basis = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.0], [0.5, 0.0, 0.5], [0.0, 0.5, 0.5]])
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    # atom order: x fastest over unit cells, like a LAMMPS create_atoms box
+    origins = np.stack([ix.ravel(order="F"), iy.ravel(order="F"), iz.ravel(order="F")], axis=1).astype(np.float64)
+    x = ((origins[:, None, :] + basis[None, :, :]) * a).reshape(-1, 3)
+    x = x + rng.normal(0.0, jitter, size=x.shape)
+    boxlo = np.zeros(3)
+    boxhi = np.array([nx * a, ny * a, nz * a], dtype=np.float64)
+    x = boxlo + np.mod(x - boxlo, boxhi - boxlo)
+    sigma = math.sqrt(BOLTZ * temperature / (mass * MVV2E)) if temperature > 0 else 0.0
+    v = rng.normal(0.0, sigma, size=x.shape)
+    v -= v.mean(axis=0)
+    n = x.shape[0]
+    return Atoms(x=np.ascontiguousarray(x), v=np.ascontiguousarray(v), type=np.ones(n, dtype=np.int32),
+                 mask=np.ones(n, dtype=np.int32), boxlo=boxlo, boxhi=boxhi, mass=np.array([0.0, mass]))
+
+
+def add_pka(atoms: Atoms, energy_ev: float, seed: int = 7) -> int:
+    """Give the atom nearest the box centre `energy_ev` of kinetic energy in a
+    seeded random direction; returns its index."""
+    rng = np.random.default_rng(seed)
+    centre = 0.5 * (atoms.boxlo + atoms.boxhi)
+    i = int(np.argmin(((atoms.x - centre) ** 2).sum(axis=1)))
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    m = atoms.mass[atoms.type[i]]
+    speed = math.sqrt(2.0 * energy_ev / (m * MVV2E))
+    atoms.v[i] = speed * d
+    return i
+
+
+def kinetic_temperature(atoms: Atoms) -> float:
+    m = atoms.mass[atoms.type][:, None]
+    ke = 0.5 * MVV2E * float((m * atoms.v ** 2).sum())
+    dof = 3 * atoms.n - 3
+    return 2.0 * ke / (dof * BOLTZ)
+
+
+def synthetic_rho(r: np.ndarray, rc: float = 4.6, length: float = 0.6) -> np.ndarray:
+    """rho(r) = exp(-r/length) * (1 - (r/rc)^2)^2 for r < rc, 0 beyond: smooth
+    (C1) at the cutoff."""
+    r = np.asarray(r, dtype=np.float64)
+    s = np.clip(1.0 - (r / rc) ** 2, 0.0, None)
+    return np.exp(-r / length) * s * s
+
+
+def synthetic_beta(rho: np.ndarray) -> np.ndarray:
+    """beta(rho) = 0.05 + 0.02 tanh(rho - 2) in eV ps / A^2 (>= 0.03)."""
+    return 0.05 + 0.02 * np.tanh(np.asarray(rho, dtype=np.float64) - 2.0)
+
+
+def write_beta_file(path: str, elements=("Ni",), numbers=(28,), n_rho: int = 2000, rc: float = 4.6,
+                    n_beta: int = 2000, drho: float = 0.005, rho_fn=synthetic_rho, beta_fn=synthetic_beta) -> str:
+    """Write a beta file in the reference format (three comment lines,
+    "N name...", "Nrho dr Nbeta drho rcut", then per element Z, the Nrho
+    rho(r) knots and the Nbeta beta(rho) knots), values round-trip exact."""
+    dr = rc / (n_rho - 1)
+    r = np.arange(n_rho) * dr
+    rho_knots = rho_fn(r)
+    beta_knots = beta_fn(np.arange(n_beta) * drho)
+    with open(path, "w") as f:
+        f.write("# synthetic beta(rho) file\n")
+        f.write("# rho(r) = exp(-r/0.6)*(1-(r/rc)^2)^2, beta(rho) = 0.05 + 0.02 tanh(rho - 2)\n")
+        f.write("# r in A, beta in eV ps / A^2\n")
+        f.write(f"{len(elements)} {' '.join(elements)}\n")
+        f.write(f"{n_rho} {dr!r} {n_beta} {drho!r} {rc!r}\n")
+        for k, z in enumerate(numbers):
+            f.write(f"{z}\n")
+            scale = 1.0 + 0.1 * k  # distinct densities per element for multi-element files
+            f.write("\n".join(repr(float(val)) for val in rho_knots * scale))
+            f.write("\n")
+            f.write("\n".join(repr(float(val)) for val in beta_knots * (1.0 + 0.05 * k)))
+            f.write("\n")
+    return path
+
+
+def fix_args(beta_file: str, seed: int = 4242, flags: int | str = 7, model: int = 4, rho_e: float = 1.0,
+             C_e: float = 3.5e-6, kappa_e: float = 0.1, T_e: float = 300.0, grid=(10, 10, 10),
+             T_infile: str = "NULL", T_freq: int = 0, T_out: str = "Te_out", elements=("Ni",),
+             fix_id: str = "eph", group: str = "all") -> list[str]:
+    """The words of `fix ID group eph seed flags model rho_e C_e kappa_e T_e
+    NX NY NZ T_infile freq Te_out beta_file A B ...` (README.md:186-214)."""
+    return [fix_id, group, "eph", str(seed), str(flags), str(model), repr(rho_e), repr(C_e), repr(kappa_e),
+            repr(T_e), str(grid[0]), str(grid[1]), str(grid[2]), T_infile, str(T_freq), T_out, beta_file,
+            *elements]
+
+
+def gaussian_stream(n_in_group: int, seed: int, step: int) -> np.ndarray:
+    """Deviates a RanMars-like source would hand the fix in one step: three
+    per in-group atom, atom order.  Seeded per (seed, step)."""
+    return np.random.default_rng([seed, step]).standard_normal(3 * n_in_group)
