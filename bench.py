@@ -53,9 +53,11 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def make_system(workdir, cells=CELLS, grid=GRID):
+def make_system(workdir, cells=None, grid=None):
     from ephgb import workloads as W
 
+    cells = CELLS if cells is None else cells
+    grid = GRID if grid is None else grid
     bf = W.write_beta_file(os.path.join(workdir, "synth.beta"))
     atoms = W.fcc_lattice(cells, seed=SEED)
     W.add_pka(atoms, PKA_EV, seed=SEED + 1)
@@ -169,6 +171,8 @@ def run_gpu(args, rank, world):
         n_pairs = fix.pair_count()
         out.update(ms=ms, phases=phases, launches=launches, n_pairs=n_pairs, clocks=clock, n=n,
                    rebuilds=fix.counter("wrap"))
+        if args.no_e2e:
+            return out
         # ------------------------------------------------ end to end (host)
         x = torch.empty((n, 3), dtype=torch.float64).pin_memory()
         v = torch.empty((n, 3), dtype=torch.float64).pin_memory()
@@ -233,13 +237,21 @@ def cpu_baseline(threads, steps=1, warm=1):
 
 
 def main():
+    global CELLS, GRID, WORKLOAD
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="omit the cpu_baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="omit the end-to-end leg")
+    ap.add_argument("--cells", type=int, default=CELLS, help="fcc cells per edge (profiling cases)")
+    ap.add_argument("--grid", type=int, default=GRID[0], help="FDM cells per edge (profiling cases)")
     args = ap.parse_args()
+    if args.cells != CELLS or args.grid != GRID[0]:
+        CELLS, GRID = args.cells, (args.grid,) * 3
+        WORKLOAD = (f"fcc Ni {CELLS}^3 cells ({4 * CELLS ** 3:,} atoms), 10 keV PKA, dt 0.5 fs, FDM {GRID[0]}^3, "
+                    "flags 7, model 4")
     args.warmup = max(args.warmup, 3)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -269,7 +281,6 @@ def main():
     res = run_gpu(args, rank, world)
     n = res["n"]
     value = world * n * args.steps / (res["ms"] / 1000.0)
-    e2e = world * n * res["e2e_steps"] / res["t_e2e"]
     ms_f, nl_f = res["phases"]["forces"]
     hbm, peak_src = peaks()
     t_launch = ms_f / max(nl_f, 1) / 1000.0
@@ -282,8 +293,6 @@ def main():
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 52 // 2 ** 20),
                    "mode": "fast", "xi": "device Philox4x32-10"},
-        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
-                "steps": res["e2e_steps"]},
         "gpu_launches": res["launches"],
         "roofline": {"bound": "hbm", "kernel": "k_forces", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
@@ -293,6 +302,9 @@ def main():
         "pairs_per_atom": res["n_pairs"] / n,
         "wraps": res["rebuilds"],
     }
+    if "t_e2e" in res:
+        line["e2e"] = {"value": world * n * res["e2e_steps"] / res["t_e2e"], "unit": METRIC,
+                       "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"]}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(threads, steps=1, warm=1).items() if k != "seconds"}
     if rank == 0:
