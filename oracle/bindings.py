@@ -345,3 +345,63 @@ class RefGrid:
     def __getattr__(self, name):
         fn = getattr(self.lib, "refg_" + name)
         return lambda *a: fn(self.h, *[x.encode() if isinstance(x, str) else x for x in a])
+
+
+GB_SO = os.path.join(HERE, "libgbfix.so")
+
+
+def gb_available():
+    return os.path.exists(GB_SO)
+
+
+class GbFix:
+    """The GB300 fix eph/gb (user-eph_gb300/lammps/fix_eph_gb.cpp) inside the
+    engine stand-in, driven exactly like RefFix drives the reference fix."""
+
+    _lib = None
+
+    def __init__(self, words, atoms, dt, rc, mode=0, xi_host=1, skin=1.0, boltz=8.617343e-5,
+                 ftm2v=1.0 / 1.0364269e-4):
+        if GbFix._lib is None:
+            lib = C.CDLL(GB_SO)
+            lib.gbh_create.restype = C.c_void_p
+            lib.gbh_create.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_int, _dp, _dp, _ip, _ip, C.c_int, _dp,
+                                       _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_int, C.c_int, C.c_char_p, C.c_int]
+            lib.gbh_destroy.argtypes = [C.c_void_p]
+            lib.gbh_step.argtypes = [C.c_void_p, _dp, C.c_long, C.c_char_p, C.c_int]
+            lib.gbh_get.argtypes = [C.c_void_p, C.c_char_p, _dp]
+            lib.gbh_post_run.argtypes = [C.c_void_p]
+            GbFix._lib = lib
+        lib = GbFix._lib
+        self.lib = lib
+        err = C.create_string_buffer(512)
+        mass = np.ascontiguousarray(atoms.mass, dtype=np.float64)
+        x = np.ascontiguousarray(atoms.x, dtype=np.float64)
+        v = np.ascontiguousarray(atoms.v, dtype=np.float64)
+        t = np.ascontiguousarray(atoms.type, dtype=np.int32)
+        m = np.ascontiguousarray(atoms.mask, dtype=np.int32)
+        self.h = lib.gbh_create(len(words), _argv(words), atoms.n, _d(x), _d(v), _i(t), _i(m), len(mass) - 1,
+                                _d(mass), _d(atoms.boxlo), _d(atoms.boxhi), dt, boltz, ftm2v, skin, rc, mode,
+                                xi_host, err, 512)
+        if not self.h:
+            raise RuntimeError(err.value.decode())
+        self.n = atoms.n
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.gbh_destroy(self.h)
+            self.h = None
+
+    def step(self, xi=None):
+        a = None if xi is None else np.ascontiguousarray(xi, dtype=np.float64)
+        err = C.create_string_buffer(512)
+        if self.lib.gbh_step(self.h, _d(a), 0 if a is None else a.size, err, 512):
+            raise RuntimeError(err.value.decode())
+
+    def get(self, what):
+        k = {"x": 3, "v": 3, "f": 3, "array": 8}.get(what)
+        out = np.zeros(2) if what == "vector" else np.zeros((self.n, k))
+        if self.lib.gbh_get(self.h, what.encode(), _d(out)):
+            raise KeyError(what)
+        return out

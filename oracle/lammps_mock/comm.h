@@ -9,6 +9,7 @@ class Fix;
 class Comm {
  public:
   int ghost_velocity = 0;
+  int me = 0, nprocs = 1;
   int *ghost_owner = nullptr;
   int nghost = 0, nlocal = 0;
   double *buf = nullptr;

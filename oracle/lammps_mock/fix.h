@@ -30,6 +30,8 @@ class Fix : protected Pointers {
   double **array_atom = nullptr;
 
   virtual void init() {}
+  virtual void setup(int) {}
+  virtual int modify_param(int, char **) { return 0; }
   virtual void init_list(int, NeighList *) {}
   virtual int setmask() = 0;
   virtual void post_force(int) {}

@@ -9,6 +9,8 @@ class Neighbor {
   NeighRequest request;
   Fix *requestor = nullptr;
   int nrequest = 0;
+  double skin = 1.0;  // neighbor skin distance
+  bigint ago = 0;     // steps since the last re-neighbouring
   NeighRequest *add_request(Fix *f, int style) {
     requestor = f;
     request.style = style;

@@ -36,6 +36,7 @@
 #include "neighbor.h"
 #include "random_mars.h"
 #include "update.h"
+#include "engine.hpp"
 
 #include "fix_eph.h"
 
@@ -59,225 +60,8 @@ class FixEPHProbe : public FixEPH {
   void save_state(const char *path) const { fdm.save_state(path); }
 };
 
-struct Sim {
-  LAMMPS lmp;
-  Atom atom;
-  Domain domain;
-  Neighbor neighbor;
-  Memory memory;
-  Force force;
-  Update update;
-  Comm comm;
-  Error error;
-  NeighList list;
-  FixEPHProbe *fix = nullptr;
-
-  double skin = 1.0, cutneigh = 0.0;
-  std::vector<int> ghost_owner;
-  std::vector<int> ghost_shift;  // 3 per ghost, values -1, 0, +1
-  std::vector<double> xhold;
-  std::vector<double> fext;
-  std::vector<int> numneigh;
-  std::vector<int *> firstneigh;
-  std::vector<std::vector<int>> neigh;
-  std::vector<double> commbuf;
-  long nbuild = 0;
-
-  Sim() {
-    lmp.atom = &atom;
-    lmp.domain = &domain;
-    lmp.neighbor = &neighbor;
-    lmp.memory = &memory;
-    lmp.force = &force;
-    lmp.update = &update;
-    lmp.comm = &comm;
-    lmp.error = &error;
-  }
-  ~Sim() {
-    delete fix;
-    memory.destroy(atom.x);
-    memory.destroy(atom.v);
-    memory.destroy(atom.f);
-    memory.destroy(atom.type);
-    memory.destroy(atom.mask);
-    memory.destroy(atom.mass);
-  }
-
-  void grow_atoms(int n) {
-    if (n <= atom.nmax) return;
-    atom.nmax = n;
-    memory.grow(atom.x, n, 3, "x");
-    memory.grow(atom.v, n, 3, "v");
-    memory.grow(atom.f, n, 3, "f");
-    memory.grow(atom.type, n, "type");
-    memory.grow(atom.mask, n, "mask");
-    commbuf.resize((size_t)3 * n);
-    comm.buf = commbuf.data();
-    if (fix) fix->grow_arrays(n);
-  }
-
-  // Domain::pbc for an orthogonal periodic box.
-  void pbc() {
-    for (int i = 0; i < atom.nlocal; ++i)
-      for (int k = 0; k < 3; ++k) {
-        double &c = atom.x[i][k];
-        if (c < domain.boxlo[k]) c += domain.prd[k];
-        if (c >= domain.boxhi[k]) {
-          c -= domain.prd[k];
-          c = std::max(c, domain.boxlo[k]);
-        }
-      }
-  }
-
-  // Ghosts: every periodic image of a local atom that falls inside the box
-  // grown by the neighbour cutoff on each side.
-  void borders() {
-    const int nlocal = atom.nlocal;
-    ghost_owner.clear();
-    ghost_shift.clear();
-    std::vector<double> gx;
-    for (int i = 0; i < nlocal; ++i)
-      for (int sz = -1; sz <= 1; ++sz)
-        for (int sy = -1; sy <= 1; ++sy)
-          for (int sx = -1; sx <= 1; ++sx) {
-            if (!sx && !sy && !sz) continue;
-            const int s[3] = {sx, sy, sz};
-            double c[3];
-            bool inside = true;
-            for (int k = 0; k < 3; ++k) {
-              c[k] = atom.x[i][k];
-              if (s[k] > 0) c[k] = atom.x[i][k] + domain.prd[k];
-              if (s[k] < 0) c[k] = atom.x[i][k] + (-domain.prd[k]);
-              if (!(c[k] >= domain.boxlo[k] - cutneigh && c[k] < domain.boxhi[k] + cutneigh)) inside = false;
-            }
-            if (!inside) continue;
-            ghost_owner.push_back(i);
-            ghost_shift.insert(ghost_shift.end(), s, s + 3);
-            gx.insert(gx.end(), c, c + 3);
-          }
-    const int ng = (int)ghost_owner.size();
-    grow_atoms(nlocal + ng + 1);
-    atom.nghost = ng;
-    for (int g = 0; g < ng; ++g) {
-      const int j = nlocal + g, o = ghost_owner[g];
-      for (int k = 0; k < 3; ++k) {
-        atom.x[j][k] = gx[3 * g + k];
-        atom.v[j][k] = atom.v[o][k];
-      }
-      atom.type[j] = atom.type[o];
-      atom.mask[j] = atom.mask[o];
-    }
-    comm.ghost_owner = ghost_owner.data();
-    comm.nghost = ng;
-    comm.nlocal = nlocal;
-  }
-
-  // Owner x, v to ghosts (forward communication with ghost_velocity = 1).
-  void forward_xv() {
-    const int nlocal = atom.nlocal;
-    for (int g = 0; g < atom.nghost; ++g) {
-      const int j = nlocal + g, o = ghost_owner[g];
-      for (int k = 0; k < 3; ++k) {
-        const int s = ghost_shift[3 * g + k];
-        double c = atom.x[o][k];
-        if (s > 0) c = atom.x[o][k] + domain.prd[k];
-        if (s < 0) c = atom.x[o][k] + (-domain.prd[k]);
-        atom.x[j][k] = c;
-        atom.v[j][k] = atom.v[o][k];
-      }
-    }
-  }
-
-  int owner(int j) const { return j < atom.nlocal ? j : ghost_owner[j - atom.nlocal]; }
-
-  // Full list of every local atom, neighbours ordered by owner index.
-  void build_list() {
-    const int nlocal = atom.nlocal, ntot = nlocal + atom.nghost;
-    const double cutsq = cutneigh * cutneigh;
-    // bin all atoms (local + ghost) on a grid of cells of edge >= cutneigh
-    double lo[3], w[3];
-    int nb[3];
-    for (int k = 0; k < 3; ++k) {
-      lo[k] = domain.boxlo[k] - cutneigh;
-      const double ext = domain.prd[k] + 2.0 * cutneigh;
-      nb[k] = std::max(1, (int)(ext / cutneigh));
-      w[k] = ext / nb[k];
-    }
-    auto bin_of = [&](const double *c, int *b) {
-      for (int k = 0; k < 3; ++k) {
-        int v = (int)std::floor((c[k] - lo[k]) / w[k]);
-        b[k] = std::min(std::max(v, 0), nb[k] - 1);
-      }
-    };
-    std::vector<std::vector<int>> bins((size_t)nb[0] * nb[1] * nb[2]);
-    for (int j = 0; j < ntot; ++j) {
-      int b[3];
-      bin_of(atom.x[j], b);
-      bins[(size_t)b[0] + (size_t)nb[0] * (b[1] + (size_t)nb[1] * b[2])].push_back(j);
-    }
-    neigh.assign(nlocal, {});
-    numneigh.assign(nlocal, 0);
-    firstneigh.assign(nlocal, nullptr);
-    for (int i = 0; i < nlocal; ++i) {
-      int b[3];
-      bin_of(atom.x[i], b);
-      std::vector<std::pair<int, int>> cand;
-      for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy)
-          for (int dx = -1; dx <= 1; ++dx) {
-            const int c0 = b[0] + dx, c1 = b[1] + dy, c2 = b[2] + dz;
-            if (c0 < 0 || c1 < 0 || c2 < 0 || c0 >= nb[0] || c1 >= nb[1] || c2 >= nb[2]) continue;
-            for (int j : bins[(size_t)c0 + (size_t)nb[0] * (c1 + (size_t)nb[1] * c2)]) {
-              if (j == i) continue;
-              const double ex = atom.x[j][0] - atom.x[i][0];
-              const double ey = atom.x[j][1] - atom.x[i][1];
-              const double ez = atom.x[j][2] - atom.x[i][2];
-              const double rsq = ex * ex + ey * ey + ez * ez;
-              if (rsq < cutsq) cand.emplace_back(owner(j), j);
-            }
-          }
-      std::sort(cand.begin(), cand.end());
-      for (size_t c = 1; c < cand.size(); ++c)
-        if (cand[c].first == cand[c - 1].first)
-          throw std::runtime_error("two images of one atom in a list: box narrower than 2*(rc+skin)");
-      for (auto &p : cand) neigh[i].push_back(p.second);
-      numneigh[i] = (int)neigh[i].size();
-      firstneigh[i] = neigh[i].data();
-    }
-    list.inum = nlocal;
-    list.numneigh = numneigh.data();
-    list.firstneigh = firstneigh.data();
-    xhold.assign((size_t)3 * nlocal, 0.0);
-    for (int i = 0; i < nlocal; ++i)
-      for (int k = 0; k < 3; ++k) xhold[3 * (size_t)i + k] = atom.x[i][k];
-    ++nbuild;
-  }
-
-  bool decide() const {
-    const double triggersq = 0.25 * skin * skin;
-    for (int i = 0; i < atom.nlocal; ++i) {
-      const double dx = atom.x[i][0] - xhold[3 * (size_t)i + 0];
-      const double dy = atom.x[i][1] - xhold[3 * (size_t)i + 1];
-      const double dz = atom.x[i][2] - xhold[3 * (size_t)i + 2];
-      if (dx * dx + dy * dy + dz * dz > triggersq) return true;
-    }
-    return false;
-  }
-
-  void reneighbor() {
-    pbc();
-    borders();
-    build_list();
-  }
-
-  void clear_forces() {
-    const int ntot = atom.nlocal + atom.nghost;
-    for (int i = 0; i < ntot; ++i)
-      for (int k = 0; k < 3; ++k) atom.f[i][k] = 0.0;
-    if (!fext.empty())
-      for (int i = 0; i < atom.nlocal; ++i)
-        for (int k = 0; k < 3; ++k) atom.f[i][k] = fext[3 * (size_t)i + k];
-  }
+struct Sim : Engine {
+  FixEPHProbe *probe() { return static_cast<FixEPHProbe *>(fix); }
 };
 
 void copy_err(const char *msg, char *errbuf, int errlen) {
@@ -300,38 +84,18 @@ void *ref_create(int narg, const char **arg, int nlocal, const double *x, const 
                  double boltz, double ftm2v, double skin, char *errbuf, int errlen) {
   Sim *s = new Sim();
   try {
-    s->domain.set_box(lo, hi);
-    s->update.dt = dt;
-    s->force.boltz = boltz;
-    s->force.ftm2v = ftm2v;
-    s->skin = skin;
-    s->atom.ntypes = ntypes;
-    s->atom.natoms = nlocal;
-    s->atom.nlocal = nlocal;
-    s->memory.grow(s->atom.mass, ntypes + 1, "mass");
-    for (int t = 0; t <= ntypes; ++t) s->atom.mass[t] = mass[t];
-    s->grow_atoms(std::max(nlocal, 1));
-    for (int i = 0; i < nlocal; ++i) {
-      for (int k = 0; k < 3; ++k) {
-        s->atom.x[i][k] = x[3 * (size_t)i + k];
-        s->atom.v[i][k] = v[3 * (size_t)i + k];
-        s->atom.f[i][k] = 0.0;
-      }
-      s->atom.type[i] = type[i];
-      s->atom.mask[i] = mask ? mask[i] : 1;
-    }
+    s->load(nlocal, x, v, type, mask, ntypes, mass, lo, hi, dt, boltz, ftm2v, skin);
     std::vector<std::string> words(arg, arg + narg);
     std::vector<char *> argv;
     for (auto &w : words) argv.push_back(&w[0]);
-    s->fix = new FixEPHProbe(&s->lmp, narg, argv.data());
-    s->fix->init();
+    FixEPHProbe *f = new FixEPHProbe(&s->lmp, narg, argv.data());
+    s->fix = f;
+    s->rng = f->rng();
+    f->init();
     if (s->neighbor.nrequest != 1) throw std::runtime_error("fix did not request a neighbour list");
     s->cutneigh = s->neighbor.request.cutoff + skin;
-    s->fix->init_list(0, &s->list);
-    // Verlet::setup
-    s->reneighbor();
-    s->fix->grow_arrays(s->atom.nmax);
-    s->clear_forces();
+    f->init_list(0, &s->list);
+    s->setup();
   } catch (std::exception &e) {
     copy_err(e.what(), errbuf, errlen);
     delete s;
@@ -358,21 +122,7 @@ int ref_set_fext(void *h, const double *fext) {
 int ref_step(void *h, const double *xi, long nxi, char *errbuf, int errlen) {
   Sim *s = static_cast<Sim *>(h);
   try {
-    s->update.ntimestep += 1;
-    s->fix->initial_integrate(0);
-    if (s->decide())
-      s->reneighbor();
-    else
-      s->forward_xv();
-    s->clear_forces();
-    RanMars *r = s->fix->rng();
-    r->stream = xi;
-    r->count = xi ? nxi : 0;
-    r->pos = 0;
-    s->fix->post_force(0);
-    if (xi && r->pos != nxi) throw std::runtime_error("fix drew a different number of deviates than injected");
-    s->fix->final_integrate();
-    s->fix->end_of_step();
+    s->step(xi, nxi);
   } catch (std::exception &e) {
     copy_err(e.what(), errbuf, errlen);
     return 1;
@@ -394,15 +144,15 @@ int ref_get(void *h, const char *what, double *out) {
   if (w == "x") rows3(s->atom.x);
   else if (w == "v") rows3(s->atom.v);
   else if (w == "f") rows3(s->atom.f);
-  else if (w == "f_eph") rows3(s->fix->feph());
-  else if (w == "f_rng") rows3(s->fix->frng());
-  else if (w == "w") rows3(s->fix->w());
-  else if (w == "xi") rows3(s->fix->xi());
+  else if (w == "f_eph") rows3(s->probe()->feph());
+  else if (w == "f_rng") rows3(s->probe()->frng());
+  else if (w == "w") rows3(s->probe()->w());
+  else if (w == "xi") rows3(s->probe()->xi());
   else if (w == "rho") {
-    for (int i = 0; i < n; ++i) out[i] = s->fix->rho()[i];
+    for (int i = 0; i < n; ++i) out[i] = s->probe()->rho()[i];
   } else if (w == "array") {
     for (int i = 0; i < n; ++i)
-      for (int k = 0; k < 8; ++k) out[8 * (size_t)i + k] = s->fix->arr()[i][k];
+      for (int k = 0; k < 8; ++k) out[8 * (size_t)i + k] = s->probe()->arr()[i][k];
   } else if (w == "vector") {
     out[0] = s->fix->compute_vector(0);
     out[1] = s->fix->compute_vector(1);
@@ -420,7 +170,7 @@ int ref_get_T(void *h, int nx, int ny, int nz, const double *lo, const double *h
     for (int j = 0; j < ny; ++j)
       for (int i = 0; i < nx; ++i)
         out[i + (size_t)nx * (j + (size_t)ny * k)] =
-            s->fix->T_at(lo[0] + (i + 0.5) * dx, lo[1] + (j + 0.5) * dy, lo[2] + (k + 0.5) * dz);
+            s->probe()->T_at(lo[0] + (i + 0.5) * dx, lo[1] + (j + 0.5) * dy, lo[2] + (k + 0.5) * dz);
   return 0;
 }
 
@@ -442,12 +192,12 @@ int ref_get_neigh(void *h, int *numneigh, int *owners, int maxn) {
 long ref_nbuild(void *h) { return static_cast<Sim *>(h)->nbuild; }
 
 int ref_save_temperature(void *h, const char *path, int n) {
-  static_cast<Sim *>(h)->fix->save_T(path, n);
+  static_cast<Sim *>(h)->probe()->save_T(path, n);
   return 0;
 }
 
 int ref_save_state(void *h, const char *path) {
-  static_cast<Sim *>(h)->fix->save_state(path);
+  static_cast<Sim *>(h)->probe()->save_state(path);
   return 0;
 }
 

@@ -275,7 +275,13 @@ int launch_final(eph_ctx *c) {
 
 template <bool FAST, bool MULTI>
 void launch_density_t(eph_ctx *c, int xi_mode) {
-  k_density<FAST, MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+  const size_t smem = sizeof(unsigned) * (size_t)c->kcap * BLOCK;
+  static size_t configured = 0;  // per instantiation: the largest dynamic shared memory allowed so far
+  if (smem > configured) {
+    cudaFuncSetAttribute(k_density<FAST, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  k_density<FAST, MULTI><<<nblocks(c->n), BLOCK, smem, c->stream>>>(
       c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p,
       c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,
       c->wrapflag.p, c->d_err.p, c->counters.p);
@@ -307,6 +313,8 @@ int launch_post_force(eph_ctx *c, int xi_mode) {
     CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
     k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
                                        c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p);
+    ps.launched();
+    k_bin_sort<<<nblocks(c->nbins), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p, c->bins.p);
   }
   const bool fast = c->mode == EPH_MODE_FAST;
   {
@@ -551,6 +559,7 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
     P.wf[k] = (float)P.w[k];
   }
   c->nbins = P.nb[0] * P.nb[1] * P.nb[2];
+  CUDA_TRY(c, cudaDeviceSynchronize());  // the set-up copies and memsets above ran on the default stream
   return EPH_OK;
 }
 
@@ -589,39 +598,42 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
     if (htype[i] < 1 || htype[i] > c->ntypes) return fail(c, EPH_ERR_ARG, "atom type outside 1..ntypes");
   CUDA_TRY(c, cudaSetDevice(c->device));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-  c->n = n;
-  c->P.n = n;
   const size_t N = (size_t)n;
-  for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw})
-    CUDA_TRY(c, b->alloc(N));
-  CUDA_TRY(c, c->type.alloc(N));
-  CUDA_TRY(c, c->mask.alloc(N));
-  CUDA_TRY(c, c->nshort.alloc(N));
-  CUDA_TRY(c, c->cell.alloc(N));
-  CUDA_TRY(c, c->rho.alloc(N));
-  CUDA_TRY(c, c->beta_i.alloc(N));
-  CUDA_TRY(c, c->Te_i.alloc(N));
-  CUDA_TRY(c, c->stage.alloc(8 * N));
-  CUDA_TRY(c, c->atom_bin.alloc(N));
-  CUDA_TRY(c, c->atom_off.alloc(N));
-  CUDA_TRY(c, c->tmap.alloc(65));
-  CUDA_TRY(c, c->part.alloc((size_t)nblocks(n, 256)));
-  CUDA_TRY(c, c->bin_count.alloc((size_t)c->nbins));
-  // capacities from the number density: a bin holds ~density*w^3 atoms, the
-  // cutoff sphere ~density*4/3 pi rc^3
-  const double vol = c->prd[0] * c->prd[1] * c->prd[2];
-  const double dens = n / vol;
-  const double per_bin = dens * c->P.w[0] * c->P.w[1] * c->P.w[2];
-  const double rc = c->beta.r_cutoff;
-  const double per_sphere = dens * 4.18879020478639 * rc * rc * rc;
-  if (c->bcap <= 0) c->bcap = ((int)std::ceil(2.0 * per_bin + 16.0) + 7) / 8 * 8;
-  if (c->kcap <= 0) c->kcap = std::min(KMAX, ((int)std::ceil(2.0 * per_sphere + 24.0) + 7) / 8 * 8);
-  c->P.bcap = c->bcap;
-  c->P.kcap = c->kcap;
-  CUDA_TRY(c, c->bins.alloc((size_t)c->nbins * c->bcap));
-  CUDA_TRY(c, c->pj.alloc((size_t)c->kcap * N));
-  CUDA_TRY(c, c->pe.alloc((size_t)c->kcap * N));
-  CUDA_TRY(c, c->pg.alloc((size_t)c->kcap * N));
+  if (n != c->n) {  // (re)allocate the per-atom storage
+    c->n = n;
+    c->P.n = n;
+    for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw})
+      CUDA_TRY(c, b->alloc(N));
+    CUDA_TRY(c, c->type.alloc(N));
+    CUDA_TRY(c, c->mask.alloc(N));
+    CUDA_TRY(c, c->nshort.alloc(N));
+    CUDA_TRY(c, c->cell.alloc(N));
+    CUDA_TRY(c, c->rho.alloc(N));
+    CUDA_TRY(c, c->beta_i.alloc(N));
+    CUDA_TRY(c, c->Te_i.alloc(N));
+    CUDA_TRY(c, c->stage.alloc(8 * N));
+    CUDA_TRY(c, c->atom_bin.alloc(N));
+    CUDA_TRY(c, c->atom_off.alloc(N));
+    CUDA_TRY(c, c->part.alloc((size_t)nblocks(n, 256)));
+    if (c->fext.p) CUDA_TRY(c, c->fext.alloc(N));
+    // capacities from the number density: a bin holds ~density*w^3 atoms, the
+    // cutoff sphere ~density*4/3 pi rc^3
+    const double vol = c->prd[0] * c->prd[1] * c->prd[2];
+    const double dens = n / vol;
+    const double per_bin = dens * c->P.w[0] * c->P.w[1] * c->P.w[2];
+    const double rc = c->beta.r_cutoff;
+    const double per_sphere = dens * 4.18879020478639 * rc * rc * rc;
+    if (c->bcap <= 0) c->bcap = ((int)std::ceil(2.0 * per_bin + 16.0) + 7) / 8 * 8;
+    if (c->kcap <= 0) c->kcap = std::min(KMAX, ((int)std::ceil(2.0 * per_sphere + 24.0) + 7) / 8 * 8);
+    c->P.bcap = c->bcap;
+    c->P.kcap = c->kcap;
+    CUDA_TRY(c, c->bins.alloc((size_t)c->nbins * c->bcap));
+    CUDA_TRY(c, c->pj.alloc((size_t)c->kcap * N));
+    CUDA_TRY(c, c->pe.alloc((size_t)c->kcap * N));
+    CUDA_TRY(c, c->pg.alloc((size_t)c->kcap * N));
+  }
+  if (!c->tmap.p) CUDA_TRY(c, c->tmap.alloc(65));
+  if (!c->bin_count.p) CUDA_TRY(c, c->bin_count.alloc((size_t)c->nbins));
   // atoms
   std::vector<int> m(N, 1);
   if (hmask) std::memcpy(m.data(), hmask, sizeof(int) * N);
@@ -629,7 +641,7 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
   CUDA_TRY(c, cudaMemcpy(c->mask.p, m.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->tmap.p, c->P.type_map, sizeof(int) * 65, cudaMemcpyHostToDevice));
   for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw})
-    CUDA_TRY(c, cudaMemset(b->p, 0, sizeof(D4) * N));
+    CUDA_TRY(c, cudaMemsetAsync(b->p, 0, sizeof(D4) * N, c->stream));
   int r = eph_put(c, EPH_FIELD_X, hx, EPH_HOST);
   if (r) return r;
   r = eph_put(c, EPH_FIELD_V, hv, EPH_HOST);

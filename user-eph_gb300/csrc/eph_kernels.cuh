@@ -32,7 +32,7 @@ struct __align__(16) U128 {
   unsigned long long lo, hi;  // two's-complement 128-bit fixed point, 2^-64 units
 };
 
-constexpr int KMAX = 128;  // local candidate array of one atom
+constexpr int KMAX = 128;  // largest pair capacity (shared-memory candidate rows of one atom)
 constexpr unsigned IDX_BITS = 27;
 constexpr unsigned IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr unsigned CODE_NOSHIFT = 13;  // (0,0,0) image of the 3x3x3 code
@@ -354,19 +354,44 @@ __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, 
 
 // -------------------------------------------------------- density sweep
 
+// Sort every bin's entries by atom index (one thread per bin, a handful of
+// entries each), so the candidate order below is fixed run to run.
+__global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  int cnt = bin_count[b];
+  cnt = cnt < bcap ? cnt : bcap;
+  BinEntry *e = bins + (size_t)b * bcap;
+  for (int k = 1; k < cnt; ++k) {
+    const BinEntry v = e[k];
+    const unsigned key = v.idx & IDX_MASK;
+    int p = k;
+    while (p > 0 && (e[p - 1].idx & IDX_MASK) > key) {
+      e[p] = e[p - 1];
+      --p;
+    }
+    e[p] = v;
+  }
+}
+
 // calculate_environment (fix_eph.cpp:431-466) plus everything per atom the
-// later sweeps need.  Per atom: (1) candidates from the 27 bins with an FP32
-// distance test padded by 1e-4 of rc^2, kept in ascending neighbour index
-// (the order of the reference's list, so sums round identically); (2) the
-// exact FP64 test r^2 < rc^2 with e = (x_j + image) - x_i, the density sum,
-// and the pair cache of the in-cutoff pairs for the force sweeps.
-//
+// later sweeps need.  One thread per atom, warps kept converged: a warp FP64
+// instruction costs the same whether 1 or 32 lanes are active, so the FP64
+// work must run in lockstep.
+//   pass 1 (FP32/integer): candidates from the 27 bins around the atom with an
+//     FP32 distance test padded by 1e-4 of rc^2, kept in shared memory; EXACT
+//     mode keeps them in ascending neighbour index (the order of the
+//     reference's list, so sums round identically), FAST mode in the fixed
+//     bin-stencil order of index-sorted bins
+//   pass 2 (FP64): the exact test r^2 < rc^2 with e = (x_j + image) - x_i, the
+//     density sum, and the pair cache of the in-cutoff pairs
 // Pair cache row k of atom i sits at k*n + i (coalesced across the warp):
 //   pj: neighbour index | image code << 27
 //   pe: e_ij and (EXACT) r^2 or (FAST) rho_j(r^2)/r^2
-//   pg: (EXACT) rho_j(r^2), rho_i(r^2); (FAST) rho_i(r^2)/r^2 in .x
+//   pg: (EXACT) rho_j(r^2), rho_i(r^2); (FAST, several elements) rho_i(r^2)/r^2
 // A[i] = {rho_i, alpha_i (EXACT) | alpha_i/rho_i (FAST), xi_x, xi_y}
 // Bw[i] = {xi_z, w_i} (w written by the friction sweep)
+// Dynamic shared memory: kcap x blockDim unsigned (candidate rows).
 template <bool FAST, bool MULTI>
 __global__ void __launch_bounds__(128) k_density(
     StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
@@ -376,69 +401,81 @@ __global__ void __launch_bounds__(128) k_density(
     D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell,
     double *__restrict__ Te_i, int *__restrict__ wrapflag, unsigned *__restrict__ err,
     unsigned long long *__restrict__ counters) {
+  extern __shared__ unsigned s_cand[];  // [kcap][blockDim.x]
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
   if (i == 0) *wrapflag = 0;  // the binning kernel has read it
-  if (i >= P.n) return;
-  const bool in_group = (mask[i] & P.groupbit) != 0;
-  const D4 xi = x[i];
+  const bool valid = i < P.n;
+  const bool active = valid && (mask[i] & P.groupbit) != 0;
+  D4 xi = D4{0.0, 0.0, 0.0, 0.0};
+  if (valid) xi = x[i];
   const int ei = (int)xi.w;
   double rho = 0.0;
-  int ns = 0;
-  if (in_group) {
-    unsigned cand[KMAX];
-    int nc = 0;
-    const int4 Bi = atom_bin[i];
-    const float4 oi = atom_off[i];
-    const int Bv[3] = {Bi.x, Bi.y, Bi.z};
-    // pass 1: candidates, FP32/integer work only
-    for (int dz = -1; dz <= 1; ++dz) {
-      int Tz = Bv[2] + dz, tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
-      const int kz = Tz < 0 ? -1 : (Tz >= P.nb[2] ? 1 : 0);
-      const float bz = (float)dz * P.wf[2] - oi.z;
-      for (int dy = -1; dy <= 1; ++dy) {
-        int Ty = Bv[1] + dy, ty = Ty < 0 ? Ty + P.nb[1] : (Ty >= P.nb[1] ? Ty - P.nb[1] : Ty);
-        const int ky = Ty < 0 ? -1 : (Ty >= P.nb[1] ? 1 : 0);
-        const float by = (float)dy * P.wf[1] - oi.y;
-        for (int dx = -1; dx <= 1; ++dx) {
-          int Tx = Bv[0] + dx, tx = Tx < 0 ? Tx + P.nb[0] : (Tx >= P.nb[0] ? Tx - P.nb[0] : Tx);
-          const int kx = Tx < 0 ? -1 : (Tx >= P.nb[0] ? 1 : 0);
-          const float bx = (float)dx * P.wf[0] - oi.x;
-          const int flat = tx + P.nb[0] * (ty + P.nb[1] * tz);
-          int cnt = bin_count[flat];
+  int ns = 0, nc = 0;
+  int4 Bi = make_int4(0, 0, 0, 0);
+  float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (active) {
+    Bi = atom_bin[i];
+    oi = atom_off[i];
+  }
+  // pass 1: candidates, FP32/integer work only, warp-uniform loop bounds
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int Tz = Bi.z + dz, tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
+    const int kz = Tz < 0 ? -1 : (Tz >= P.nb[2] ? 1 : 0);
+    const float bz = (float)dz * P.wf[2] - oi.z;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int Ty = Bi.y + dy, ty = Ty < 0 ? Ty + P.nb[1] : (Ty >= P.nb[1] ? Ty - P.nb[1] : Ty);
+      const int ky = Ty < 0 ? -1 : (Ty >= P.nb[1] ? 1 : 0);
+      const float by = (float)dy * P.wf[1] - oi.y;
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int Tx = Bi.x + dx, tx = Tx < 0 ? Tx + P.nb[0] : (Tx >= P.nb[0] ? Tx - P.nb[0] : Tx);
+        const int kx = Tx < 0 ? -1 : (Tx >= P.nb[0] ? 1 : 0);
+        const float bx = (float)dx * P.wf[0] - oi.x;
+        const int flat = tx + P.nb[0] * (ty + P.nb[1] * tz);
+        int cnt = 0;
+        if (active) {
+          cnt = bin_count[flat];
           cnt = cnt < P.bcap ? cnt : P.bcap;
-          const BinEntry *be = bins + (size_t)flat * P.bcap;
-          for (int s = 0; s < cnt; ++s) {
+        }
+        const int cmax = __reduce_max_sync(0xffffffffu, cnt);
+        const BinEntry *be = bins + (size_t)flat * P.bcap;
+        for (int s = 0; s < cmax; ++s) {
+          if (s < cnt) {
             const BinEntry b = be[s];
             const unsigned j = b.idx & IDX_MASK;
-            if (j == (unsigned)i) continue;
             const float ex = bx + b.ox, ey = by + b.oy, ez = bz + b.oz;
             const float r2 = ex * ex + ey * ey + ez * ez;
-            if (r2 >= P.rc2_band) continue;
-            const unsigned wc = b.idx >> IDX_BITS;
-            const int mx = kx - ((int)(wc % 3u) - 1), my = ky - ((int)((wc / 3u) % 3u) - 1),
-                      mz = kz - ((int)(wc / 9u) - 1);
-            if (mx < -1 || mx > 1 || my < -1 || my > 1 || mz < -1 || mz > 1) {
-              atomicOr(err, ERR_DRIFT);
-              continue;
+            if (j != (unsigned)i && r2 < P.rc2_band) {
+              const unsigned wc = b.idx >> IDX_BITS;
+              const int mx = kx - ((int)(wc % 3u) - 1), my = ky - ((int)((wc / 3u) % 3u) - 1),
+                        mz = kz - ((int)(wc / 9u) - 1);
+              if (mx < -1 || mx > 1 || my < -1 || my > 1 || mz < -1 || mz > 1) {
+                atomicOr(err, ERR_DRIFT);
+              } else if (nc >= P.kcap) {
+                atomicOr(err, ERR_PAIR_OVERFLOW);
+              } else {
+                const unsigned u = j | ((unsigned)((mx + 1) + 3 * (my + 1) + 9 * (mz + 1)) << IDX_BITS);
+                int pos = nc++;
+                if (!FAST) {  // ascending neighbour index
+                  while (pos > 0 && (s_cand[(pos - 1) * nt + t] & IDX_MASK) > j) {
+                    s_cand[pos * nt + t] = s_cand[(pos - 1) * nt + t];
+                    --pos;
+                  }
+                }
+                s_cand[pos * nt + t] = u;
+              }
             }
-            if (nc >= KMAX || nc >= P.kcap) {
-              atomicOr(err, ERR_PAIR_OVERFLOW);
-              continue;
-            }
-            const unsigned u = j | ((unsigned)((mx + 1) + 3 * (my + 1) + 9 * (mz + 1)) << IDX_BITS);
-            int pos = nc++;
-            while (pos > 0 && (cand[pos - 1] & IDX_MASK) > j) {
-              cand[pos] = cand[pos - 1];
-              --pos;
-            }
-            cand[pos] = u;
           }
         }
       }
     }
-    // pass 2: exact FP64 test, density and pair cache
-    for (int k = 0; k < nc; ++k) {
-      const unsigned u = cand[k];
+  }
+  __syncwarp();
+  // pass 2: exact FP64 test, density and pair cache, in lockstep
+  const int nmax = __reduce_max_sync(0xffffffffu, nc);
+  for (int k = 0; k < nmax; ++k) {
+    if (k < nc) {
+      const unsigned u = s_cand[k * nt + t];
       const unsigned j = u & IDX_MASK, code = u >> IDX_BITS;
       const D4 xj = x[j];
       double cx = xj.x, cy = xj.y, cz = xj.z;
@@ -450,30 +487,33 @@ __global__ void __launch_bounds__(128) k_density(
       }
       const double ex = cx - xi.x, ey = cy - xi.y, ez = cz - xi.z;
       const double r2 = FAST ? dot3_fma(ex, ey, ez, ex, ey, ez) : dot3(ex, ey, ez, ex, ey, ez);
-      if (!(r2 < P.rc2)) continue;
-      const int ej = (int)xj.w;
-      const double rji = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
-      double rij = rji;
-      if (MULTI && ej != ei)
-        rij = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
-      rho += rji;
-      const size_t slot = (size_t)ns * P.n + i;
-      pj[slot] = u;
-      if (FAST) {
-        const double inv_r2 = 1.0 / r2;
-        pe[slot] = D4{ex, ey, ez, rji * inv_r2};
-        pg[slot] = make_double2(rij * inv_r2, 0.0);
-      } else {
-        pe[slot] = D4{ex, ey, ez, r2};
-        pg[slot] = make_double2(rji, rij);
+      if (r2 < P.rc2) {
+        const int ej = (int)xj.w;
+        const double rji =
+            spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+        double rij = rji;
+        if (MULTI && ej != ei)
+          rij = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+        rho += rji;
+        const size_t slot = (size_t)ns * P.n + i;
+        pj[slot] = u;
+        if (FAST) {
+          const double inv_r2 = 1.0 / r2;
+          pe[slot] = D4{ex, ey, ez, rji * inv_r2};
+          if (MULTI) pg[slot] = make_double2(rij * inv_r2, 0.0);
+        } else {
+          pe[slot] = D4{ex, ey, ez, r2};
+          pg[slot] = make_double2(rji, rij);
+        }
+        ++ns;
       }
-      ++ns;
     }
   }
+  if (!valid) return;
   nshort[i] = ns;
   // per-atom quantities
   double alpha = 0.0, beta = 0.0, xi3[3] = {0.0, 0.0, 0.0};
-  if (in_group) {
+  if (active) {
     if (rho > P.rho_cutoff) {  // eph_beta.h:174-197
       atomicAdd(&counters[CNT_RHO_CUTOFF], 1ull);
     } else {

@@ -1,0 +1,196 @@
+/*
+ * LAMMPS fix `eph/gb` (see fix_eph_gb.h): the hooks of the reference fix
+ * (fix_eph.cpp:293-302) calling the GB300 C ABI.  Atom data stays owned by
+ * the engine on the host; each hook copies in what it reads and copies back
+ * what it writes:
+ *   initial_integrate  x, v, f in   -> device integrate -> x, v out
+ *   post_force         f in         -> bins, density, force_prl -> f out
+ *   final_integrate    f in         -> device integrate -> v out
+ *   end_of_step        (device)     -> deposition, FDM, T output; per-atom array out
+ * After the engine re-neighbours (atoms may have moved between ranks or been
+ * re-sorted) the whole atom set is uploaded again.
+ */
+#include "fix_eph_gb.h"
+
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "atom.h"
+#include "comm.h"
+#include "domain.h"
+#include "error.h"
+#include "force.h"
+#include "memory.h"
+#include "neighbor.h"
+#include "random_mars.h"
+#include "update.h"
+
+using namespace LAMMPS_NS;
+using namespace FixConst;
+
+static char *dup_word(const char *s) {
+  const size_t n = std::strlen(s) + 1;
+  char *p = static_cast<char *>(malloc(n));
+  std::memcpy(p, s, n);
+  return p;
+}
+
+FixEPHGB::FixEPHGB(LAMMPS *lmp, int narg, char **arg) : Fix(lmp, narg, arg) {
+  if (narg < 18) error->all(FLERR, "Illegal fix eph/gb command: too few arguments");
+  if (atom->natoms < 1) error->all(FLERR, "fix_eph: error no atoms in simulation");
+  if (comm->nprocs != 1) error->all(FLERR, "fix eph/gb runs on one MPI rank per GPU holding the whole box");
+  vector_flag = 1;
+  size_vector = 2;
+  global_freq = 1;
+  extvector = 1;
+  nevery = 1;
+  peratom_flag = 1;
+  size_peratom_cols = 8;
+  peratom_freq = 1;
+  eph_flag = (int)strtol(arg[4], nullptr, 0);
+  time_integrate = (eph_flag & 0x08) ? 0 : 1;
+  for (int i = 0; i < narg; ++i) words.push_back(dup_word(arg[i]));
+  random = new RanMars(lmp, atoi(arg[3]) + comm->me);
+  grow_arrays(atom->nmax);
+  atom->add_callback(0);
+  create_context();
+}
+
+FixEPHGB::~FixEPHGB() {
+  if (ctx) eph_destroy(ctx);
+  for (char *w : words) free(w);
+  delete random;
+  atom->delete_callback(id, 0);
+  memory->destroy(array);
+}
+
+void FixEPHGB::check(int status, const char *where) {
+  if (status != EPH_OK)
+    error->all(FLERR, std::string("fix eph/gb: ") + where + ": " + eph_status_string(status) + ": " +
+                          eph_last_error(ctx));
+}
+
+void FixEPHGB::create_context() {
+  if (ctx) eph_destroy(ctx);
+  ctx = nullptr;
+  eph_md md;
+  md.ntypes = atom->ntypes;
+  md.mass = atom->mass;
+  for (int k = 0; k < 3; ++k) {
+    md.boxlo[k] = domain->boxlo[k];
+    md.boxhi[k] = domain->boxhi[k];
+  }
+  md.dt = update->dt;
+  md.boltz = force->boltz;
+  md.ftm2v = force->ftm2v;
+  md.skin = neighbor->skin;
+  md.groupbit = groupbit;
+  md.device = device;
+  md.mode = mode;
+  check(eph_create((int)words.size(), words.data(), &md, &ctx), "create");
+  nlocal_dev = -1;
+}
+
+int FixEPHGB::setmask() {
+  return INITIAL_INTEGRATE | POST_FORCE | FINAL_INTEGRATE | END_OF_STEP;
+}
+
+void FixEPHGB::init() {
+  if (domain->dimension == 2) error->all(FLERR, "Cannot use fix eph with 2d simulation");
+  if (domain->nonperiodic != 0) error->all(FLERR, "Cannot use nonperiodic boundares with fix eph");
+  if (domain->triclinic) error->all(FLERR, "Cannot use fix eph with triclinic box");
+  reset_dt();
+}
+
+int FixEPHGB::modify_param(int narg, char **arg) {
+  if (narg < 2) error->all(FLERR, "Illegal fix_modify command");
+  if (strcmp(arg[0], "mode") == 0) {
+    mode = strcmp(arg[1], "exact") == 0 ? EPH_MODE_EXACT : EPH_MODE_FAST;
+  } else if (strcmp(arg[0], "xi") == 0) {
+    xi_on_host = strcmp(arg[1], "host") == 0;
+    return 2;
+  } else if (strcmp(arg[0], "device") == 0) {
+    device = atoi(arg[1]);
+  } else {
+    return 0;
+  }
+  create_context();
+  return 2;
+}
+
+void FixEPHGB::upload_atoms() {
+  const int n = atom->nlocal;
+  check(eph_set_atoms(ctx, n, &atom->x[0][0], &atom->v[0][0], atom->type, atom->mask), "set atoms");
+  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "put f");
+  nlocal_dev = n;
+  last_upload_step = update->ntimestep;
+}
+
+void FixEPHGB::setup(int) { upload_atoms(); }
+
+void FixEPHGB::initial_integrate(int) {
+  if (eph_flag & 0x08) return;
+  if (nlocal_dev != atom->nlocal) upload_atoms();
+  check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST), "put x");
+  check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "put v");
+  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "put f");
+  check(eph_initial_integrate(ctx), "initial_integrate");
+  check(eph_get(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST), "get x");
+  check(eph_get(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "get v");
+}
+
+void FixEPHGB::post_force(int) {
+  // the engine re-neighboured this step: atoms may be re-sorted or wrapped
+  if (neighbor->ago == 0 || nlocal_dev != atom->nlocal) upload_atoms();
+  check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST), "put x");
+  check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "put v");
+  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "put f");
+  int source = EPH_XI_DEVICE_RNG;
+  if (xi_on_host && (eph_flag & 0x02)) {
+    // the engine's own Gaussian stream, three per in-group atom in atom
+    // order, as the reference draws it (fix_eph.cpp:854-860)
+    const int n = atom->nlocal;
+    xi.assign(3 * (size_t)n, 0.0);
+    for (int i = 0; i < n; ++i)
+      if (atom->mask[i] & groupbit)
+        for (int k = 0; k < 3; ++k) xi[3 * (size_t)i + k] = random->gaussian();
+    check(eph_put(ctx, EPH_FIELD_XI, xi.data(), EPH_HOST), "put xi");
+    source = EPH_XI_GIVEN;
+  }
+  check(eph_post_force(ctx, source), "post_force");
+  check(eph_get(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "get f");
+}
+
+void FixEPHGB::final_integrate() {
+  if (eph_flag & 0x08) return;
+  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "put f");
+  check(eph_final_integrate(ctx), "final_integrate");
+  check(eph_get(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "get v");
+}
+
+void FixEPHGB::end_of_step() {
+  check(eph_set_timestep(ctx, (long)update->ntimestep), "set timestep");
+  if (eph_flag & 0x08) check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "put v");
+  check(eph_end_of_step(ctx), "end_of_step");
+  check(eph_get(ctx, EPH_FIELD_PERATOM, &array[0][0], EPH_HOST), "get per-atom array");
+}
+
+void FixEPHGB::reset_dt() {
+  if (ctx) check(eph_reset_dt(ctx, update->dt), "reset_dt");
+}
+
+void FixEPHGB::grow_arrays(int ngrow) {
+  memory->grow(array, ngrow, 8, "eph/gb:array");
+  array_atom = array;
+}
+
+double FixEPHGB::compute_vector(int i) {
+  double v = 0.0;
+  check(eph_compute_vector(ctx, i == 1 ? 1 : 0, &v), "compute_vector");
+  return v;
+}
+
+void FixEPHGB::post_run() { check(eph_post_run(ctx), "post_run"); }
+
+double FixEPHGB::memory_usage() { return 8.0 * 8.0 * atom->nmax; }
