@@ -166,6 +166,25 @@ int eph_launch_count(eph_ctx *ctx, long *out);
 /* in-cutoff pairs (directed) of the last post_force */
 int eph_pair_count(eph_ctx *ctx, long *out);
 
+/* Electronic-grid solve that allocates nothing.  No counterpart in the
+ * reference.  For callers that own all device memory and may not call
+ * cudaMalloc/cudaFree while they run (an engine with its own device pool, a
+ * time-step loop that must not synchronise the device): one EPH_FDM::solve
+ * (eph_fdm.h:267-400, constant C_e and kappa) on caller-owned device arrays of
+ * an nx*ny*nz grid spanning [lo, hi): T is updated in place, dT, S, rho_e,
+ * C_e, kappa and flag are read (dT is not cleared).  The only other memory is
+ * a static scratch array of EPH_NOALLOC_MAX_CELLS + 8 doubles that every GPU
+ * loading this library holds until exit; larger grids return
+ * EPH_ERR_CAPACITY.  The first call on a device looks up that array's device
+ * address, so make it before any stream capture.  All calls share the
+ * scratch: calls that overlap on the GPU race.  Work is ordered on `stream`
+ * (a cudaStream_t, 0 for the default stream) and finished on return; the
+ * number of substeps taken goes to *nsub_out (may be NULL). */
+#define EPH_NOALLOC_MAX_CELLS 262144 /* 64^3 */
+int eph_fdm_solve_noalloc(long nx, long ny, long nz, const double *lo, const double *hi, double dt, long steps,
+                          double *T, const double *dT, const double *S, const double *rho_e, const double *C_e,
+                          const double *kappa, const signed char *flag, void *stream, unsigned *nsub_out);
+
 /* Host-side parametrisation (no GPU needed): the beta file reader and the
  * splines it builds (eph_beta.h:39-128, eph_spline.h:31-142). */
 typedef struct eph_beta eph_beta;

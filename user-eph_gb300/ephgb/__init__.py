@@ -76,6 +76,9 @@ SIGNATURES = {
     "eph_phase_times": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_long)]),
     "eph_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_long)]),
     "eph_pair_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_long)]),
+    "eph_fdm_solve_noalloc": (C.c_int, [C.c_long, C.c_long, C.c_long, _dp, _dp, C.c_double, C.c_long, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.POINTER(C.c_uint)]),
     "eph_beta_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
     "eph_beta_free": (None, [C.c_void_p]),
     "eph_beta_info": (C.c_int, [C.c_void_p, _ip, _dp, _dp]),
