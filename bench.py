@@ -119,12 +119,12 @@ class ClockSampler:
 
 
 def forces_bytes(n_atoms, n_pairs):
-    """Algorithmic HBM bytes of one launch of the force sweep (k_forces):
-    per atom A_i, Bw_i (64 B), pair count (4), T_e at the atom (8), f read and
-    written (64), f_EPH and f_RNG written (64); per in-cutoff pair the cached
-    index (4), e_ij with rho_j(r^2)/r^2 (32) and rho_i(r^2)/r^2 (16).  The
-    neighbours' records are L2 hits and not counted."""
-    return 204 * n_atoms + 52 * n_pairs
+    """Algorithmic HBM bytes of one launch of the force sweep (k_forces, FAST,
+    one element): per atom A_i, Bw_i (64 B), pair count (4), T_e at the atom
+    (8), f read and written (64), f_EPH and f_RNG written (64); per in-cutoff
+    pair the cached index (4) and e_ij with rho_j(r^2)/r^2 (32).  The
+    neighbours' records (A_j, Bw_j) are L2 hits and not counted."""
+    return 204 * n_atoms + 36 * n_pairs
 
 
 def run_gpu(args, rank, world):

@@ -48,7 +48,7 @@ extern "C" {
 #define EPH_FIELD_X 0       /* positions, n x 3 (put/get) */
 #define EPH_FIELD_V 1       /* velocities, n x 3 (put/get) */
 #define EPH_FIELD_F 2       /* total force, n x 3 (put/get) */
-#define EPH_FIELD_XI 3      /* Gaussian deviates for the next post_force, n x 3 (put) */
+#define EPH_FIELD_XI 3      /* Gaussian deviates: put = for the next post_force; get = those the last used, n x 3 */
 #define EPH_FIELD_F_EPH 4   /* friction force of the last post_force, n x 3 (get) */
 #define EPH_FIELD_F_RNG 5   /* random force of the last post_force, n x 3 (get) */
 #define EPH_FIELD_RHO 6     /* site density rho_i, n (get) */
@@ -119,6 +119,12 @@ int eph_end_of_step(eph_ctx *ctx);
  * EPH_XI_GIVEN every step reuses the deviates last put. */
 int eph_step(eph_ctx *ctx, int nsteps, int xi_source);
 
+/* Replay eph_step from a CUDA graph of one captured step (on != 0): one
+ * launch per step instead of one per kernel.  No reference counterpart.
+ * Re-captured after eph_set_atoms, eph_reset_dt, eph_set_capacity or a
+ * change of deviate source; bypassed while profiling is on. */
+int eph_set_graph(eph_ctx *ctx, int on);
+
 /* FixEPH::compute_vector (fix_eph.cpp:940-948): 0 -> cumulative energy
  * transferred to the electrons, 1 -> mean electronic temperature
  * (eph_fdm.h:189-196). */
@@ -165,6 +171,25 @@ int eph_phase_times(eph_ctx *ctx, double *ms, long *launches);
 int eph_launch_count(eph_ctx *ctx, long *out);
 /* in-cutoff pairs (directed) of the last post_force */
 int eph_pair_count(eph_ctx *ctx, long *out);
+
+/* Batched replicas: many independent fix instances (each its own words,
+ * box, atoms, grid and seed) on one GPU, stepped together: one step of every
+ * replica is captured as parallel branches of one CUDA graph and each
+ * eph_batch_step step is one graph launch.  Each replica's results are those
+ * of the same replica run alone with eph_step (device deviates).  No
+ * reference counterpart (the reference runs one system per LAMMPS run). */
+typedef struct eph_batch eph_batch;
+int eph_batch_create(int nrep, const int *narg, const char *const *const *arg, const eph_md *md, eph_batch **out);
+void eph_batch_destroy(eph_batch *batch);
+const char *eph_batch_last_error(const eph_batch *batch);
+int eph_batch_set_atoms(eph_batch *batch, int rep, int n, const double *x, const double *v, const int *type,
+                        const int *mask);
+int eph_batch_step(eph_batch *batch, int nsteps);
+int eph_batch_synchronize(eph_batch *batch);
+/* the context of replica rep (for eph_get, eph_compute_vector, ...) */
+eph_ctx *eph_batch_context(eph_batch *batch, int rep);
+/* kernels one batched step launches (inside its graph) */
+int eph_batch_launch_count(eph_batch *batch, long *per_step);
 
 /* Electronic-grid solve that allocates nothing.  No counterpart in the
  * reference.  For callers that own all device memory and may not call
