@@ -214,6 +214,38 @@ def run_gpu(args, rank, world):
     return out
 
 
+def run_batched(args, dev):
+    """The batched form: 64 independent cascades (32k-500k atoms, grids
+    16^3-48^3) stepped together, one CUDA-graph launch per step, against the
+    same replicas stepped one after another through the plain path."""
+    import ephgb
+    from ephgb import workloads as W
+
+    with tempfile.TemporaryDirectory() as wd:
+        bf = W.write_beta_file(os.path.join(wd, "synth.beta"))
+        reps = W.batched_cascades(64, beta_file=bf)
+        total = sum(at.n for _, at in reps)
+        batch = ephgb.Batch(reps, dt=DT, device=dev)
+        del reps
+        batch.step(2)
+        batch.synchronize()
+        k = args.batch_steps
+        t0 = time.perf_counter()
+        batch.step(k)
+        batch.synchronize()
+        t_batch = time.perf_counter() - t0
+        # the same replicas through the plain path, one after another
+        t0 = time.perf_counter()
+        for rep in batch.replicas:
+            rep.step(k)
+            rep.synchronize()
+        t_seq = time.perf_counter() - t0
+        return {"value": total * k / t_batch, "unit": METRIC, "replicas": len(batch.replicas), "atoms": total,
+                "steps": k, "ms_per_step": 1000.0 * t_batch / k, "launches_per_step": batch.launches_per_step(),
+                "sequential_value": total * k / t_seq, "speedup_vs_sequential": t_seq / t_batch,
+                "timing": "host wall clock around the graph launches, synchronised"}
+
+
 def cpu_baseline(threads, steps=1, warm=1):
     """The CPU restatement (oracle port) on the same workload: `steps` steps
     of the full system after `warm` warm-up steps; time of the fix's own hooks
@@ -245,6 +277,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="omit the end-to-end leg")
+    ap.add_argument("--no-batched", action="store_true", help="omit the batched-replicas leg")
+    ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--cells", type=int, default=CELLS, help="fcc cells per edge (profiling cases)")
     ap.add_argument("--grid", type=int, default=GRID[0], help="FDM cells per edge (profiling cases)")
     args = ap.parse_args()
@@ -305,6 +339,12 @@ def main():
     if "t_e2e" in res:
         line["e2e"] = {"value": world * n * res["e2e_steps"] / res["t_e2e"], "unit": METRIC,
                        "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"]}
+    if not args.no_batched:
+        line["batched"] = run_batched(args, int(os.environ.get("LOCAL_RANK", rank)))
+        if world > 1:
+            t = torch.tensor([line["batched"]["value"]], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+            line["batched"]["value"] = float(t.item())
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(threads, steps=1, warm=1).items() if k != "seconds"}
     if rank == 0:

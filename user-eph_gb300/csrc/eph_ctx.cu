@@ -61,7 +61,6 @@ struct eph_ctx {
   double dt = 0, boltz = 0, ftm2v = 0, skin = 0;
   int groupbit = 1, mode = EPH_MODE_FAST;
   long ntimestep = 0;
-  unsigned long long rng_step = 0;
 
   StepParams P{};
   bool multi = false;
@@ -100,10 +99,18 @@ struct eph_ctx {
   long phase_launches[EPH_NPHASES] = {0};
   long launches = 0;
 
+  // one captured engine step replayed by eph_step (eph_set_graph)
+  bool use_graph = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_xi = -1;
+  long graph_launches = 0;  // kernels in one replay
+
   DevBuf<double> scal;  // 0 Ee, 1 E_local, 2 T_total
   DevBuf<unsigned> d_err;
   DevBuf<unsigned long long> counters;
   DevBuf<int> wrapflag;
+  DevBuf<unsigned long long> step_ctr;  // post_force calls so far (the Philox counter)
   unsigned *h_err = nullptr;  // pinned
 };
 
@@ -275,13 +282,7 @@ int launch_final(eph_ctx *c) {
 
 template <bool FAST, bool MULTI>
 void launch_density_t(eph_ctx *c, int xi_mode) {
-  const size_t smem = sizeof(unsigned) * (size_t)c->kcap * BLOCK;
-  static size_t configured = 0;  // per instantiation: the largest dynamic shared memory allowed so far
-  if (smem > configured) {
-    cudaFuncSetAttribute(k_density<FAST, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = smem;
-  }
-  k_density<FAST, MULTI><<<nblocks(c->n), BLOCK, smem, c->stream>>>(
+  k_density<FAST, MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
       c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p,
       c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,
       c->wrapflag.p, c->d_err.p, c->counters.p);
@@ -306,13 +307,12 @@ void launch_forces_m(eph_ctx *c) {
 // post_force: bins, density, friction pre-vector, forces
 int launch_post_force(eph_ctx *c, int xi_mode) {
   const int nb = nblocks(c->n);
-  c->P.step = c->rng_step;
   {
     PhaseScope ps(c, EPH_PHASE_BIN);
     ps.launched();
     CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
     k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
-                                       c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p);
+                                       c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 1);
     ps.launched();
     k_bin_sort<<<nblocks(c->nbins), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p, c->bins.p);
   }
@@ -350,7 +350,6 @@ int launch_post_force(eph_ctx *c, int xi_mode) {
     }
   }
   CUDA_TRY(c, cudaGetLastError());
-  c->rng_step += 1;
   return EPH_OK;
 }
 
@@ -413,6 +412,51 @@ int write_T_output(eph_ctx *c) {
     if (c->grid.save_temperature(c->args.T_out.c_str(), (int)(c->ntimestep / c->args.T_freq)))
       return fail(c, EPH_ERR_FILE, "cannot write " + c->args.T_out);
   }
+  return EPH_OK;
+}
+
+// One engine step (Verlet::run order) issued on the context's stream; the
+// same sequence is executed directly or captured into a graph.
+int record_step(eph_ctx *c, int xi_mode) {
+  int r;
+  if ((r = launch_initial(c, 1))) return r;
+  // force clear + the external (pair) force
+  if (c->have_fext)
+    CUDA_TRY(c, cudaMemcpyAsync(c->f.p, c->fext.p, sizeof(D4) * (size_t)c->n, cudaMemcpyDeviceToDevice, c->stream));
+  else
+    CUDA_TRY(c, cudaMemsetAsync(c->f.p, 0, sizeof(D4) * (size_t)c->n, c->stream));
+  if ((r = launch_post_force(c, xi_mode))) return r;
+  if ((r = launch_final(c))) return r;
+  return launch_end_of_step(c);
+}
+
+void drop_graph(eph_ctx *c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr;
+  c->graph = nullptr;
+  c->graph_xi = -1;
+}
+
+// Capture one step into c->gexec (replays must not change host-side state:
+// the random-number counter and the wrap flag live on the device).
+int capture_step(eph_ctx *c, int xi_mode) {
+  drop_graph(c);
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  const long before = c->launches;
+  const int r = record_step(c, xi_mode);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->graph_launches = c->launches - before;
+  c->launches = before;
+  if (r || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return r ? r : fail(c, EPH_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
+  }
+  c->graph = g;
+  CUDA_TRY(c, cudaGraphInstantiate(&c->gexec, g, 0));
+  c->graph_xi = xi_mode;
   return EPH_OK;
 }
 
@@ -504,6 +548,8 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
   CUDA_TRY(c, c->d_err.alloc(1));
   CUDA_TRY(c, c->counters.alloc(NCOUNTERS));
   CUDA_TRY(c, c->wrapflag.alloc(1));
+  CUDA_TRY(c, c->step_ctr.alloc(1));
+  CUDA_TRY(c, cudaMemset(c->step_ctr.p, 0, sizeof(unsigned long long)));
   CUDA_TRY(c, c->scal.alloc(4));
   CUDA_TRY(c, c->gsum.alloc(1));
   CUDA_TRY(c, cudaMemset(c->d_err.p, 0, sizeof(unsigned)));
@@ -548,6 +594,7 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
   P.gdy = g.dy;
   P.gdz = g.dz;
   P.seed = (unsigned)c->args.seed;
+  P.step = c->step_ctr.p;
   set_time_params(c);
   // bins: edge >= rc (1 + 5e-5), at least 3 per axis
   for (int k = 0; k < 3; ++k) {
@@ -566,6 +613,7 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
 void eph_destroy(eph_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
   collect_marks(c);
   for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -575,6 +623,7 @@ void eph_destroy(eph_ctx *c) {
 
 int eph_set_capacity(eph_ctx *c, int bin_capacity, int pair_capacity) {
   if (!c) return EPH_ERR_ARG;
+  drop_graph(c);
   if (pair_capacity > KMAX) return fail(c, EPH_ERR_ARG, "pair capacity above the compiled maximum");
   if (bin_capacity > 0) c->bcap = bin_capacity;
   if (pair_capacity > 0) c->kcap = pair_capacity;
@@ -591,6 +640,7 @@ int eph_set_capacity(eph_ctx *c, int bin_capacity, int pair_capacity) {
 
 int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const int *htype, const int *hmask) {
   if (!c) return EPH_ERR_ARG;
+  drop_graph(c);
   if (n < 1) return fail(c, EPH_ERR_ARG, "fix_eph: error no atoms in simulation");
   if ((unsigned)n > IDX_MASK) return fail(c, EPH_ERR_ARG, "too many atoms for one context");
   if (!hx || !hv || !htype) return fail(c, EPH_ERR_ARG, "null atom buffer");
@@ -652,7 +702,7 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
   CUDA_TRY(c, cudaMemsetAsync(c->wrapflag.p, 0xff, sizeof(int), c->stream));
   CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
   k_bin<<<nblocks(n), BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
-                                             c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p);
+                                             c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 0);
   CUDA_TRY(c, cudaMemsetAsync(c->wrapflag.p, 0, sizeof(int), c->stream));
   c->have_fext = false;
   CUDA_TRY(c, cudaGetLastError());
@@ -678,6 +728,7 @@ int eph_put(eph_ctx *c, int field, const double *src, int where) {
     case EPH_FIELD_F_EXT:
       if (!c->fext.p) CUDA_TRY(c, c->fext.alloc((size_t)c->n));
       dst = &c->fext;
+      if (!c->have_fext) drop_graph(c);  // the captured step cleared f instead of copying it
       c->have_fext = true;
       break;
     default: return fail(c, EPH_ERR_ARG, "field cannot be written");
@@ -710,7 +761,7 @@ int eph_get(eph_ctx *c, int field, double *dst, int where) {
     case EPH_FIELD_X: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->x.p, d); break;
     case EPH_FIELD_V: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->v.p, d); break;
     case EPH_FIELD_F: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->f.p, d); break;
-    case EPH_FIELD_XI: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->xi.p, d); break;
+    case EPH_FIELD_XI: k_get_xi<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->A.p, c->Bw.p, d); break;
     case EPH_FIELD_F_EPH: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->f_eph.p, d); break;
     case EPH_FIELD_F_RNG: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->f_rng.p, d); break;
     case EPH_FIELD_W: k_get_w<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->Bw.p, d); break;
@@ -771,20 +822,26 @@ int eph_step(eph_ctx *c, int nsteps, int xi_source) {
   if (r) return r;
   if (xi_source == EPH_XI_GIVEN && !c->have_xi && (c->P.flags & FLAG_RANDOM))
     return fail(c, EPH_ERR_STATE, "EPH_XI_GIVEN without eph_put(EPH_FIELD_XI)");
+  const int xi_mode = xi_source == EPH_XI_GIVEN ? 1 : 0;
+  const bool graph = c->use_graph && !c->profiling;
+  if (graph && (!c->gexec || c->graph_xi != xi_mode) && (r = capture_step(c, xi_mode))) return r;
   for (int s = 0; s < nsteps; ++s) {
     c->ntimestep += 1;
-    if ((r = launch_initial(c, 1))) return r;
-    // force clear + the external (pair) force
-    if (c->have_fext)
-      CUDA_TRY(c, cudaMemcpyAsync(c->f.p, c->fext.p, sizeof(D4) * (size_t)c->n, cudaMemcpyDeviceToDevice,
-                                  c->stream));
-    else
-      CUDA_TRY(c, cudaMemsetAsync(c->f.p, 0, sizeof(D4) * (size_t)c->n, c->stream));
-    if ((r = launch_post_force(c, xi_source == EPH_XI_GIVEN ? 1 : 0))) return r;
-    if ((r = launch_final(c))) return r;
-    if ((r = launch_end_of_step(c))) return r;
+    if (graph) {
+      CUDA_TRY(c, cudaGraphLaunch(c->gexec, c->stream));
+      c->launches += c->graph_launches;
+    } else if ((r = record_step(c, xi_mode))) {
+      return r;
+    }
     if ((r = write_T_output(c))) return r;
   }
+  return EPH_OK;
+}
+
+int eph_set_graph(eph_ctx *c, int on) {
+  if (!c) return EPH_ERR_ARG;
+  c->use_graph = on != 0;
+  if (!c->use_graph) drop_graph(c);
   return EPH_OK;
 }
 
@@ -814,6 +871,7 @@ int eph_compute_vector(eph_ctx *c, int i, double *out) {
 
 int eph_reset_dt(eph_ctx *c, double dt) {
   if (!c || !(dt > 0)) return EPH_ERR_ARG;
+  drop_graph(c);
   c->dt = dt;
   set_time_params(c);
   return EPH_OK;
@@ -904,6 +962,169 @@ int eph_get_counter(eph_ctx *c, int which, long *out) {
   CUDA_TRY(c, cudaMemcpyAsync(&v, c->counters.p + which, sizeof(v), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   *out = (long)v;
+  return EPH_OK;
+}
+
+// ------------------------------------------------------ batched replicas
+
+struct eph_batch {
+  std::vector<eph_ctx *> reps;
+  cudaStream_t main = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  long launches_per_step = 0;
+  std::string err;
+};
+
+static void batch_drop_graph(eph_batch *b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->gexec = nullptr;
+  b->graph = nullptr;
+}
+
+int eph_batch_create(int nrep, const int *narg, const char *const *const *arg, const eph_md *md, eph_batch **out) {
+  if (!out || nrep < 1 || !narg || !arg || !md) return EPH_ERR_ARG;
+  *out = nullptr;
+  eph_batch *b = new (std::nothrow) eph_batch();
+  if (!b) return EPH_ERR_ARG;
+  *out = b;
+  for (int r = 0; r < nrep; ++r) {
+    eph_ctx *c = nullptr;
+    const int rc = eph_create(narg[r], arg[r], &md[r], &c);
+    b->reps.push_back(c);
+    if (rc) {
+      b->err = "replica " + std::to_string(r) + ": " + eph_last_error(c);
+      return rc;
+    }
+    if (md[r].device != md[0].device) {
+      b->err = "all replicas of a batch run on one device";
+      return EPH_ERR_ARG;
+    }
+  }
+  if (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+    b->err = "cannot create the batch stream";
+    return EPH_ERR_CUDA;
+  }
+  b->joins.assign(nrep, nullptr);
+  for (auto &e : b->joins)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return EPH_ERR_CUDA;
+  return EPH_OK;
+}
+
+void eph_batch_destroy(eph_batch *b) {
+  if (!b) return;
+  if (b->main) cudaStreamSynchronize(b->main);
+  batch_drop_graph(b);
+  for (eph_ctx *c : b->reps) eph_destroy(c);
+  for (auto e : b->joins)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->main) cudaStreamDestroy(b->main);
+  delete b;
+}
+
+const char *eph_batch_last_error(const eph_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+eph_ctx *eph_batch_context(eph_batch *b, int rep) {
+  if (!b || rep < 0 || rep >= (int)b->reps.size()) return nullptr;
+  return b->reps[rep];
+}
+
+int eph_batch_set_atoms(eph_batch *b, int rep, int n, const double *x, const double *v, const int *type,
+                        const int *mask) {
+  eph_ctx *c = eph_batch_context(b, rep);
+  if (!c) return EPH_ERR_ARG;
+  batch_drop_graph(b);
+  return eph_set_atoms(c, n, x, v, type, mask);
+}
+
+// Capture one step of every replica as parallel branches of one graph.
+static int batch_capture(eph_batch *b) {
+  batch_drop_graph(b);
+  for (eph_ctx *c : b->reps) {
+    if (c->n <= 0) {
+      b->err = "a replica has no atoms";
+      return EPH_ERR_STATE;
+    }
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return EPH_ERR_CUDA;
+  }
+  if (cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return EPH_ERR_CUDA;
+  int rc = EPH_OK;
+  long launches = 0;
+  if (cudaEventRecord(b->fork, b->main) != cudaSuccess) rc = EPH_ERR_CUDA;
+  for (size_t r = 0; r < b->reps.size() && !rc; ++r) {
+    eph_ctx *c = b->reps[r];
+    if (cudaStreamWaitEvent(c->stream, b->fork, 0) != cudaSuccess) {
+      rc = EPH_ERR_CUDA;
+      break;
+    }
+    const long before = c->launches;
+    rc = record_step(c, 0);
+    launches += c->launches - before;
+    c->launches = before;
+    if (rc) {
+      b->err = "replica " + std::to_string(r) + ": " + c->err;
+      break;
+    }
+    if (cudaEventRecord(b->joins[r], c->stream) != cudaSuccess || cudaStreamWaitEvent(b->main, b->joins[r], 0) != cudaSuccess)
+      rc = EPH_ERR_CUDA;
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(b->main, &g);
+  if (rc || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (!rc) b->err = std::string("batch capture: ") + cudaGetErrorString(e);
+    return rc ? rc : EPH_ERR_CUDA;
+  }
+  b->graph = g;
+  if (cudaGraphInstantiate(&b->gexec, g, 0) != cudaSuccess) {
+    b->err = "cannot instantiate the batch graph";
+    return EPH_ERR_CUDA;
+  }
+  b->launches_per_step = launches;
+  return EPH_OK;
+}
+
+int eph_batch_step(eph_batch *b, int nsteps) {
+  if (!b || nsteps < 0) return EPH_ERR_ARG;
+  int rc;
+  if (!b->gexec && (rc = batch_capture(b))) return rc;
+  for (int s = 0; s < nsteps; ++s) {
+    if (cudaGraphLaunch(b->gexec, b->main) != cudaSuccess) {
+      b->err = "graph launch failed";
+      return EPH_ERR_CUDA;
+    }
+    for (eph_ctx *c : b->reps) {
+      c->ntimestep += 1;
+      if (c->args.T_freq > 0) {
+        if (cudaStreamSynchronize(b->main) != cudaSuccess) return EPH_ERR_CUDA;
+        if ((rc = write_T_output(c))) return rc;
+      }
+    }
+  }
+  return EPH_OK;
+}
+
+int eph_batch_synchronize(eph_batch *b) {
+  if (!b) return EPH_ERR_ARG;
+  if (cudaStreamSynchronize(b->main) != cudaSuccess) return EPH_ERR_CUDA;
+  for (size_t r = 0; r < b->reps.size(); ++r) {
+    const int rc = eph_synchronize(b->reps[r]);
+    if (rc) {
+      b->err = "replica " + std::to_string(r) + ": " + b->reps[r]->err;
+      return rc;
+    }
+  }
+  return EPH_OK;
+}
+
+int eph_batch_launch_count(eph_batch *b, long *per_step) {
+  if (!b || !per_step) return EPH_ERR_ARG;
+  *per_step = b->launches_per_step;
   return EPH_OK;
 }
 

@@ -32,7 +32,8 @@ struct __align__(16) U128 {
   unsigned long long lo, hi;  // two's-complement 128-bit fixed point, 2^-64 units
 };
 
-constexpr int KMAX = 128;  // largest pair capacity (shared-memory candidate rows of one atom)
+constexpr int KMAX = 128;   // largest pair capacity (rows of one atom in the pair arrays)
+constexpr int CAND_SMEM = 48;  // candidate rows of one atom kept in shared memory
 constexpr unsigned IDX_BITS = 27;
 constexpr unsigned IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr unsigned CODE_NOSHIFT = 13;  // (0,0,0) image of the 3x3x3 code
@@ -76,18 +77,37 @@ struct StepParams {
   long gnx, gny, gnz, ncells;
   double gx0, gy0, gz0, gdx, gdy, gdz;
   double prescale;  // dV * dt (eph_fdm.h:176)
-  // random numbers
+  // random numbers: Philox key = seed, counter = (atom, *step) with *step the
+  // number of post_force calls so far, kept on the device so a captured
+  // step replays with fresh numbers
   unsigned seed;
-  unsigned long long step;
+  unsigned long long *step;
 };
 
 // ------------------------------------------------------------------ helpers
+
+// v > 0 and w < c for non-negative c, on the bit patterns: integer compares
+// keep these tests off the FP64 pipe (IEEE order of non-negative doubles is
+// the order of their bits).
+__device__ __forceinline__ bool pos_double(double v) { return __double_as_longlong(v) > 0; }
+__device__ __forceinline__ bool below(double v, double c) { return __double_as_longlong(v) < __double_as_longlong(c); }
+
+// (size_t)y for a non-negative double y, by integer work on its bits (the
+// conversion instruction runs on the FP64 pipe); y >= 2^53, negative or NaN
+// gives ~0ull.
+__device__ __forceinline__ unsigned long long trunc_index(double y) {
+  const long long b = __double_as_longlong(y);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (b < 0 || e > 1075) return ~0ull;
+  if (e < 1023) return 0ull;
+  return (((unsigned long long)b & ((1ull << 52) - 1ull)) | (1ull << 52)) >> (1075 - e);
+}
 
 template <bool FAST>
 __device__ __forceinline__ double spline_eval(const D4 *__restrict__ tab, double inv_dx, int n, double x,
                                               unsigned *err) {
   // eph_spline.h:134-142: index floor(x/dx), value a + x(b + x(c + x d))
-  unsigned long long idx = (unsigned long long)(x * inv_dx);
+  unsigned long long idx = trunc_index(x * inv_dx);
   if (idx >= (unsigned long long)n) {
     atomicOr(err, ERR_SPLINE_RANGE);
     idx = (unsigned long long)(n - 1);
@@ -95,6 +115,16 @@ __device__ __forceinline__ double spline_eval(const D4 *__restrict__ tab, double
   const D4 c = tab[idx];
   if (FAST) return fma(x, fma(x, fma(x, c.w, c.z), c.y), c.x);
   return c.x + x * (c.y + x * (c.z + x * c.w));
+}
+
+// 1/x for FAST mode: the hardware estimate refined by two Newton-Raphson
+// steps r <- r + r (1 - x r) (quadratic convergence); x > 0 and normal.
+__device__ __forceinline__ double recip_nr(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  r = fma(r, fma(-x, r, 1.0), r);
+  r = fma(r, fma(-x, r, 1.0), r);
+  return r;
 }
 
 __device__ __forceinline__ double dot3(double ax, double ay, double az, double bx, double by, double bz) {
@@ -299,8 +329,9 @@ __global__ void k_final_integrate(StepParams P, D4 *__restrict__ v, const D4 *__
 __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, const int *__restrict__ wrapflag,
                       int *__restrict__ bin_count, BinEntry *__restrict__ bins, int4 *__restrict__ atom_bin,
                       float4 *__restrict__ atom_off, unsigned *__restrict__ err,
-                      unsigned long long *__restrict__ counters) {
+                      unsigned long long *__restrict__ counters, int bump_step) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && bump_step) *P.step += 1ull;  // read by the density sweep that follows
   if (i >= P.n) return;
   D4 xi = x[i];
   if (*wrapflag) {
@@ -391,7 +422,9 @@ __global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_coun
 //   pg: (EXACT) rho_j(r^2), rho_i(r^2); (FAST, several elements) rho_i(r^2)/r^2
 // A[i] = {rho_i, alpha_i (EXACT) | alpha_i/rho_i (FAST), xi_x, xi_y}
 // Bw[i] = {xi_z, w_i} (w written by the friction sweep)
-// Dynamic shared memory: kcap x blockDim unsigned (candidate rows).
+// Candidates: the first CAND_SMEM rows of an atom live in shared memory
+// ([CAND_SMEM][blockDim]), further ones in the atom's own rows of pj (read
+// back before pass 2 overwrites them: pair slot <= candidate slot).
 template <bool FAST, bool MULTI>
 __global__ void __launch_bounds__(128) k_density(
     StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
@@ -401,12 +434,19 @@ __global__ void __launch_bounds__(128) k_density(
     D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell,
     double *__restrict__ Te_i, int *__restrict__ wrapflag, unsigned *__restrict__ err,
     unsigned long long *__restrict__ counters) {
-  extern __shared__ unsigned s_cand[];  // [kcap][blockDim.x]
+  __shared__ unsigned s_cand[CAND_SMEM * 128];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int t = threadIdx.x, nt = blockDim.x;
   if (i == 0) *wrapflag = 0;  // the binning kernel has read it
   const bool valid = i < P.n;
   const bool active = valid && (mask[i] & P.groupbit) != 0;
+  auto cget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : pj[(size_t)k * P.n + i]; };
+  auto cset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM)
+      s_cand[k * nt + t] = u;
+    else
+      pj[(size_t)k * P.n + i] = u;
+  };
   D4 xi = D4{0.0, 0.0, 0.0, 0.0};
   if (valid) xi = x[i];
   const int ei = (int)xi.w;
@@ -457,12 +497,14 @@ __global__ void __launch_bounds__(128) k_density(
                 const unsigned u = j | ((unsigned)((mx + 1) + 3 * (my + 1) + 9 * (mz + 1)) << IDX_BITS);
                 int pos = nc++;
                 if (!FAST) {  // ascending neighbour index
-                  while (pos > 0 && (s_cand[(pos - 1) * nt + t] & IDX_MASK) > j) {
-                    s_cand[pos * nt + t] = s_cand[(pos - 1) * nt + t];
+                  while (pos > 0) {
+                    const unsigned prev = cget(pos - 1);
+                    if ((prev & IDX_MASK) <= j) break;
+                    cset(pos, prev);
                     --pos;
                   }
                 }
-                s_cand[pos * nt + t] = u;
+                cset(pos, u);
               }
             }
           }
@@ -475,7 +517,7 @@ __global__ void __launch_bounds__(128) k_density(
   const int nmax = __reduce_max_sync(0xffffffffu, nc);
   for (int k = 0; k < nmax; ++k) {
     if (k < nc) {
-      const unsigned u = s_cand[k * nt + t];
+      const unsigned u = cget(k);
       const unsigned j = u & IDX_MASK, code = u >> IDX_BITS;
       const D4 xj = x[j];
       double cx = xj.x, cy = xj.y, cz = xj.z;
@@ -487,7 +529,7 @@ __global__ void __launch_bounds__(128) k_density(
       }
       const double ex = cx - xi.x, ey = cy - xi.y, ez = cz - xi.z;
       const double r2 = FAST ? dot3_fma(ex, ey, ez, ex, ey, ez) : dot3(ex, ey, ez, ex, ey, ez);
-      if (r2 < P.rc2) {
+      if (below(r2, P.rc2)) {  // r2 >= 0
         const int ej = (int)xj.w;
         const double rji =
             spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
@@ -498,7 +540,7 @@ __global__ void __launch_bounds__(128) k_density(
         const size_t slot = (size_t)ns * P.n + i;
         pj[slot] = u;
         if (FAST) {
-          const double inv_r2 = 1.0 / r2;
+          const double inv_r2 = recip_nr(r2);
           pe[slot] = D4{ex, ey, ez, rji * inv_r2};
           if (MULTI) pg[slot] = make_double2(rij * inv_r2, 0.0);
         } else {
@@ -523,7 +565,7 @@ __global__ void __launch_bounds__(128) k_density(
     if (FAST && rho > 0) alpha = alpha / rho;
     if (P.flags & 0x02) {
       if (xi_mode == 0) {
-        gaussian3(P.seed, P.step, (unsigned)i, xi3);
+        gaussian3(P.seed, *P.step, (unsigned)i, xi3);
       } else {
         const D4 g = xi_given[i];
         xi3[0] = g.x;
@@ -554,7 +596,7 @@ __global__ void __launch_bounds__(128) k_friction_w(StepParams P, const int *__r
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const D4 Ai = A[i];
-  if (!(mask[i] & P.groupbit) || !(Ai.x > 0)) return;  // Bw[i].yzw stays 0
+  if (!(mask[i] & P.groupbit) || !pos_double(Ai.x)) return;  // Bw[i].yzw stays 0
   const D4 vi = v[i];
   const int ns = nshort[i];
   double wx = 0.0, wy = 0.0, wz = 0.0;
@@ -602,7 +644,7 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
   if (i >= P.n) return;
   double fex = 0.0, fey = 0.0, fez = 0.0, frx = 0.0, fry = 0.0, frz = 0.0;
   const D4 Ai = A[i];
-  if ((mask[i] & P.groupbit) && Ai.x > 0) {
+  if ((mask[i] & P.groupbit) && pos_double(Ai.x)) {
     const D4 Bi = Bw[i];
     const double xix = Ai.z, xiy = Ai.w, xiz = Bi.x;
     const int ns = nshort[i];
@@ -610,7 +652,7 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
       const size_t slot = (size_t)k * P.n + i;
       const unsigned j = pj[slot] & IDX_MASK;
       const D4 Aj = A[j];
-      if (!(Aj.x > 0)) continue;
+      if (!pos_double(Aj.x)) continue;
       const D4 e = pe[slot];
       const double2 g = pg[slot];
       const D4 Bj = Bw[j];
@@ -870,6 +912,15 @@ __global__ void k_get_w(int n, const D4 *__restrict__ Bw, double *__restrict__ d
   dst[3 * (size_t)i + 0] = b.y;
   dst[3 * (size_t)i + 1] = b.z;
   dst[3 * (size_t)i + 2] = b.w;
+}
+
+// the deviates the last post_force used (A.z, A.w, Bw.x)
+__global__ void k_get_xi(int n, const D4 *__restrict__ A, const D4 *__restrict__ Bw, double *__restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dst[3 * (size_t)i + 0] = A[i].z;
+  dst[3 * (size_t)i + 1] = A[i].w;
+  dst[3 * (size_t)i + 2] = Bw[i].x;
 }
 
 __global__ void k_set_elem(int n, const int *__restrict__ type, const int *__restrict__ type_map,

@@ -72,6 +72,16 @@ SIGNATURES = {
     "eph_synchronize": (C.c_int, [C.c_void_p]),
     "eph_get_counter": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_long)]),
     "eph_set_capacity": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "eph_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "eph_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.POINTER(C.c_char_p)),
+                                   C.POINTER(eph_md), C.POINTER(C.c_void_p)]),
+    "eph_batch_destroy": (None, [C.c_void_p]),
+    "eph_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "eph_batch_set_atoms": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _ip, _ip]),
+    "eph_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "eph_batch_synchronize": (C.c_int, [C.c_void_p]),
+    "eph_batch_context": (C.c_void_p, [C.c_void_p, C.c_int]),
+    "eph_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_long)]),
     "eph_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "eph_phase_times": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_long)]),
     "eph_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_long)]),
@@ -346,8 +356,90 @@ class FixEPH:
     def set_stream(self, stream_ptr):
         self._check(self.L.eph_set_stream(self.h, C.c_void_p(stream_ptr)))
 
+    def set_graph(self, on=True):
+        self._check(self.L.eph_set_graph(self.h, 1 if on else 0))
+
     def set_timestep(self, n):
         self._check(self.L.eph_set_timestep(self.h, n))
+
+
+class _View(FixEPH):
+    """A replica's context owned by a Batch (not destroyed on its own)."""
+
+    def __init__(self, L, h, words, n):
+        self.L, self.h, self.n = L, h, n
+        self.ncells = grid_cells(words)
+
+    def __del__(self):
+        pass
+
+
+class Batch:
+    """Batched replicas: independent fix instances stepped together, one
+    CUDA-graph launch per step (eph_batch_* in include/eph_gb.h)."""
+
+    def __init__(self, replicas, dt=0.001, skin=1.0, boltz=workloads.BOLTZ, ftm2v=workloads.FTM2V, device=0,
+                 mode=MODE_FAST):
+        """replicas: list of (words, atoms)."""
+        L = lib()
+        self.L = L
+        R = len(replicas)
+        self._keep = []
+        mds = (eph_md * R)()
+        argvs = (C.POINTER(C.c_char_p) * R)()
+        nargs = (C.c_int * R)()
+        for r, (words, atoms) in enumerate(replicas):
+            mass = np.ascontiguousarray(atoms.mass, dtype=np.float64)
+            argv = (C.c_char_p * len(words))(*[w.encode() for w in words])
+            self._keep += [mass, argv]
+            md = mds[r]
+            md.ntypes = len(mass) - 1
+            md.mass = mass.ctypes.data_as(_dp)
+            for k in range(3):
+                md.boxlo[k] = float(atoms.boxlo[k])
+                md.boxhi[k] = float(atoms.boxhi[k])
+            md.dt, md.boltz, md.ftm2v, md.skin = dt, boltz, ftm2v, skin
+            md.groupbit, md.device, md.mode = 1, device, mode
+            argvs[r] = C.cast(argv, C.POINTER(C.c_char_p))
+            nargs[r] = len(words)
+        h = C.c_void_p()
+        rc = L.eph_batch_create(R, nargs, argvs, mds, C.byref(h))
+        self.h = h
+        if rc:
+            msg = L.eph_batch_last_error(h).decode() if h else ""
+            raise EphError(rc, msg)
+        self.replicas = []
+        for r, (words, atoms) in enumerate(replicas):
+            x = np.ascontiguousarray(atoms.x, dtype=np.float64)
+            v = np.ascontiguousarray(atoms.v, dtype=np.float64)
+            t = np.ascontiguousarray(atoms.type, dtype=np.int32)
+            m = np.ascontiguousarray(atoms.mask, dtype=np.int32)
+            rc = L.eph_batch_set_atoms(h, r, atoms.n, x.ctypes.data_as(_dp), v.ctypes.data_as(_dp),
+                                       t.ctypes.data_as(_ip), m.ctypes.data_as(_ip))
+            if rc:
+                raise EphError(rc, L.eph_batch_last_error(h).decode())
+            self.replicas.append(_View(L, L.eph_batch_context(h, r), words, atoms.n))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.replicas = []
+            self.L.eph_batch_destroy(self.h)
+            self.h = None
+
+    def step(self, nsteps=1):
+        rc = self.L.eph_batch_step(self.h, nsteps)
+        if rc:
+            raise EphError(rc, self.L.eph_batch_last_error(self.h).decode())
+
+    def synchronize(self):
+        rc = self.L.eph_batch_synchronize(self.h)
+        if rc:
+            raise EphError(rc, self.L.eph_batch_last_error(self.h).decode())
+
+    def launches_per_step(self):
+        out = C.c_long()
+        self.L.eph_batch_launch_count(self.h, C.byref(out))
+        return out.value
 
 
 def grid_cells(words):

@@ -144,3 +144,24 @@ def gaussian_stream(n_in_group: int, seed: int, step: int) -> np.ndarray:
     """Deviates a RanMars-like source would hand the fix in one step: three
     per in-group atom, atom order.  Seeded per (seed, step)."""
     return np.random.default_rng([seed, step]).standard_normal(3 * n_in_group)
+
+
+def batched_cascades(nrep: int = 64, beta_file: str = "synth.beta", seed: int = 2024, min_atoms: int = 32000,
+                     max_atoms: int = 500000):
+    """Independent fcc Ni cascades for the batched form: atom counts drawn
+    log-uniformly in [min_atoms, max_atoms] and rounded to whole fcc cells
+    (4 n^3 atoms, cubic boxes), a PKA of 1-20 keV in a random direction per
+    replica, an FDM grid from 16^3 to 48^3 growing with the box, one seed per
+    replica.  Returns a list of (words, atoms)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(nrep):
+        target = math.exp(rng.uniform(math.log(min_atoms), math.log(max_atoms)))
+        n = int(round((target / 4.0) ** (1.0 / 3.0)))
+        n = max(20, min(50, n))
+        at = fcc_lattice(n, seed=seed + 17 * r)
+        add_pka(at, float(rng.uniform(1000.0, 20000.0)), seed=seed + 31 * r)
+        g = int(round(16 + (n - 20) * 32.0 / 30.0))
+        words = fix_args(beta_file, seed=seed + r + 1, flags=7, model=4, grid=(g, g, g))
+        out.append((words, at))
+    return out
