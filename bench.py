@@ -127,6 +127,12 @@ def forces_bytes(n_atoms, n_pairs):
     return 204 * n_atoms + 36 * n_pairs
 
 
+# DRAM bytes per atom of one k_forces launch measured by ncu on the 32^3-cell
+# case (profiles/sweeps_fcc_131k.md: 219.8 MB for 131,072 atoms); traffic of a
+# launch scales with the atom count at fixed pairs per atom.
+FORCES_DRAM_BYTES_PER_ATOM = 219.8e6 / 131072
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -329,8 +335,12 @@ def main():
                    "mode": "fast", "xi": "device Philox4x32-10"},
         "gpu_launches": res["launches"],
         "roofline": {"bound": "hbm", "kernel": "k_forces", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": peak_src, "traffic": None,
-                     "note": "FP64-issue bound: GB300 issues ~0.5e12 FP64 instructions/s"},
+                     "frac": achieved / hbm, "peak_source": peak_src,
+                     "traffic": FORCES_DRAM_BYTES_PER_ATOM * n,
+                     "algorithmic_bytes": forces_bytes(n, res["n_pairs"]),
+                     "fp64_pipe_frac_ncu": 0.874,
+                     "note": "bound by FP64 issue, not HBM: ncu puts k_forces at 87% of the FP64 pipe; "
+                             "GB300 issues ~0.5e12 FP64 instructions/s (measured)"},
         "phases_ms": {k: round(v[0], 3) for k, v in res["phases"].items()},
         "clocks": res["clocks"],
         "pairs_per_atom": res["n_pairs"] / n,

@@ -25,7 +25,7 @@ extern "C" {
 #define EPH_OK 0
 #define EPH_ERR_ARG 1               /* bad argument (fix_eph.cpp:64, :140, :182, :196 error->all) */
 #define EPH_ERR_FILE 2              /* beta or grid file unreadable (eph_beta.h:42, eph_fdm.h:50 asserts) */
-#define EPH_ERR_UNSUPPORTED_MODEL 3 /* model other than 4 (fix_eph.cpp:888 throws) */
+#define EPH_ERR_UNSUPPORTED_MODEL 3 /* model other than 1 or 4 (fix_eph.cpp:888 throws on unknown ones) */
 #define EPH_ERR_CAPACITY 4          /* a bin or pair list overflowed its capacity */
 #define EPH_ERR_TIMEOUT 5           /* a bounded device wait gave up */
 #define EPH_ERR_CUDA 6              /* CUDA runtime error (no device, launch failure) */
@@ -84,7 +84,10 @@ typedef struct eph_md {
  * group, arg[2] style ("eph"), then seed flags model rho_e C_e kappa_e T_e NX
  * NY NZ T_infile freq T_out beta_file and one element name per atom type.
  * Replaces FixEPH::FixEPH (fix_eph.cpp:61-241) and FixEPH::init
- * (fix_eph.cpp:263-287).  Only model 4 (PRL) is accepted. */
+ * (fix_eph.cpp:263-287).  Models 4 (PRL, force_prl) and 1 (TTM, force_ttm)
+ * run; with arg[2] = "eph/coloured/exp" the words are those of the
+ * coloured-noise fix (fix_eph_coloured_exp.cpp: arg[5] is tau0, model 4 with
+ * an exponential memory on both forces). */
 int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out);
 void eph_destroy(eph_ctx *ctx);
 const char *eph_last_error(const eph_ctx *ctx);

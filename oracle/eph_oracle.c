@@ -585,6 +585,9 @@ enum { F_FRICTION = 0x01, F_RANDOM = 0x02, F_FDM = 0x04, F_NOINT = 0x08, F_NOFRI
 
 struct orc_fix {
   int eph_flag, eph_model, seed, types;
+  int coloured;       /* style eph/coloured/exp: arg[5] is tau0, model 4 */
+  double tau0, zeta;  /* zeta = 1 - exp(-dt/tau0) (fix_eph_coloured_exp.cpp:190) */
+  double *f_dis, *f_sto;
   int type_map[64];
   orc_beta *beta;
   orc_fdm *fdm;
@@ -641,7 +644,13 @@ orc_fix *orc_fix_create(int narg, const char **arg, int ntypes, const double *ma
   f->seed = atoi(arg[3]);
   orc_ranmars_init(&f->rng, f->seed + 0);
   f->eph_flag = (int)strtol(arg[4], NULL, 0);
-  f->eph_model = atoi(arg[5]);
+  f->coloured = strcmp(arg[2], "eph/coloured/exp") == 0;
+  if (f->coloured) {
+    f->tau0 = atof(arg[5]);
+    f->eph_model = 4;
+  } else {
+    f->eph_model = atoi(arg[5]);
+  }
   double v_rho = atof(arg[6]), v_Ce = atof(arg[7]), v_kappa = atof(arg[8]), v_Te = atof(arg[9]);
   int nx = atoi(arg[10]), ny = atoi(arg[11]), nz = atoi(arg[12]);
   for (int k = 0; k < 3; ++k) {
@@ -696,6 +705,7 @@ orc_fix *orc_fix_create(int narg, const char **arg, int ntypes, const double *ma
     }
   }
   f->eta_factor = sqrt(2.0 * boltz / dt);
+  if (f->coloured) f->zeta = 1.0 - exp(-dt / f->tau0);
   f->dt = dt;
   f->dtv = dt;
   f->dtf = 0.5 * dt * ftm2v;
@@ -711,6 +721,7 @@ void orc_fix_free(orc_fix *f) {
   free(f->x); free(f->v); free(f->f); free(f->fext); free(f->type); free(f->mask);
   free(f->rho); free(f->alpha); free(f->f_eph); free(f->f_rng); free(f->w); free(f->xi); free(f->array);
   free(f->numneigh); free(f->neigh); free(f->shift); free(f->xhold);
+  free(f->f_dis); free(f->f_sto);
   free(f);
 }
 
@@ -886,6 +897,8 @@ int orc_fix_set_atoms(orc_fix *f, int n, const double *x, const double *v, const
   REALLOC(f->w, n3, double);
   REALLOC(f->xi, n3, double);
   REALLOC(f->array, 8 * (size_t)n, double);
+  REALLOC(f->f_dis, n3, double);
+  REALLOC(f->f_sto, n3, double);
   free(f->xhold);
   f->xhold = NULL;
 #undef REALLOC
@@ -901,6 +914,8 @@ int orc_fix_set_atoms(orc_fix *f, int n, const double *x, const double *v, const
   memset(f->w, 0, sizeof(double) * n3);
   memset(f->xi, 0, sizeof(double) * n3);
   memset(f->array, 0, sizeof(double) * 8 * (size_t)n);
+  memset(f->f_dis, 0, sizeof(double) * n3);
+  memset(f->f_sto, 0, sizeof(double) * n3);
   free(f->fext);
   f->fext = NULL;
   /* engine setup: wrap, list, force clear */
@@ -1045,6 +1060,13 @@ static void fix_force_prl(orc_fix *f) {
         fe[1] -= dvar * e[1];
         fe[2] -= dvar * e[2];
       }
+      if (f->coloured) { /* fix_eph_coloured_exp.cpp:562-568 */
+        double *fd = f->f_dis + 3 * (size_t)i;
+        for (int k = 0; k < 3; ++k) {
+          fd[k] = fd[k] * (1. - f->zeta) + f->zeta * fe[k];
+          fe[k] = fd[k];
+        }
+      }
     }
   }
   if (f->eph_flag & F_RANDOM) {
@@ -1079,13 +1101,39 @@ static void fix_force_prl(orc_fix *f) {
       fr[0] *= var;
       fr[1] *= var;
       fr[2] *= var;
+      if (f->coloured) { /* fix_eph_coloured_exp.cpp:619-625 */
+        double *fs = f->f_sto + 3 * (size_t)i;
+        for (int k = 0; k < 3; ++k) {
+          fs[k] = fs[k] * (1. - f->zeta) + f->zeta * fr[k];
+          fr[k] = fs[k];
+        }
+      }
     }
   }
 }
 
-/* fix_eph.cpp:841-907 (model 4 only) */
+/* fix_eph.cpp:468-503: model 1, local Langevin with beta(rho_i) */
+static void fix_force_ttm(orc_fix *f) {
+  const int n = f->n;
+  if (f->eph_flag & F_FRICTION)
+    for (int i = 0; i < n; ++i)
+      if (f->mask[i] & f->groupbit) {
+        double var = -orc_beta_get_beta(f->beta, f->type_map[f->type[i] - 1], f->rho[i]);
+        for (int k = 0; k < 3; ++k) f->f_eph[3 * (size_t)i + k] = var * f->v[3 * (size_t)i + k];
+      }
+  if (f->eph_flag & F_RANDOM)
+    for (int i = 0; i < n; ++i)
+      if (f->mask[i] & f->groupbit) {
+        const double *x = f->x + 3 * (size_t)i;
+        double v_Te = orc_fdm_get_T(f->fdm, x[0], x[1], x[2]);
+        double var = f->eta_factor * orc_beta_get_alpha(f->beta, f->type_map[f->type[i] - 1], f->rho[i]) * sqrt(v_Te);
+        for (int k = 0; k < 3; ++k) f->f_rng[3 * (size_t)i + k] = var * f->xi[3 * (size_t)i + k];
+      }
+}
+
+/* fix_eph.cpp:841-907 (models 1 and 4) */
 int orc_fix_post_force(orc_fix *f, const double *xi) {
-  if (f->eph_model != 4) return 3;
+  if (f->eph_model != 4 && f->eph_model != 1) return 3;
   double t0 = now_s();
   const int n = f->n;
   size_t n3 = 3 * (size_t)n;
@@ -1100,7 +1148,10 @@ int orc_fix_post_force(orc_fix *f, const double *xi) {
         for (int k = 0; k < 3; ++k) f->xi[3 * (size_t)i + k] = xi ? xi[m++] : orc_ranmars_gaussian(&f->rng);
   }
   fix_density(f);
-  fix_force_prl(f);
+  if (f->eph_model == 1)
+    fix_force_ttm(f);
+  else
+    fix_force_prl(f);
   if ((f->eph_flag & F_FRICTION) && !(f->eph_flag & F_NOFRICTION))
     for (size_t k = 0; k < n3; ++k) f->f[k] += f->f_eph[k];
   if ((f->eph_flag & F_RANDOM) && !(f->eph_flag & F_NORANDOM))

@@ -26,7 +26,7 @@ class Fix : protected Pointers {
   int groupbit = 1;
   int vector_flag = 0, size_vector = 0, global_freq = 0, extvector = 0;
   int nevery = 1, peratom_flag = 0, size_peratom_cols = 0, peratom_freq = 0;
-  int comm_forward = 0, time_integrate = 0;
+  int comm_forward = 0, time_integrate = 0, maxexchange = 0;
   double **array_atom = nullptr;
 
   virtual void init() {}
@@ -44,6 +44,9 @@ class Fix : protected Pointers {
   virtual void initial_integrate(int) {}
   virtual void final_integrate() {}
   virtual int pack_forward_comm(int, int *, double *, int, int *) { return 0; }
+  virtual int pack_exchange(int, double *) { return 0; }
+  virtual int unpack_exchange(int, double *) { return 0; }
+  virtual void copy_arrays(int, int, int) {}
   virtual void unpack_forward_comm(int, int, double *) {}
 };
 

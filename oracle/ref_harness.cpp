@@ -39,29 +39,47 @@
 #include "engine.hpp"
 
 #include "fix_eph.h"
+#include "fix_eph_coloured_exp.h"
 
 using namespace LAMMPS_NS;
 
 namespace {
 
-// The reference fix with read access to its per-atom arrays.
-class FixEPHProbe : public FixEPH {
+// Read access to the per-atom arrays of a reference fix (`eph` and
+// `eph/coloured/exp` name them alike).
+struct Access {
+  virtual ~Access() = default;
+  virtual double *rho() = 0;
+  virtual double **feph() = 0;
+  virtual double **frng() = 0;
+  virtual double **w() = 0;
+  virtual double **xi() = 0;
+  virtual double **arr() = 0;
+  virtual RanMars *rng() = 0;
+  virtual double T_at(double x, double y, double z) const = 0;
+  virtual void save_T(const char *path, int n) const = 0;
+  virtual void save_state(const char *path) const = 0;
+};
+
+template <class F>
+class Probe : public F, public Access {
  public:
-  FixEPHProbe(LAMMPS *l, int narg, char **arg) : FixEPH(l, narg, arg) {}
-  double *rho() { return rho_i; }
-  double **feph() { return f_EPH; }
-  double **frng() { return f_RNG; }
-  double **w() { return w_i; }
-  double **xi() { return xi_i; }
-  double **arr() { return array; }
-  RanMars *rng() { return random; }
-  double T_at(double x, double y, double z) const { return fdm.get_T(x, y, z); }
-  void save_T(const char *path, int n) const { fdm.save_temperature(path, n); }
-  void save_state(const char *path) const { fdm.save_state(path); }
+  Probe(LAMMPS *l, int narg, char **arg) : F(l, narg, arg) {}
+  double *rho() override { return this->rho_i; }
+  double **feph() override { return this->f_EPH; }
+  double **frng() override { return this->f_RNG; }
+  double **w() override { return this->w_i; }
+  double **xi() override { return this->xi_i; }
+  double **arr() override { return this->array; }
+  RanMars *rng() override { return this->random; }
+  double T_at(double x, double y, double z) const override { return this->fdm.get_T(x, y, z); }
+  void save_T(const char *path, int n) const override { this->fdm.save_temperature(path, n); }
+  void save_state(const char *path) const override { this->fdm.save_state(path); }
 };
 
 struct Sim : Engine {
-  FixEPHProbe *probe() { return static_cast<FixEPHProbe *>(fix); }
+  Access *acc = nullptr;
+  Access *probe() { return acc; }
 };
 
 void copy_err(const char *msg, char *errbuf, int errlen) {
@@ -88,9 +106,18 @@ void *ref_create(int narg, const char **arg, int nlocal, const double *x, const 
     std::vector<std::string> words(arg, arg + narg);
     std::vector<char *> argv;
     for (auto &w : words) argv.push_back(&w[0]);
-    FixEPHProbe *f = new FixEPHProbe(&s->lmp, narg, argv.data());
+    Fix *f;
+    if (narg > 2 && std::string(arg[2]) == "eph/coloured/exp") {
+      auto *p = new Probe<FixEPHColouredExp>(&s->lmp, narg, argv.data());
+      f = p;
+      s->acc = p;
+    } else {
+      auto *p = new Probe<FixEPH>(&s->lmp, narg, argv.data());
+      f = p;
+      s->acc = p;
+    }
     s->fix = f;
-    s->rng = f->rng();
+    s->rng = s->acc->rng();
     f->init();
     if (s->neighbor.nrequest != 1) throw std::runtime_error("fix did not request a neighbour list");
     s->cutneigh = s->neighbor.request.cutoff + skin;

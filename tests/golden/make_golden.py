@@ -30,7 +30,7 @@ from ephgb import workloads as W  # noqa: E402
 from helpers import n_in_group, scenario  # noqa: E402
 from oracle.bindings import RefBeta, RefFix  # noqa: E402
 
-SCEN = {"c1_small": 3, "pka": 4, "two_elements": 2, "group": 2, "c1": 1}
+SCEN = {"c1_small": 3, "pka": 4, "two_elements": 2, "group": 2, "c1": 1, "ttm": 3, "coloured": 3}
 EVERY_STEP = ("x", "v", "f", "rho", "vector", "T", "xi")  # the rest: last step only
 
 

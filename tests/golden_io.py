@@ -6,7 +6,7 @@ import numpy as np
 from ephgb import workloads as W
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FIXTURES = ("c1_small", "pka", "two_elements", "group", "c1")
+FIXTURES = ("c1_small", "pka", "two_elements", "group", "c1", "ttm", "coloured")
 
 
 def load_fix(name, tmpdir):

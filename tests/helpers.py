@@ -68,6 +68,15 @@ def scenario(name, beta_file, beta_file_2el=None):
         at.type = np.where(np.arange(at.n) % 4 == 1, 2, 1).astype(np.int32)
         at.mass = np.array([0.0, W.NI_MASS, 55.845])
         return W.fix_args(beta_file_2el, grid=(5, 5, 5), elements=("Ni", "Fe")), at, 0.001
+    if name == "ttm":  # model 1: local Langevin with beta(rho_i)
+        at = W.fcc_lattice(5, seed=23)
+        at.mask = np.where(np.arange(at.n) % 5 == 0, 2, 1).astype(np.int32)
+        return W.fix_args(beta_file, model=1, grid=(5, 5, 5)), at, 0.001
+    if name == "coloured":  # fix eph/coloured/exp, tau0 = 5 fs
+        at = W.fcc_lattice(5, seed=24)
+        words = W.fix_args(beta_file, grid=(5, 5, 5))
+        words[2], words[5] = "eph/coloured/exp", "0.005"
+        return words, at, 0.001
     if name == "uneven_box":
         at = W.fcc_lattice((5, 4, 6), seed=22)
         return W.fix_args(beta_file, grid=(7, 3, 4)), at, 0.001
@@ -75,4 +84,4 @@ def scenario(name, beta_file, beta_file_2el=None):
 
 
 SCENARIOS = ["c1_small", "friction_only", "fric_rand_nofdm", "random_only_fdm", "noapply", "noint", "group", "pka",
-             "hot_electrons", "two_elements", "uneven_box"]
+             "hot_electrons", "two_elements", "uneven_box", "ttm", "coloured"]

@@ -67,6 +67,7 @@ struct eph_ctx {
 
   int n = 0;
   DevBuf<D4> x, v, f, xhold, f_eph, f_rng, xi, fext, A, Bw;
+  DevBuf<D4> f_dis, f_sto;  // coloured-noise memory (eph/coloured/exp)
   bool have_fext = false, have_xi = false;
   DevBuf<int> type, mask, nshort, cell, tmap;
   DevBuf<double> rho, beta_i, Te_i, stage;
@@ -182,6 +183,7 @@ void set_time_params(eph_ctx *c) {
   c->grid.dt = c->dt;  // EPH_FDM::set_dt
   c->nsub = c->grid.substeps(&c->inner_dt);
   c->P.prescale = c->grid.dV * c->dt;
+  if (c->args.coloured) c->P.zeta = 1.0 - std::exp(-c->dt / c->args.tau0);  // fix_eph_coloured_exp.cpp:190, :685
 }
 
 // read back the device error word; returns EPH_OK or the matching status
@@ -292,7 +294,23 @@ template <bool FAST, bool MULTI, bool FRIC, bool RAND>
 void launch_forces_t(eph_ctx *c) {
   k_forces<FAST, MULTI, FRIC, RAND><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
       c->P, c->mask.p, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->Te_i.p, c->f.p, c->f_eph.p,
-      c->f_rng.p);
+      c->f_rng.p, c->f_dis.p, c->f_sto.p);
+}
+
+template <bool FAST, bool FRIC, bool RAND>
+void launch_ttm_t(eph_ctx *c) {
+  k_forces_ttm<FAST, FRIC, RAND><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+      c->P, c->mask.p, c->x.p, c->v.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->Te_i.p, c->f.p, c->f_eph.p,
+      c->f_rng.p, c->d_err.p);
+}
+
+template <bool FAST>
+void launch_ttm(eph_ctx *c) {
+  const bool fr = c->P.flags & FLAG_FRICTION, ra = c->P.flags & FLAG_RANDOM;
+  if (fr && ra) launch_ttm_t<FAST, true, true>(c);
+  else if (fr) launch_ttm_t<FAST, true, false>(c);
+  else if (ra) launch_ttm_t<FAST, false, true>(c);
+  else launch_ttm_t<FAST, false, false>(c);
 }
 
 template <bool FAST, bool MULTI>
@@ -327,6 +345,14 @@ int launch_post_force(eph_ctx *c, int xi_mode) {
       if (c->multi) launch_density_t<false, true>(c, xi_mode);
       else launch_density_t<false, false>(c, xi_mode);
     }
+  }
+  if (c->args.model == 1) {  // force_ttm: per-atom, no pair sums
+    PhaseScope ps(c, EPH_PHASE_FORCES);
+    ps.launched();
+    if (fast) launch_ttm<true>(c);
+    else launch_ttm<false>(c);
+    CUDA_TRY(c, cudaGetLastError());
+    return EPH_OK;
   }
   if (c->P.flags & FLAG_FRICTION) {
     PhaseScope ps(c, EPH_PHASE_FRICTION_W);
@@ -495,8 +521,8 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
     return fail(c, r, why);
   }
   *out = c;
-  if (c->args.model != 4)
-    return fail(c, EPH_ERR_UNSUPPORTED_MODEL, "only model 4 (PRL 120, 185501) runs on the GPU path");
+  if (c->args.model != 4 && c->args.model != 1)
+    return fail(c, EPH_ERR_UNSUPPORTED_MODEL, "models 1 (TTM) and 4 (PRL 120, 185501) run on the GPU path");
   if (md->ntypes < 1 || md->ntypes > 64 || !md->mass) return fail(c, EPH_ERR_ARG, "ntypes must be 1..64 with masses");
   if (!(md->dt > 0)) return fail(c, EPH_ERR_ARG, "dt must be positive");
   c->ntypes = md->ntypes;
@@ -594,6 +620,7 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
   P.gdy = g.dy;
   P.gdz = g.dz;
   P.seed = (unsigned)c->args.seed;
+  P.coloured = c->args.coloured ? 1 : 0;
   P.step = c->step_ctr.p;
   set_time_params(c);
   // bins: edge >= rc (1 + 5e-5), at least 3 per axis
@@ -652,8 +679,13 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
   if (n != c->n) {  // (re)allocate the per-atom storage
     c->n = n;
     c->P.n = n;
-    for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw})
+    for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw, &c->f_dis,
+                          &c->f_sto})
       CUDA_TRY(c, b->alloc(N));
+    // the coloured-noise memory starts at zero (fix_eph_coloured_exp.cpp:229-230) and
+    // follows the atom index afterwards
+    CUDA_TRY(c, cudaMemsetAsync(c->f_dis.p, 0, sizeof(D4) * N, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->f_sto.p, 0, sizeof(D4) * N, c->stream));
     CUDA_TRY(c, c->type.alloc(N));
     CUDA_TRY(c, c->mask.alloc(N));
     CUDA_TRY(c, c->nshort.alloc(N));

@@ -285,9 +285,18 @@ int parse_fix_args(int narg, const char *const *arg, FixArgs *a, std::string *wh
     *why = "Illegal fix eph command: too few arguments";
     return EPH_ERR_ARG;
   }
+  a->style = arg[2];
+  // the coloured-noise fix (fix_eph_coloured_exp.cpp:113) reads tau0 where
+  // the plain fix reads the model, and always runs the PRL model
+  a->coloured = a->style.find("coloured/exp") != std::string::npos;
   a->seed = std::atoi(arg[3]);
   a->flags = (int)std::strtol(arg[4], nullptr, 0);
-  a->model = std::atoi(arg[5]);
+  if (a->coloured) {
+    a->tau0 = std::atof(arg[5]);
+    a->model = 4;
+  } else {
+    a->model = std::atoi(arg[5]);
+  }
   a->rho_e = std::atof(arg[6]);
   a->C_e = std::atof(arg[7]);
   a->kappa_e = std::atof(arg[8]);

@@ -70,6 +70,9 @@ struct Grid {
 // Parsed `fix ID group eph seed flags model rho_e C_e kappa_e T_e NX NY NZ
 // T_infile freq T_out beta_file A B ...` (fix_eph.cpp:36-58, :61-241).
 struct FixArgs {
+  std::string style;        // arg[2]: "eph", or "eph/coloured/exp" (arg[5] is then tau0)
+  bool coloured = false;
+  double tau0 = 0;
   int seed = 0, flags = 0, model = 0;
   double rho_e = 0, C_e = 0, kappa_e = 0, T_e = 0;
   int nx = 0, ny = 0, nz = 0;

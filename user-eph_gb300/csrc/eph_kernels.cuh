@@ -77,6 +77,10 @@ struct StepParams {
   long gnx, gny, gnz, ncells;
   double gx0, gy0, gz0, gdx, gdy, gdz;
   double prescale;  // dV * dt (eph_fdm.h:176)
+  // coloured noise (fix_eph_coloured_exp.cpp:190): exponential memory on
+  // f_EPH and f_RNG, zeta = 1 - exp(-dt / tau0)
+  int coloured;
+  double zeta;
   // random numbers: Philox key = seed, counter = (atom, *step) with *step the
   // number of post_force calls so far, kept on the device so a captured
   // step replays with fresh numbers
@@ -639,12 +643,14 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
                                                 const double2 *__restrict__ pg, const int *__restrict__ nshort,
                                                 const D4 *__restrict__ A, const D4 *__restrict__ Bw,
                                                 const double *__restrict__ Te_i, D4 *__restrict__ f,
-                                                D4 *__restrict__ f_eph, D4 *__restrict__ f_rng) {
+                                                D4 *__restrict__ f_eph, D4 *__restrict__ f_rng,
+                                                D4 *__restrict__ f_dis, D4 *__restrict__ f_sto) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   double fex = 0.0, fey = 0.0, fez = 0.0, frx = 0.0, fry = 0.0, frz = 0.0;
   const D4 Ai = A[i];
-  if ((mask[i] & P.groupbit) && pos_double(Ai.x)) {
+  const bool live = (mask[i] & P.groupbit) && pos_double(Ai.x);
+  if (live) {
     const D4 Bi = Bw[i];
     const double xix = Ai.z, xiy = Ai.w, xiz = Bi.x;
     const int ns = nshort[i];
@@ -705,6 +711,28 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
       frz *= var;
     }
   }
+  if (P.coloured && live) {  // fix_eph_coloured_exp.cpp:562-568, :619-625
+    if (FRIC) {
+      D4 d = f_dis[i];
+      d.x = d.x * (1. - P.zeta) + P.zeta * fex;
+      d.y = d.y * (1. - P.zeta) + P.zeta * fey;
+      d.z = d.z * (1. - P.zeta) + P.zeta * fez;
+      f_dis[i] = d;
+      fex = d.x;
+      fey = d.y;
+      fez = d.z;
+    }
+    if (RAND) {
+      D4 d = f_sto[i];
+      d.x = d.x * (1. - P.zeta) + P.zeta * frx;
+      d.y = d.y * (1. - P.zeta) + P.zeta * fry;
+      d.z = d.z * (1. - P.zeta) + P.zeta * frz;
+      f_sto[i] = d;
+      frx = d.x;
+      fry = d.y;
+      frz = d.z;
+    }
+  }
   f_eph[i] = D4{fex, fey, fez, 0.0};
   f_rng[i] = D4{frx, fry, frz, 0.0};
   D4 fi = f[i];
@@ -717,6 +745,53 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
     fi.x += frx;
     fi.y += fry;
     fi.z += frz;
+  }
+  f[i] = fi;
+}
+
+// --------------------------------------------------------- model 1 (TTM)
+
+// force_ttm (fix_eph.cpp:468-503): a local Langevin thermostat with the
+// site's beta(rho_i): f_EPH = -beta v_i, f_RNG = eta alpha(rho_i) sqrt(T_e) xi_i;
+// then the force update of post_force (:892-906).
+template <bool FAST, bool FRIC, bool RAND>
+__global__ void k_forces_ttm(StepParams P, const int *__restrict__ mask, const D4 *__restrict__ x,
+                             const D4 *__restrict__ v,
+                             const D4 *__restrict__ A, const D4 *__restrict__ Bw, const double *__restrict__ rho,
+                             const double *__restrict__ beta, const double *__restrict__ Te_i, D4 *__restrict__ f,
+                             D4 *__restrict__ f_eph, D4 *__restrict__ f_rng, unsigned *__restrict__ err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  D4 fe = D4{0.0, 0.0, 0.0, 0.0}, fr = D4{0.0, 0.0, 0.0, 0.0};
+  if (mask[i] & P.groupbit) {
+    if (FRIC) {
+      const double var = -beta[i];
+      const D4 vi = v[i];
+      fe = D4{var * vi.x, var * vi.y, var * vi.z, 0.0};
+    }
+    if (RAND) {
+      const double r = rho[i];
+      double alpha = 0.0;
+      if (!(r > P.rho_cutoff)) {  // eph_beta.h:188-197
+        const int e = (int)x[i].w;
+        alpha = spline_eval<FAST>(P.tab_alpha + (size_t)e * P.n_beta, P.inv_drho, P.n_beta, r, err);
+      }
+      const double var = P.eta * alpha * sqrt(Te_i[i]);
+      fr = D4{var * A[i].z, var * A[i].w, var * Bw[i].x, 0.0};
+    }
+  }
+  f_eph[i] = fe;
+  f_rng[i] = fr;
+  D4 fi = f[i];
+  if (FRIC && !(P.flags & 0x10)) {
+    fi.x += fe.x;
+    fi.y += fe.y;
+    fi.z += fe.z;
+  }
+  if (RAND && !(P.flags & 0x20)) {
+    fi.x += fr.x;
+    fi.y += fr.y;
+    fi.z += fr.z;
   }
   f[i] = fi;
 }

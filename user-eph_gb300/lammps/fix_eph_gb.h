@@ -2,7 +2,8 @@
  * LAMMPS fix `eph/gb`: the USER-EPH fix `eph` (fix_eph.h, FixStyle(eph,FixEPH))
  * with its per-step work on one GB300 through the C ABI of eph_gb.h.
  *
- * Same command words as `fix eph` (README.md:186-214):
+ * Same command words as `fix eph` (README.md:186-214) -- or, as
+ * `eph/coloured/exp/gb`, those of `fix eph/coloured/exp` (arg[5] = tau0):
  *   fix ID group eph/gb seed flags model rho_e C_e kappa_e T_e NX NY NZ
  *       T_infile freq T_out beta_file A B ...
  * Same hooks (INITIAL_INTEGRATE, POST_FORCE, FINAL_INTEGRATE, END_OF_STEP),
@@ -20,6 +21,7 @@
 #ifdef FIX_CLASS
 // clang-format off
 FixStyle(eph/gb,FixEPHGB)
+FixStyle(eph/coloured/exp/gb,FixEPHGB)
 // clang-format on
 #else
 
