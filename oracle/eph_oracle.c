@@ -246,7 +246,17 @@ static inline double beta_rho_r_sq(const orc_beta *b, int elem, double r_sq) {
 
 enum { FDM_CONSTANT = 0, FDM_DYNAMIC = 1, FDM_ZERO_DERIVATIVE = 2 };
 
+/* eph_linear.h: piecewise-linear table with reverse lookup */
+typedef struct {
+  double dx;
+  long n;
+  double *y, *dy; /* dy[n-1] = 0: the reference reads one past its slopes there */
+} orc_linear;
+
 struct orc_fdm {
+  int has_tdyn;
+  orc_spline C_T, K_T;
+  orc_linear E_T;
   long nx, ny, nz, ntotal;
   double x0, x1, y0, y1, z0, z1, dx, dy, dz, dV;
   double *T, *dT, *ddT, *C, *rho, *kappa, *S;
@@ -326,7 +336,38 @@ orc_fdm *orc_fdm_load(const char *path) {
   if (fscanf(fd, "%lf %lf %lf %lf %lf %lf", &b[0], &b[1], &b[2], &b[3], &b[4], &b[5]) != 6) goto fail;
   fdm_set_box(g, b[0], b[1], b[2], b[3], b[4], b[5]);
   if (fscanf(fd, "%1023s", g->parameter_filename) != 1) goto fail;
-  if (strcmp(g->parameter_filename, "NULL") != 0) goto fail; /* temperature-dependent C_e(T): not restated */
+  if (strcmp(g->parameter_filename, "NULL") != 0) {
+    /* eph_fdm.h:73-104: C_e(T), kappa_e(T) splines and E_e(T) = sum C_e dT */
+    FILE *pf = fopen(g->parameter_filename, "r");
+    if (!pf) goto fail;
+    char ln[1024];
+    long n = 0;
+    double dT = 0;
+    int ok = 1;
+    for (int k = 0; k < 3 && ok; ++k) ok = fgets(ln, sizeof ln, pf) && ln[0] == '#';
+    if (ok) ok = fscanf(pf, "%ld %lf", &n, &dT) == 2 && n > 4;
+    double *c = ok ? (double *)malloc(sizeof(double) * (size_t)n) : NULL;
+    double *kk = ok ? (double *)malloc(sizeof(double) * (size_t)n) : NULL;
+    for (long i = 0; ok && i < n; ++i) ok = fscanf(pf, "%lf %lf", &c[i], &kk[i]) == 2;
+    fclose(pf);
+    if (ok) {
+      orc_spline_build(&g->C_T, dT, c, n);
+      orc_spline_build(&g->K_T, dT, kk, n);
+      c[0] = 0.;
+      for (long i = 1; i < n; ++i) c[i] = c[i - 1] + c[i] * dT;
+      g->E_T.dx = dT;
+      g->E_T.n = n;
+      g->E_T.y = c;
+      g->E_T.dy = (double *)calloc((size_t)n, sizeof(double));
+      for (long i = 0; i < n - 1; ++i) g->E_T.dy[i] = (c[i + 1] - c[i]) / dT;
+      g->has_tdyn = 1;
+      free(kk);
+    } else {
+      free(c);
+      free(kk);
+      goto fail;
+    }
+  }
   for (long c = 0; c < g->ntotal; ++c) {
     int lx, ly, lz, fl, td;
     double T, S, rho, Ce, kap;
@@ -353,6 +394,12 @@ fail:
 
 void orc_fdm_free(orc_fdm *g) {
   if (!g) return;
+  if (g->has_tdyn) {
+    orc_spline_free(&g->C_T);
+    orc_spline_free(&g->K_T);
+    free(g->E_T.y);
+    free(g->E_T.dy);
+  }
   free(g->T); free(g->dT); free(g->ddT); free(g->C); free(g->rho); free(g->kappa); free(g->S);
   free(g->flag); free(g->Tdyn);
   free(g);
@@ -396,9 +443,42 @@ double orc_fdm_get_T_total(const orc_fdm *g) {
   return result;
 }
 
-/* eph_fdm.h:267-400, constant C_e and kappa_e (T_dynamic_flag 0) */
+/* eph_linear.h:41-48 */
+static double linear_eval(const orc_linear *l, double x) {
+  size_t idx = (size_t)(x / l->dx);
+  if (idx < (size_t)l->n) {
+    double delta = x - idx * l->dx;
+    return l->y[idx] + l->dy[idx] * delta;
+  }
+  return 0.;
+}
+
+/* eph_linear.h:51-60 (first knot above v) */
+static double linear_reverse(const orc_linear *l, double v) {
+  size_t lo = 0, hi = (size_t)l->n;
+  while (lo < hi) {
+    size_t mid = (lo + hi) / 2;
+    if (!(v < l->y[mid]))
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  if (lo != (size_t)l->n && lo > 0) {
+    size_t idx = lo - 1;
+    return idx * l->dx + 1. / l->dy[idx] * (v - l->y[idx]);
+  }
+  return 0.;
+}
+
+/* eph_fdm.h:267-400 */
 unsigned orc_fdm_solve(orc_fdm *g) {
   const size_t nx = (size_t)g->nx, ny = (size_t)g->ny, nz = (size_t)g->nz, ntotal = (size_t)g->ntotal;
+  if (g->has_tdyn) /* eph_fdm.h:280-287 */
+    for (size_t i = 0; i < ntotal; ++i)
+      if (g->Tdyn[i]) {
+        g->C[i] = orc_spline_eval(&g->C_T, g->T[i]);
+        g->kappa[i] = orc_spline_eval(&g->K_T, g->T[i]);
+      }
   double inner_dt = g->dt / (double)(size_t)g->steps;
   double dtdxdydz = inner_dt * (1.0 / g->dx / g->dx + 1.0 / g->dy / g->dy + 1.0 / g->dz / g->dz);
   double c_min = g->C[0], rho_min = g->rho[0], kappa_max = g->kappa[0];
@@ -451,7 +531,15 @@ unsigned orc_fdm_solve(orc_fdm *g) {
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < (long)ntotal; i++) {
       double prescaler = g->rho[i] * g->C[i];
-      if (fl[i] == FDM_DYNAMIC) T[i] += (ddT[i] + g->dT[i] + g->S[i]) / prescaler * inner_dt;
+      if (fl[i] == FDM_DYNAMIC) {
+        if (g->Tdyn[i] == 1) { /* eph_fdm.h:378-382 */
+          double E_e = linear_eval(&g->E_T, T[i]);
+          E_e += (ddT[i] + g->dT[i] + g->S[i]) / g->rho[i] * inner_dt;
+          T[i] = linear_reverse(&g->E_T, E_e);
+        } else {
+          T[i] += (ddT[i] + g->dT[i] + g->S[i]) / prescaler * inner_dt;
+        }
+      }
       if (T[i] < 0.0) T[i] = 0.0;
     }
   }

@@ -100,3 +100,28 @@ def test_hook_sequence_matches_step(built, beta_file):
         for k in ATOM_KEYS:
             assert np.array_equal(a.get(k), b.get(k)), (s, k)
         assert np.array_equal(a.get("T"), b.get("T"))
+
+
+@pytest.mark.parametrize("mode", [ephgb.MODE_EXACT, ephgb.MODE_FAST])
+def test_tdyn_grid(built, beta_file, tmp_path, mode):
+    """A grid file with temperature-dependent cells (C_e(T), kappa_e(T),
+    E_e(T) inverse update): the device grid solve against the oracle."""
+    pf = W.write_grid_parameters(str(tmp_path / "params.data"))
+    gf = W.write_grid_file(str(tmp_path / "Tdyn.in"), parameter_file=pf, tdyn=True, T=2000.0)
+    at = W.fcc_lattice(5, seed=61)
+    words = W.fix_args(beta_file, T_infile=gf, grid=(1, 1, 1))
+
+    def check(s, gpu, ref):
+        for k in ATOM_KEYS:
+            if mode == ephgb.MODE_EXACT and s == 0:
+                assert np.array_equal(gpu.get(k), ref.get(k)), k
+            else:
+                assert rel_err(gpu.get(k), ref.get(k)) <= TOL, (s, k)
+        assert rel_err(gpu.get("T"), ref.get("T")) <= TOL, s
+
+    run_pair(words, at, 0.001, mode, 10, check)
+    gpu = ephgb.FixEPH(words, at, dt=0.001, mode=mode)
+    gpu.step(3)
+    gpu.save_state(str(tmp_path / "after.restart"))  # C_e, kappa_e follow T in the written state
+    text = open(tmp_path / "after.restart").read().splitlines()
+    assert text[7].endswith("params.data") and len(text) == 8 + 8 * 6 * 5

@@ -83,6 +83,12 @@ struct eph_ctx {
   DevBuf<D4> tab_rho_r_sq, tab_beta, tab_alpha;
 
   DevBuf<double> T0, T1, kappa, rhoC, S, dT;
+  // temperature-dependent cells: per-cell C_e and rho_e, the parameter tables
+  DevBuf<double> gC, grho, E_y, E_dy, bounds;
+  DevBuf<D4> C_T, K_T;
+  DevBuf<unsigned char> tdyn;
+  TdynTables td{};
+  double *h_bounds = nullptr;  // pinned
   DevBuf<signed char> gflag;
   DevBuf<U128> acc, part, gsum;
   unsigned nsub = 1;
@@ -170,6 +176,31 @@ int upload_grid(eph_ctx *c) {
   CUDA_TRY(c, cudaMemcpy(c->gflag.p, fl.data(), nc, cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemset(c->dT.p, 0, nc * 8));
   CUDA_TRY(c, cudaMemset(c->acc.p, 0, nc * sizeof(U128)));
+  c->td = TdynTables{};
+  bool any = false;
+  for (size_t i = 0; i < nc; ++i) any = any || g.T_dynamic[i];
+  if (g.has_tdyn && any) {
+    const size_t nt = (size_t)g.E_T.y.size();
+    std::vector<unsigned char> td(nc);
+    for (size_t i = 0; i < nc; ++i) td[i] = (unsigned char)std::min<unsigned>(g.T_dynamic[i], 255u);
+    CUDA_TRY(c, c->tdyn.alloc(nc));
+    CUDA_TRY(c, c->gC.alloc(nc));
+    CUDA_TRY(c, c->grho.alloc(nc));
+    CUDA_TRY(c, c->E_y.alloc(nt));
+    CUDA_TRY(c, c->E_dy.alloc(nt));
+    CUDA_TRY(c, c->C_T.alloc(nt));
+    CUDA_TRY(c, c->K_T.alloc(nt));
+    CUDA_TRY(c, c->bounds.alloc(4));
+    CUDA_TRY(c, cudaMemcpy(c->tdyn.p, td.data(), nc, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->gC.p, g.C.data(), nc * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->grho.p, g.rho.data(), nc * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->E_y.p, g.E_T.y.data(), nt * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->E_dy.p, g.E_T.dy.data(), nt * 8, cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->C_T.p, g.C_T.c.data(), nt * sizeof(D4), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->K_T.p, g.kappa_T.c.data(), nt * sizeof(D4), cudaMemcpyHostToDevice));
+    if (!c->h_bounds) CUDA_TRY(c, cudaMallocHost(&c->h_bounds, 4 * sizeof(double)));
+    c->td = TdynTables{c->tdyn.p, c->C_T.p, c->K_T.p, c->E_y.p, c->E_dy.p, c->grho.p, g.E_T.dx, g.C_T.inv_dx, (int)nt};
+  }
   return EPH_OK;
 }
 
@@ -405,14 +436,28 @@ int launch_end_of_step(eph_ctx *c) {
   }
   if (gr) {
     PhaseScope ps(c, EPH_PHASE_FDM);
-    ps.launched((int)c->nsub);
     const Grid &g = c->grid;
+    if (c->td.tdyn) {
+      // eph_fdm.h:280-313: T-dependent C_e, kappa_e, then this step's substeps
+      k_fdm_tdyn_params<<<nblocks(g.ntotal, 128), 128, 0, c->stream>>>(g.ntotal, c->td, c->T0.p, c->gC.p,
+                                                                       c->kappa.p, c->rhoC.p, c->d_err.p);
+      k_fdm_bounds<<<1, 256, 0, c->stream>>>(g.ntotal, c->gC.p, c->grho.p, c->kappa.p, c->gflag.p, c->bounds.p);
+      CUDA_TRY(c, cudaMemcpyAsync(c->h_bounds, c->bounds.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      c->nsub = g.substeps_from(c->h_bounds[0], c->h_bounds[1], c->h_bounds[2], &c->inner_dt);
+      ps.launched(2);
+    }
+    ps.launched((int)c->nsub);
     double *src = c->T0.p, *dst = c->T1.p;
     for (unsigned s = 0; s < c->nsub; ++s) {
-      k_fdm_substep<<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt,
-                                                                 src, dst, c->kappa.p, c->rhoC.p, c->S.p,
-                                                                 c->gflag.p, c->dT.p, c->acc.p, s == 0,
-                                                                 c->counters.p);
+      if (c->mode == EPH_MODE_FAST)
+        k_fdm_substep<true><<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(
+            g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt, src, dst, c->kappa.p, c->rhoC.p, c->S.p, c->gflag.p,
+            c->dT.p, c->acc.p, s == 0, c->counters.p, c->td);
+      else
+        k_fdm_substep<false><<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(
+            g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt, src, dst, c->kappa.p, c->rhoC.p, c->S.p, c->gflag.p,
+            c->dT.p, c->acc.p, s == 0, c->counters.p, c->td);
       std::swap(src, dst);
     }
     if (src != c->T0.p)
@@ -426,6 +471,12 @@ int launch_end_of_step(eph_ctx *c) {
 int download_grid(eph_ctx *c) {
   CUDA_TRY(c, cudaMemcpyAsync(c->grid.T.data(), c->T0.p, sizeof(double) * (size_t)c->grid.ntotal,
                               cudaMemcpyDeviceToHost, c->stream));
+  if (c->td.tdyn) {  // C_e and kappa_e follow T in these cells
+    CUDA_TRY(c, cudaMemcpyAsync(c->grid.C.data(), c->gC.p, sizeof(double) * (size_t)c->grid.ntotal,
+                                cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->grid.kappa.data(), c->kappa.p, sizeof(double) * (size_t)c->grid.ntotal,
+                                cudaMemcpyDeviceToHost, c->stream));
+  }
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return EPH_OK;
 }
@@ -645,6 +696,7 @@ void eph_destroy(eph_ctx *c) {
   for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->h_bounds) cudaFreeHost(c->h_bounds);
   delete c;
 }
 
@@ -855,7 +907,8 @@ int eph_step(eph_ctx *c, int nsteps, int xi_source) {
   if (xi_source == EPH_XI_GIVEN && !c->have_xi && (c->P.flags & FLAG_RANDOM))
     return fail(c, EPH_ERR_STATE, "EPH_XI_GIVEN without eph_put(EPH_FIELD_XI)");
   const int xi_mode = xi_source == EPH_XI_GIVEN ? 1 : 0;
-  const bool graph = c->use_graph && !c->profiling;
+  // a T-dependent grid decides its substep count on the host every step
+  const bool graph = c->use_graph && !c->profiling && !c->td.tdyn;
   if (graph && (!c->gexec || c->graph_xi != xi_mode) && (r = capture_step(c, xi_mode))) return r;
   for (int s = 0; s < nsteps; ++s) {
     c->ntimestep += 1;
@@ -1080,6 +1133,10 @@ static int batch_capture(eph_batch *b) {
   for (eph_ctx *c : b->reps) {
     if (c->n <= 0) {
       b->err = "a replica has no atoms";
+      return EPH_ERR_STATE;
+    }
+    if (c->td.tdyn) {
+      b->err = "replicas with temperature-dependent grid cells cannot be captured (substeps decided per step)";
       return EPH_ERR_STATE;
     }
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return EPH_ERR_CUDA;

@@ -142,6 +142,40 @@ std::string Beta::load(const char *path) {
   return "";
 }
 
+void Linear::build(double in_dx, const std::vector<double> &in_y) {
+  dx = in_dx;
+  y = in_y;
+  dy.assign(y.size(), 0.0);
+  for (size_t i = 0; i + 1 < y.size(); ++i) dy[i] = (y[i + 1] - y[i]) / dx;
+  // dy has one entry per interval in the reference; at idx = n-1 it reads one
+  // past its end (eph_linear.h:44-45) -- a zero slope there here
+}
+
+double Linear::operator()(double x) const {
+  const size_t idx = (size_t)(x / dx);
+  if (idx < y.size()) {
+    const double delta = x - idx * dx;
+    return y[idx] + dy[idx] * delta;
+  }
+  return 0.;
+}
+
+double Linear::reverse_lookup(double v) const {
+  size_t lo = 0, hi = y.size();  // first element > v (std::upper_bound)
+  while (lo < hi) {
+    const size_t mid = (lo + hi) / 2;
+    if (!(v < y[mid]))
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  if (lo != y.size() && lo > 0) {
+    const size_t idx = lo - 1;
+    return idx * dx + 1. / dy[idx] * (v - y[idx]);
+  }
+  return 0.;
+}
+
 const Spline &Beta::table(int which, int elem) const {
   switch (which) {
     case EPH_SPLINE_RHO_R: return rho[elem];
@@ -191,8 +225,10 @@ std::string Grid::load(const char *path) {
   for (double &v : b)
     if (!(fd >> v)) return "grid file: bad box lines";
   if (!(fd >> parameter_filename)) return "grid file: missing parameter-file line";
-  if (parameter_filename != "NULL")
-    return "grid file: temperature-dependent parameter files (C_e(T), kappa(T)) are not supported";
+  if (parameter_filename != "NULL") {
+    std::string e = load_parameters(parameter_filename.c_str());
+    if (!e.empty()) return e;
+  }
   T.assign(ntotal, 0.0);
   S.assign(ntotal, 0.0);
   rho.assign(ntotal, 0.0);
@@ -208,7 +244,7 @@ std::string Grid::load(const char *path) {
     if (!(fd >> lx >> ly >> lz >> t >> s >> r >> ce >> k >> fl >> td)) return "grid file: too few cell lines";
     const long index = lx + ly * nx + lz * nx * ny;
     if (lx < 0 || ly < 0 || lz < 0 || index >= ntotal) return "grid file: cell index outside the grid";
-    if (td != 0) return "grid file: temperature-dependent cells are not supported";
+    if (td != 0 && !has_tdyn) return "grid file: temperature-dependent cells need a parameter file";
     T[index] = t;
     S[index] = s;
     rho[index] = r;
@@ -221,9 +257,30 @@ std::string Grid::load(const char *path) {
   return "";
 }
 
+std::string Grid::load_parameters(const char *path) {
+  // eph_fdm.h:73-104: three comment lines, "n dT", then n lines "C_e kappa_e"
+  std::ifstream fd(path);
+  if (!fd) return std::string("cannot open grid parameter file ") + path;
+  std::string line;
+  for (int k = 0; k < 3; ++k)
+    if (!std::getline(fd, line) || line.empty() || line[0] != '#')
+      return "grid parameter file: three '#' comment lines expected";
+  size_t n;
+  double dT;
+  if (!(fd >> n >> dT) || n < 5 || !(dT > 0)) return "grid parameter file: bad size line";
+  std::vector<double> c(n), k(n);
+  for (size_t i = 0; i < n; ++i)
+    if (!(fd >> c[i] >> k[i])) return "grid parameter file: too few lines";
+  C_T.build(dT, c);
+  kappa_T.build(dT, k);
+  c[0] = 0.;
+  for (size_t i = 1; i < c.size(); ++i) c[i] = c[i - 1] + c[i] * dT;
+  E_T.build(dT, c);
+  has_tdyn = true;
+  return "";
+}
+
 unsigned Grid::substeps(double *inner_dt_out) const {
-  double inner_dt = dt / (double)(size_t)steps;
-  const double dtdxdydz = inner_dt * (1.0 / dx / dx + 1.0 / dy / dy + 1.0 / dz / dz);
   double c_min = C[0], rho_min = rho[0], kappa_max = kappa[0];
   for (long i = 1; i < ntotal; ++i)
     if (flag[i] != GRID_CONSTANT) {
@@ -231,6 +288,12 @@ unsigned Grid::substeps(double *inner_dt_out) const {
       if (rho[i] < rho_min) rho_min = rho[i];
       if (kappa[i] > kappa_max) kappa_max = kappa[i];
     }
+  return substeps_from(c_min, rho_min, kappa_max, inner_dt_out);
+}
+
+unsigned Grid::substeps_from(double c_min, double rho_min, double kappa_max, double *inner_dt_out) const {
+  double inner_dt = dt / (double)(size_t)steps;
+  const double dtdxdydz = inner_dt * (1.0 / dx / dx + 1.0 / dy / dy + 1.0 / dz / dz);
   const double r = dtdxdydz / c_min / rho_min * kappa_max;
   unsigned new_steps = (unsigned)steps;
   if (r > 0.4) {

@@ -44,6 +44,16 @@ struct Beta {
 
 enum : int { GRID_CONSTANT = 0, GRID_DYNAMIC = 1, GRID_ZERO_DERIVATIVE = 2 };
 
+// Piecewise-linear table with a reverse lookup (eph_linear.h:21-75), used for
+// the electronic energy E_e(T) = integral of C_e(T) dT.
+struct Linear {
+  double dx = 1;
+  std::vector<double> y, dy;  // dy[i] = (y[i+1] - y[i]) / dx; dy[n-1] = 0
+  void build(double dx, const std::vector<double> &y);
+  double operator()(double x) const;        // eph_linear.h:41-48
+  double reverse_lookup(double v) const;    // eph_linear.h:51-60
+};
+
 // Electronic grid of eph_fdm.h: uniform (constructor :28-46) or read from a
 // grid file (:48-119); index i + j nx + k nx ny.
 struct Grid {
@@ -55,6 +65,14 @@ struct Grid {
   std::string parameter_filename = "NULL";
   long steps = 1;
   double dt = 1;
+  // temperature-dependent cells (T_dynamic != 0): C_e(T), kappa_e(T) splines
+  // and E_e(T), read from the parameter file (eph_fdm.h:73-104)
+  bool has_tdyn = false;
+  Spline C_T, kappa_T;
+  Linear E_T;
+  std::string load_parameters(const char *path);
+  // substeps from given bounds (c_min, rho_min, kappa_max over the grid)
+  unsigned substeps_from(double c_min, double rho_min, double kappa_max, double *inner_dt) const;
 
   void create(long nx, long ny, long nz, double x0, double x1, double y0, double y1, double z0, double z1,
               double T_e, double C_e, double rho_e, double kappa_e);

@@ -868,17 +868,99 @@ __global__ void k_energy_total(const U128 *__restrict__ part, int nparts, double
 
 // ------------------------------------------------------------- FDM solve
 
+// Temperature-dependent cells (T_dynamic): tables of the grid parameter file.
+struct TdynTables {
+  const unsigned char *tdyn;  // per cell, nonzero: C_e(T), kappa_e(T), E_e(T) apply
+  const D4 *C_T, *K_T;        // splines of C_e and kappa_e over T (eph_fdm.h:94-95)
+  const double *E_y, *E_dy;   // E_e(T) = integral of C_e dT, piecewise linear (eph_fdm.h:97-103)
+  const double *rho;          // rho_e per cell
+  double dT, inv_dT;
+  int n;
+};
+
+// eph_linear.h:41-48
+__device__ __forceinline__ double linear_eval(const TdynTables &t, double x) {
+  const unsigned long long idx = trunc_index(x / t.dT);
+  if (idx < (unsigned long long)t.n) {
+    const double delta = x - (double)idx * t.dT;
+    return t.E_y[idx] + t.E_dy[idx] * delta;
+  }
+  return 0.;
+}
+
+// eph_linear.h:51-60: first knot above v (upper bound), linear inverse
+__device__ __forceinline__ double linear_reverse(const TdynTables &t, double v) {
+  int lo = 0, hi = t.n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (!(v < t.E_y[mid]))
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  if (lo != t.n && lo > 0) {
+    const int idx = lo - 1;
+    return (double)idx * t.dT + 1. / t.E_dy[idx] * (v - t.E_y[idx]);
+  }
+  return 0.;
+}
+
+// eph_fdm.h:280-287: C_e and kappa_e of the T-dependent cells from T, before
+// the stability test; the prescaler rho_e C_e follows.
+__global__ void k_fdm_tdyn_params(long ncells, TdynTables t, const double *__restrict__ T, double *__restrict__ C,
+                                  double *__restrict__ kappa, double *__restrict__ rhoC, unsigned *__restrict__ err) {
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= ncells || !t.tdyn[r]) return;
+  const double c = spline_eval<false>(t.C_T, t.inv_dT, t.n, T[r], err);
+  C[r] = c;
+  kappa[r] = spline_eval<false>(t.K_T, t.inv_dT, t.n, T[r], err);
+  rhoC[r] = t.rho[r] * c;
+}
+
+// c_min, rho_min, kappa_max of the stability rule (eph_fdm.h:290-300): cell 0
+// whatever its flag, then every cell that is not CONSTANT_VALUE.  One block.
+__global__ void k_fdm_bounds(long ncells, const double *__restrict__ C, const double *__restrict__ rho,
+                             const double *__restrict__ kappa, const signed char *__restrict__ flag,
+                             double *__restrict__ out) {
+  double c_min = C[0], r_min = rho[0], k_max = kappa[0];
+  for (long i = 1 + threadIdx.x; i < ncells; i += blockDim.x)
+    if (flag[i] != 0) {
+      c_min = fmin(c_min, C[i]);
+      r_min = fmin(r_min, rho[i]);
+      k_max = fmax(k_max, kappa[i]);
+    }
+  __shared__ double s[3][256];
+  s[0][threadIdx.x] = c_min;
+  s[1][threadIdx.x] = r_min;
+  s[2][threadIdx.x] = k_max;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      s[0][threadIdx.x] = fmin(s[0][threadIdx.x], s[0][threadIdx.x + h]);
+      s[1][threadIdx.x] = fmin(s[1][threadIdx.x], s[1][threadIdx.x + h]);
+      s[2][threadIdx.x] = fmax(s[2][threadIdx.x], s[2][threadIdx.x + h]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = s[0][0];
+    out[1] = s[1][0];
+    out[2] = s[2][0];
+  }
+}
+
 // One substep of EPH_FDM::solve (eph_fdm.h:315-396) with the reference's
 // expression order: the variable-kappa 7-point stencil with periodic wrap and
 // ZERO_DERIVATIVE walls, then T += (ddT + dT + S)/(rho_e C_e) dt' on DYNAMIC
 // cells and the clamp at T = 0.  Reads T_in, writes T_out.  The first
 // substep turns the fixed-point deposits into dT and clears them.
+template <bool FAST>
 __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, double dz, double inner_dt,
                               const double *__restrict__ T, double *__restrict__ Tout,
                               const double *__restrict__ kappa, const double *__restrict__ rhoC,
                               const double *__restrict__ S, const signed char *__restrict__ flag,
                               double *__restrict__ dT, U128 *__restrict__ acc, int first,
-                              unsigned long long *__restrict__ counters) {
+                              unsigned long long *__restrict__ counters, TdynTables td) {
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long ntotal = nx * ny * nz;
   if (r >= ntotal) return;
@@ -895,27 +977,39 @@ __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, d
   double ddT = 0.0;
   if (flag[r] != 2) {
     long p, q;
-    p = (i > 0) ? r - 1 : r + (nx - 1);
-    q = (i < nx - 1) ? r + 1 : r - (nx - 1);
-    if (flag[q] == 2) q = r;
-    else if (flag[p] == 2) p = r;
-    ddT += (kappa[q] - kappa[p]) * (T[q] - T[p]) / dx / dx / 4.0;
-    ddT += kappa[r] * ((T[q] + T[p] - 2.0 * T[r]) / dx / dx);
-    p = (j > 0) ? r - nx : r + (ny - 1) * nx;
-    q = (j < ny - 1) ? r + nx : r - (ny - 1) * nx;
-    if (flag[q] == 2) q = r;
-    else if (flag[p] == 2) p = r;
-    ddT += (kappa[q] - kappa[p]) * (T[q] - T[p]) / dy / dy / 4.0;
-    ddT += kappa[r] * ((T[q] + T[p] - 2.0 * T[r]) / dy / dy);
-    p = (k > 0) ? r - nx * ny : r + (nz - 1) * nx * ny;
-    q = (k < nz - 1) ? r + nx * ny : r - (nz - 1) * nx * ny;
-    if (flag[q] == 2) q = r;
-    else if (flag[p] == 2) p = r;
-    ddT += (kappa[q] - kappa[p]) * (T[q] - T[p]) / dz / dz / 4.0;
-    ddT += kappa[r] * ((T[q] + T[p] - 2.0 * T[r]) / dz / dz);
+    const long pr[3] = {(i > 0) ? r - 1 : r + (nx - 1), (j > 0) ? r - nx : r + (ny - 1) * nx,
+                        (k > 0) ? r - nx * ny : r + (nz - 1) * nx * ny};
+    const long qr[3] = {(i < nx - 1) ? r + 1 : r - (nx - 1), (j < ny - 1) ? r + nx : r - (ny - 1) * nx,
+                        (k < nz - 1) ? r + nx * ny : r - (nz - 1) * nx * ny};
+    const double h[3] = {dx, dy, dz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      p = pr[a];
+      q = qr[a];
+      if (flag[q] == 2) q = r;
+      else if (flag[p] == 2) p = r;
+      if (FAST) {  // reciprocals instead of the reference's divisions (within 1e-15 of them)
+        const double ih2 = 1.0 / (h[a] * h[a]);
+        ddT = fma((kappa[q] - kappa[p]) * (T[q] - T[p]), 0.25 * ih2, ddT);
+        ddT = fma(kappa[r] * ih2, T[q] + T[p] - 2.0 * T[r], ddT);
+      } else {
+        ddT += (kappa[q] - kappa[p]) * (T[q] - T[p]) / h[a] / h[a] / 4.0;
+        ddT += kappa[r] * ((T[q] + T[p] - 2.0 * T[r]) / h[a] / h[a]);
+      }
+    }
   }
   double t = T[r];
-  if (flag[r] == 1) t += (ddT + dTr + S[r]) / rhoC[r] * inner_dt;
+  if (FAST && flag[r] == 1 && !(td.tdyn && td.tdyn[r] == 1)) {
+    t = fma((ddT + dTr + S[r]) * inner_dt, 1.0 / rhoC[r], t);
+  } else if (flag[r] == 1) {
+    if (td.tdyn && td.tdyn[r] == 1) {  // eph_fdm.h:378-382: through E_e(T)
+      double E = linear_eval(td, t);
+      E += (ddT + dTr + S[r]) / td.rho[r] * inner_dt;
+      t = linear_reverse(td, E);
+    } else {
+      t += (ddT + dTr + S[r]) / rhoC[r] * inner_dt;
+    }
+  }
   if (t < 0.0) {
     t = 0.0;
     atomicAdd(&counters[CNT_T_CLAMP], 1ull);

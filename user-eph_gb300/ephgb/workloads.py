@@ -165,3 +165,50 @@ def batched_cascades(nrep: int = 64, beta_file: str = "synth.beta", seed: int = 
         words = fix_args(beta_file, seed=seed + r + 1, flags=7, model=4, grid=(g, g, g))
         out.append((words, at))
     return out
+
+
+def write_grid_file(path, n=(8, 6, 5), box=((0.0, 17.6), (0.0, 17.6), (0.0, 17.6)), T=300.0, C_e=3.5e-6,
+                    rho_e=1.0, kappa_e=0.1, parameter_file=None, seed=0, walls=True, tdyn=False):
+    """A grid file in the reference format (Doc/FDM/T_input.fdm, read by
+    eph_fdm.h:48-119): three comment lines, "nx ny nz steps", three box lines,
+    the parameter-file name (or NULL), then one line per cell
+    "i j k T S rho_e C_e kappa_e flag T_dynamic".  With walls, the x = 0
+    plane is ZERO_DERIVATIVE and one y-z line is CONSTANT; tdyn marks the
+    DYNAMIC cells temperature dependent.  Values carry the file's %.6e
+    precision; returns the path."""
+    rng = np.random.default_rng(seed)
+    with open(path, "w") as f:
+        f.write("# grid\n#\n#\n")
+        f.write(f"{n[0]} {n[1]} {n[2]} 1\n")
+        for lo, hi in box:
+            f.write(f"{lo:.6e} {hi:.6e}\n")
+        f.write((parameter_file or "NULL") + "\n")
+        for k in range(n[2]):
+            for j in range(n[1]):
+                for i in range(n[0]):
+                    fl = 1
+                    if walls and i == 0:
+                        fl = 2
+                    elif walls and j == 0 and k == 0:
+                        fl = 0
+                    t = T * rng.uniform(0.8, 1.6)
+                    s = rng.uniform(-1e-3, 1e-3) if fl == 1 and i == 2 else 0.0
+                    td = 1 if (tdyn and fl == 1) else 0
+                    f.write(f"{i} {j} {k} {t:.6e} {s:.6e} {rho_e:.6e} {C_e * rng.uniform(0.8, 1.2):.6e} "
+                            f"{kappa_e * rng.uniform(0.8, 1.2):.6e} {fl} {td}\n")
+    return path
+
+
+def write_grid_parameters(path, n=1001, dT=10.0, C0=3.5e-6, T0=3000.0, kappa0=0.1):
+    """A grid parameter file (eph_fdm.h:73-104): three comment lines, "n dT",
+    then C_e(T) and kappa_e(T) on T = 0, dT, ...: C_e = C0 (1 + T/T0),
+    kappa_e = kappa0 (1 + T/T0) / (1 + (T/T0)^2)."""
+    T = np.arange(n) * dT
+    C = C0 * (1.0 + T / T0)
+    K = kappa0 * (1.0 + T / T0) / (1.0 + (T / T0) ** 2)
+    with open(path, "w") as f:
+        f.write("#\n#\n#\n")
+        f.write(f"{n} {dT!r}\n")
+        for c, k in zip(C, K):
+            f.write(f"{c:.6e} {k:.6e}\n")
+    return path
