@@ -14,125 +14,20 @@
 #include <string>
 #include <vector>
 
-#include "eph_gb.h"
-#include "eph_host.hpp"
+#include "eph_ctx_impl.hpp"
 #include "eph_kernels.cuh"
 
 using namespace ephgb;
 
-namespace {
 
-template <typename T>
-struct DevBuf {
-  T *p = nullptr;
-  size_t n = 0;
-  cudaError_t alloc(size_t count) {
-    free();
-    n = count;
-    if (count == 0) return cudaSuccess;
-    return cudaMalloc(&p, sizeof(T) * count);
-  }
-  void free() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  ~DevBuf() { free(); }
-};
-
-constexpr int BLOCK = 128;
-inline int nblocks(long n, int b = BLOCK) { return (int)((n + b - 1) / b); }
-
-}  // namespace
-
-struct eph_ctx {
-  std::string err;
-  int device = 0;
-  cudaStream_t stream = 0;
-  bool own_stream = false;
-
-  FixArgs args;
-  Beta beta;
-  Grid grid;  // host copy: geometry and parameters (T lives on the device)
-  int ntypes = 0;
-  std::vector<double> mass;
-  std::vector<int> type_map;  // by LAMMPS type 1..ntypes
-  double boxlo[3], boxhi[3], prd[3];
-  double dt = 0, boltz = 0, ftm2v = 0, skin = 0;
-  int groupbit = 1, mode = EPH_MODE_FAST;
-  long ntimestep = 0;
-
-  StepParams P{};
-  bool multi = false;
-
-  int n = 0;
-  DevBuf<D4> x, v, f, xhold, f_eph, f_rng, xi, fext, A, Bw;
-  DevBuf<D4> f_dis, f_sto;  // coloured-noise memory (eph/coloured/exp)
-  bool have_fext = false, have_xi = false;
-  DevBuf<int> type, mask, nshort, cell, tmap;
-  DevBuf<double> rho, beta_i, Te_i, stage;
-  DevBuf<int> bin_count;
-  DevBuf<BinEntry> bins;
-  DevBuf<int4> atom_bin;
-  DevBuf<float4> atom_off;
-  DevBuf<unsigned> pj;
-  DevBuf<D4> pe;
-  DevBuf<double2> pg;
-  int nbins = 0, bcap = 0, kcap = 0;
-
-  DevBuf<D4> tab_rho_r_sq, tab_beta, tab_alpha;
-
-  DevBuf<double> T0, T1, kappa, rhoC, S, dT;
-  // temperature-dependent cells: per-cell C_e and rho_e, the parameter tables
-  DevBuf<double> gC, grho, E_y, E_dy, bounds;
-  DevBuf<D4> C_T, K_T;
-  DevBuf<unsigned char> tdyn;
-  TdynTables td{};
-  double *h_bounds = nullptr;  // pinned
-  DevBuf<signed char> gflag;
-  DevBuf<U128> acc, part, gsum;
-  unsigned nsub = 1;
-  double inner_dt = 0;
-
-  // per-phase CUDA-event timing (eph_set_profiling) and launch counts
-  bool profiling = false;
-  struct Mark {
-    int phase;
-    cudaEvent_t a, b;
-  };
-  std::vector<Mark> marks;
-  std::vector<cudaEvent_t> event_pool;
-  double phase_ms[EPH_NPHASES] = {0};
-  long phase_launches[EPH_NPHASES] = {0};
-  long launches = 0;
-
-  // one captured engine step replayed by eph_step (eph_set_graph)
-  bool use_graph = false;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  int graph_xi = -1;
-  long graph_launches = 0;  // kernels in one replay
-
-  DevBuf<double> scal;  // 0 Ee, 1 E_local, 2 T_total
-  DevBuf<unsigned> d_err;
-  DevBuf<unsigned long long> counters;
-  DevBuf<int> wrapflag;
-  DevBuf<unsigned long long> step_ctr;  // post_force calls so far (the Philox counter)
-  unsigned *h_err = nullptr;  // pinned
-};
-
-namespace {
+namespace ephgb {
+namespace ctxi {
 
 int fail(eph_ctx *c, int code, const std::string &msg) {
   if (c) c->err = msg;
   return code;
 }
 
-#define CUDA_TRY(ctx, call)                                                                           \
-  do {                                                                                                \
-    cudaError_t e_ = (call);                                                                          \
-    if (e_ != cudaSuccess) return fail((ctx), EPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
 
 int upload_tables(eph_ctx *c) {
   const Beta &b = c->beta;
@@ -450,6 +345,7 @@ int launch_end_of_step(eph_ctx *c) {
     ps.launched((int)c->nsub);
     double *src = c->T0.p, *dst = c->T1.p;
     for (unsigned s = 0; s < c->nsub; ++s) {
+      if (c->fdm_rec) dst = c->fdm_rec + (size_t)s * (size_t)g.ntotal;
       if (c->mode == EPH_MODE_FAST)
         k_fdm_substep<true><<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(
             g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt, src, dst, c->kappa.p, c->rhoC.p, c->S.p, c->gflag.p,
@@ -458,7 +354,8 @@ int launch_end_of_step(eph_ctx *c) {
         k_fdm_substep<false><<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(
             g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt, src, dst, c->kappa.p, c->rhoC.p, c->S.p, c->gflag.p,
             c->dT.p, c->acc.p, s == 0, c->counters.p, c->td);
-      std::swap(src, dst);
+      if (c->fdm_rec) src = dst;
+      else std::swap(src, dst);
     }
     if (src != c->T0.p)
       CUDA_TRY(c, cudaMemcpyAsync(c->T0.p, src, sizeof(double) * (size_t)g.ntotal, cudaMemcpyDeviceToDevice,
@@ -537,7 +434,10 @@ int capture_step(eph_ctx *c, int xi_mode) {
   return EPH_OK;
 }
 
-}  // namespace
+}  // namespace ctxi
+}  // namespace ephgb
+
+using namespace ephgb::ctxi;
 
 // =================================================================== C ABI
 

@@ -1,0 +1,145 @@
+// Internal: the context of one fix instance and the launch sequence of one
+// engine step, shared by eph_ctx.cu (the plain path and the C ABI) and
+// eph_adjoint.cu (the reverse-mode gradient).  Not part of the public ABI.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "eph_gb.h"
+#include "eph_device.cuh"
+#include "eph_host.hpp"
+
+namespace ephgb {
+
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, sizeof(T) * count);
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DevBuf() { free(); }
+};
+
+constexpr int BLOCK = 128;
+inline int nblocks(long n, int b = BLOCK) { return (int)((n + b - 1) / b); }
+
+}  // namespace ephgb
+
+using namespace ephgb;
+
+struct eph_ctx {
+  std::string err;
+  int device = 0;
+  cudaStream_t stream = 0;
+  bool own_stream = false;
+
+  FixArgs args;
+  Beta beta;
+  Grid grid;  // host copy: geometry and parameters (T lives on the device)
+  int ntypes = 0;
+  std::vector<double> mass;
+  std::vector<int> type_map;  // by LAMMPS type 1..ntypes
+  double boxlo[3], boxhi[3], prd[3];
+  double dt = 0, boltz = 0, ftm2v = 0, skin = 0;
+  int groupbit = 1, mode = EPH_MODE_FAST;
+  long ntimestep = 0;
+
+  StepParams P{};
+  bool multi = false;
+
+  int n = 0;
+  DevBuf<D4> x, v, f, xhold, f_eph, f_rng, xi, fext, A, Bw;
+  DevBuf<D4> f_dis, f_sto;  // coloured-noise memory (eph/coloured/exp)
+  bool have_fext = false, have_xi = false;
+  DevBuf<int> type, mask, nshort, cell, tmap;
+  DevBuf<double> rho, beta_i, Te_i, stage;
+  DevBuf<int> bin_count;
+  DevBuf<BinEntry> bins;
+  DevBuf<int4> atom_bin;
+  DevBuf<float4> atom_off;
+  DevBuf<unsigned> pj;
+  DevBuf<D4> pe;
+  DevBuf<double2> pg;
+  int nbins = 0, bcap = 0, kcap = 0;
+
+  DevBuf<D4> tab_rho_r_sq, tab_beta, tab_alpha;
+
+  DevBuf<double> T0, T1, kappa, rhoC, S, dT;
+  // temperature-dependent cells: per-cell C_e and rho_e, the parameter tables
+  DevBuf<double> gC, grho, E_y, E_dy, bounds;
+  DevBuf<D4> C_T, K_T;
+  DevBuf<unsigned char> tdyn;
+  TdynTables td{};
+  double *h_bounds = nullptr;  // pinned
+  DevBuf<signed char> gflag;
+  DevBuf<U128> acc, part, gsum;
+  unsigned nsub = 1;
+  double inner_dt = 0;
+  // set by the adjoint while it records a step: substep k of the grid solve
+  // writes its output to fdm_rec + k * ncells instead of the ping-pong buffer
+  double *fdm_rec = nullptr;
+
+  // per-phase CUDA-event timing (eph_set_profiling) and launch counts
+  bool profiling = false;
+  struct Mark {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> event_pool;
+  double phase_ms[EPH_NPHASES] = {0};
+  long phase_launches[EPH_NPHASES] = {0};
+  long launches = 0;
+
+  // one captured engine step replayed by eph_step (eph_set_graph)
+  bool use_graph = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_xi = -1;
+  long graph_launches = 0;  // kernels in one replay
+
+  DevBuf<double> scal;  // 0 Ee, 1 E_local, 2 T_total
+  DevBuf<unsigned> d_err;
+  DevBuf<unsigned long long> counters;
+  DevBuf<int> wrapflag;
+  DevBuf<unsigned long long> step_ctr;  // post_force calls so far (the Philox counter)
+  unsigned *h_err = nullptr;  // pinned
+};
+
+namespace ephgb {
+namespace ctxi {
+
+int fail(eph_ctx *c, int code, const std::string &msg);
+int check_device(eph_ctx *c);
+int require_atoms(eph_ctx *c);
+int upload_tables(eph_ctx *c);
+int upload_grid(eph_ctx *c);
+void set_time_params(eph_ctx *c);
+void drop_graph(eph_ctx *c);
+// the four phases of one engine step on the context's stream
+int launch_initial(eph_ctx *c, int check_wrap);
+int launch_post_force(eph_ctx *c, int xi_mode);
+int launch_final(eph_ctx *c);
+int launch_end_of_step(eph_ctx *c);
+
+}  // namespace ctxi
+}  // namespace ephgb
+
+#define CUDA_TRY(ctx, call)                                                                           \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess) return ephgb::ctxi::fail((ctx), EPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
