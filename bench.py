@@ -252,6 +252,111 @@ def run_batched(args, dev):
                 "timing": "host wall clock around the graph launches, synchronised"}
 
 
+ADJ_CELLS, ADJ_GRID, ADJ_STEPS, ADJ_K, ADJ_DT = 20, (16, 16, 16), 200, 20, 0.001
+
+
+def run_adjoint(args, dev):
+    """The adjoint workload: fcc Ni 20^3 cells (32,000 atoms), ions at 300 K,
+    electrons at 2,000 K on a 16^3 grid, 200 steps of 1 fs, flags 7.  The beta
+    file has 16 rho(r) knots and 64 beta(rho) knots.  Loss = sum_t (E[t] -
+    E*[t])^2, E[t] the ion-to-electron energy of step t and E* the curve the
+    plain method gives with a hidden beta(rho) (the start knots times
+    1 + 0.3 sin(k/6)).  Gradient with respect to the 64 beta knots, the 16
+    rho(r) knots, C_e and kappa_e, checkpoints every 20 steps; checked against
+    central finite differences (h = 1e-6 relative) of the same forward.  Both
+    passes and the plain method run as CUDA-graph replays."""
+    import torch
+
+    import ephgb
+    from ephgb import workloads as W
+    from ephgb.adjoint import Adjoint
+
+    with tempfile.TemporaryDirectory() as wd:
+        # beta(rho) with curvature over the table: the table construction's slope
+        # weights are ill-conditioned where knots lie nearly on a line, and a
+        # 1e-6 relative finite difference would measure that instead of the gradient
+        bf = W.write_beta_file(os.path.join(wd, "adj.beta"), n_rho=16, n_beta=64, drho=0.005,
+                               beta_fn=lambda r: 0.02 + 2.0 * r * r)
+        atoms = W.fcc_lattice(ADJ_CELLS, seed=SEED + 7)
+        words = W.fix_args(bf, seed=SEED, flags=7, T_e=2000.0, grid=ADJ_GRID)
+        fix = ephgb.FixEPH(words, atoms, dt=ADJ_DT, mode=ephgb.MODE_FAST, device=dev)
+        adj = Adjoint(fix, checkpoint_every=ADJ_K)
+        r0, b0 = (c.copy() for c in adj.columns[0])
+        hidden = b0 * (1.0 + 0.3 * np.sin(np.arange(b0.size) / 6.0))
+        adj.set_knots(0, r0, hidden)
+        target, _ = adj.forward(ADJ_STEPS)
+        adj.set_knots(0, r0, b0)
+
+        def loss(r, b, C_e, kappa_e):
+            adj.set_knots(0, r, b)
+            adj.set_grid_constants(C_e, kappa_e)
+            E, _ = adj.forward(ADJ_STEPS)
+            return float(((E - target) ** 2).sum())
+
+        for _ in range(2):  # warm-up
+            E, _ = adj.forward(ADJ_STEPS)
+            adj.backward(2.0 * (E - target), None)
+        E, _ = adj.forward(ADJ_STEPS)
+        L0 = float(((E - target) ** 2).sum())
+        adj.backward(2.0 * (E - target), None)
+        t = adj.timing()
+        g = adj.gradients(0)
+        # the plain method on the same system: eph_step, CUDA events on its stream
+        plain = ephgb.FixEPH(words, atoms, dt=ADJ_DT, mode=ephgb.MODE_FAST, device=dev)
+        stream = torch.cuda.Stream()  # a graph cannot be captured on the legacy default stream
+        plain.set_stream(stream.cuda_stream)
+        plain.set_graph(True)
+        plain.step(10)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plain.step(ADJ_STEPS)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = e0.elapsed_time(e1)
+        # central finite differences of the loss, h = 1e-6 relative
+        h = 1e-6
+        fd = {"rho_knots": np.zeros(r0.size), "beta_knots": np.zeros(b0.size)}
+        C0, K0 = adj.C_e, adj.kappa_e
+        floor = np.abs(r0[r0 != 0]).min()  # a zero knot moves by 1e-6 of the smallest non-zero one
+        for k in range(r0.size):
+            d = h * max(abs(r0[k]), floor)
+            p, m = r0.copy(), r0.copy()
+            p[k] += d
+            m[k] -= d
+            fd["rho_knots"][k] = (loss(p, b0, C0, K0) - loss(m, b0, C0, K0)) / (2 * d)
+        for k in range(b0.size):
+            d = h * abs(b0[k])
+            p, m = b0.copy(), b0.copy()
+            p[k] += d
+            m[k] -= d
+            fd["beta_knots"][k] = (loss(r0, p, C0, K0) - loss(r0, m, C0, K0)) / (2 * d)
+        fd["C_e"] = (loss(r0, b0, C0 * (1 + h), K0) - loss(r0, b0, C0 * (1 - h), K0)) / (2 * h * C0)
+        fd["kappa_e"] = (loss(r0, b0, C0, K0 * (1 + h)) - loss(r0, b0, C0, K0 * (1 - h))) / (2 * h * K0)
+        loss(r0, b0, C0, K0)
+        # each difference's rounding noise: 2 eps L / (2 step)
+        eps = 2.0 ** -52 * L0
+        steps_h = {"rho_knots": h * np.maximum(np.abs(r0), floor), "beta_knots": h * np.abs(b0),
+                   "C_e": h * C0, "kappa_e": h * K0}
+        err, err_above_noise = {}, {}
+        for k in ("rho_knots", "beta_knots", "C_e", "kappa_e"):
+            d = np.abs(np.asarray(g[k]) - fd[k])
+            err[k] = float(np.max(d) / np.abs(fd[k]).max())
+            err_above_noise[k] = float(np.max(np.maximum(d - 10.0 * eps / steps_h[k], 0.0)) / np.abs(fd[k]).max())
+        return {"workload": "fcc Ni 20^3 cells (32,000 atoms), ions 300 K, T_e 2,000 K, FDM 16^3, 200 steps of 1 fs, "
+                            "flags 7; 64 beta knots (beta = 0.02 + 2 rho^2), 16 rho(r) knots, C_e, kappa_e; "
+                            "checkpoints every 20 steps",
+                "loss": "sum_t (E[t] - E*[t])^2, E* from a hidden beta(rho)", "loss_value": L0,
+                "forward_ms": t["forward_ms"], "backward_ms": t["backward_ms"], "plain_forward_ms": plain_ms,
+                "adjoint_over_forward": t["backward_ms"] / t["forward_ms"],
+                "forward_plus_adjoint_over_plain_forward": (t["forward_ms"] + t["backward_ms"]) / plain_ms,
+                "forward_launches": t["forward_launches"], "backward_launches": t["backward_launches"],
+                "grad_rel_err_vs_fd": err, "grad_rel_err_max": max(err.values()),
+                "grad_rel_err_above_fd_noise": err_above_noise, "fd_h_relative": h,
+                "params": int(r0.size + b0.size + 2),
+                "timing": "CUDA events on the fix's stream; backward includes the recomputation from checkpoints"}
+
+
 def cpu_baseline(threads, steps=1, warm=1):
     """The CPU restatement (oracle port) on the same workload: `steps` steps
     of the full system after `warm` warm-up steps; time of the fix's own hooks
@@ -285,6 +390,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="omit the end-to-end leg")
     ap.add_argument("--no-batched", action="store_true", help="omit the batched-replicas leg")
     ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--no-adjoint", action="store_true", help="omit the adjoint leg")
     ap.add_argument("--cells", type=int, default=CELLS, help="fcc cells per edge (profiling cases)")
     ap.add_argument("--grid", type=int, default=GRID[0], help="FDM cells per edge (profiling cases)")
     args = ap.parse_args()
@@ -355,6 +461,8 @@ def main():
             t = torch.tensor([line["batched"]["value"]], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
             line["batched"]["value"] = float(t.item())
+    if rank == 0 and not args.no_adjoint:
+        line["adjoint"] = run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)))
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(threads, steps=1, warm=1).items() if k != "seconds"}
     if rank == 0:

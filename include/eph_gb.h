@@ -225,6 +225,18 @@ double eph_beta_eval(const eph_beta *b, int which, int elem, double x);
  * returns the number of knots */
 long eph_beta_table(const eph_beta *b, int which, int elem, double *out);
 
+/* Replace element elem's knot columns (the file's rho(r) and beta(rho)
+ * columns, n_rho and n_beta values) and rebuild its tables as the reader does
+ * (eph_beta.h:103-124).  No reference counterpart: lets a fitting loop change
+ * the parametrisation without writing files. */
+int eph_beta_set_knots(eph_beta *b, int elem, const double *rho_knots, long n_rho, const double *beta_knots,
+                       long n_beta);
+/* Chain rule through the table construction of element elem: from dL/d(table
+ * coefficients) of the rho(r^2) table (n_rho x 4) and of the alpha table
+ * (n_beta x 4) to dL/d(knot columns): g_rho (n_rho), g_beta (n_beta). */
+int eph_beta_knot_gradient(const eph_beta *b, int elem, const double *g_rho_r_sq, const double *g_alpha,
+                           double *g_rho, double *g_beta);
+
 /* Host-side grid (no GPU needed): uniform grid or grid file
  * (eph_fdm.h:28-119), stability substeps (eph_fdm.h:275-313), writers. */
 typedef struct eph_grid eph_grid;
@@ -237,6 +249,55 @@ long eph_grid_ncells(const eph_grid *g);
 unsigned eph_grid_substeps(const eph_grid *g, double dt, double *inner_dt);
 int eph_grid_save_state(const eph_grid *g, const char *path);
 int eph_grid_save_temperature(const eph_grid *g, const char *path, int n);
+
+/* ---------------------------------------------------------------- adjoint
+ * Reverse-mode gradients of a trajectory loss through the whole fix step
+ * (force_prl model 4: density, friction pre-vector, friction and random
+ * forces, integrator, deposition, grid solve).  No reference counterpart:
+ * the reference computes no derivatives.
+ *
+ * Parameters a fitting loop changes between trajectories: */
+/* element elem's knot columns on a context (see eph_beta_set_knots) */
+int eph_set_beta_knots(eph_ctx *ctx, int elem, const double *rho_knots, long n_rho, const double *beta_knots,
+                       long n_beta);
+/* C_e and kappa_e of every cell of a grid made from the fix's words
+ * (T_infile NULL); the substep count follows (eph_fdm.h:275-313). */
+int eph_set_grid_constants(eph_ctx *ctx, double C_e, double kappa_e);
+
+/* An adjoint object records the context's state at creation (positions,
+ * velocities, forces, T_e grid, random-number counter): every trajectory it
+ * runs starts there.  Deviates come from the device generator (EPH_XI_DEVICE_RNG),
+ * so a trajectory is a fixed function of the parameters (pathwise gradients).
+ * The backward pass recomputes each segment of checkpoint_every steps from a
+ * checkpoint taken by the forward pass and records that segment's
+ * intermediates on the device.  Supported: model 4, fix eph (not the
+ * coloured form), grids without temperature-dependent cells. */
+typedef struct eph_adjoint eph_adjoint;
+int eph_adjoint_create(eph_ctx *ctx, int checkpoint_every, eph_adjoint **out);
+void eph_adjoint_destroy(eph_adjoint *adj);
+const char *eph_adjoint_last_error(const eph_adjoint *adj);
+/* Run nsteps engine steps from the recorded start.  E[t] = energy the ions
+ * gave the electrons in step t (the reference's E_local, fix_eph.cpp:364-404),
+ * T_mean[t] = mean T_e of the grid after step t (get_T_total, eph_fdm.h:189-196);
+ * either pointer may be NULL.  The context is left at the last step. */
+int eph_adjoint_forward(eph_adjoint *adj, long nsteps, double *E, double *T_mean);
+/* Reverse sweep over the last forward trajectory for L with dL/dE[t] and
+ * dL/dT_mean[t] (host arrays of nsteps values; NULL means zero). */
+int eph_adjoint_backward(eph_adjoint *adj, const double *dL_dE, const double *dL_dT_mean);
+/* Gradient of L after eph_adjoint_backward: */
+#define EPH_GRAD_RHO_KNOTS 0  /* element elem's rho(r) knot column, n_rho values */
+#define EPH_GRAD_BETA_KNOTS 1 /* element elem's beta(rho) knot column, n_beta values */
+#define EPH_GRAD_C_E 2        /* 1 value: every cell's C_e changed together */
+#define EPH_GRAD_KAPPA 3      /* 1 value: every cell's kappa_e changed together */
+int eph_adjoint_gradient(eph_adjoint *adj, int which, int elem, double *out, long n);
+/* on (the default): each pass is captured once as a CUDA graph and replayed
+ * while the number of steps, the step constants and the buffers stay; off:
+ * every kernel is launched from the host */
+int eph_adjoint_set_graph(eph_adjoint *adj, int on);
+/* milliseconds of the last forward and backward passes (CUDA events on the
+ * context's stream) and the kernels each launched; any pointer may be NULL */
+int eph_adjoint_timing(eph_adjoint *adj, double *forward_ms, double *backward_ms, long *forward_launches,
+                       long *backward_launches);
 
 #ifdef __cplusplus
 }

@@ -37,8 +37,11 @@ int upload_tables(eph_ctx *c) {
       const Spline &s = b.table(which, e);
       std::memcpy(&h[(size_t)e * nk * 4], s.c.data(), sizeof(double) * 4 * nk);
     }
-    cudaError_t r = dst.alloc((size_t)b.n_elements * nk);
-    if (r != cudaSuccess) return r;
+    if (dst.n != (size_t)b.n_elements * nk) {  // same size: keep the buffer (captured graphs hold its address)
+      c->buf_gen += 1;
+      cudaError_t r = dst.alloc((size_t)b.n_elements * nk);
+      if (r != cudaSuccess) return r;
+    }
     return cudaMemcpy(dst.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
   };
   CUDA_TRY(c, up(c->tab_rho_r_sq, EPH_SPLINE_RHO_R_SQ, b.n_rho));
@@ -604,6 +607,7 @@ int eph_set_capacity(eph_ctx *c, int bin_capacity, int pair_capacity) {
   if (!c) return EPH_ERR_ARG;
   drop_graph(c);
   if (pair_capacity > KMAX) return fail(c, EPH_ERR_ARG, "pair capacity above the compiled maximum");
+  c->buf_gen += 1;
   if (bin_capacity > 0) c->bcap = bin_capacity;
   if (pair_capacity > 0) c->kcap = pair_capacity;
   if (c->n > 0) {
@@ -629,6 +633,7 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   const size_t N = (size_t)n;
   if (n != c->n) {  // (re)allocate the per-atom storage
+    c->buf_gen += 1;
     c->n = n;
     c->P.n = n;
     for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw, &c->f_dis,
@@ -710,7 +715,10 @@ int eph_put(eph_ctx *c, int field, const double *src, int where) {
     case EPH_FIELD_F: dst = &c->f; break;
     case EPH_FIELD_XI: dst = &c->xi; c->have_xi = true; break;
     case EPH_FIELD_F_EXT:
-      if (!c->fext.p) CUDA_TRY(c, c->fext.alloc((size_t)c->n));
+      if (!c->fext.p) {
+        c->buf_gen += 1;
+        CUDA_TRY(c, c->fext.alloc((size_t)c->n));
+      }
       dst = &c->fext;
       if (!c->have_fext) drop_graph(c);  // the captured step cleared f instead of copying it
       c->have_fext = true;
@@ -1156,6 +1164,52 @@ long eph_beta_table(const eph_beta *b, int which, int elem, double *out) {
   const Spline &s = b->b.table(which, elem);
   if (out) std::memcpy(out, s.c.data(), sizeof(double) * 4 * (size_t)s.n);
   return s.n;
+}
+
+int eph_beta_set_knots(eph_beta *b, int elem, const double *rho_knots, long n_rho, const double *beta_knots,
+                       long n_beta) {
+  if (!b || !rho_knots || !beta_knots) return EPH_ERR_ARG;
+  return b->b.set_knots(elem, rho_knots, n_rho, beta_knots, n_beta).empty() ? EPH_OK : EPH_ERR_ARG;
+}
+
+int eph_beta_knot_gradient(const eph_beta *b, int elem, const double *g_rho_r_sq, const double *g_alpha,
+                           double *g_rho, double *g_beta) {
+  if (!b || elem < 0 || elem >= b->b.n_elements || !g_rho_r_sq || !g_alpha || !g_rho || !g_beta)
+    return EPH_ERR_ARG;
+  b->b.knot_gradient(elem, g_rho_r_sq, g_alpha, g_rho, g_beta);
+  return EPH_OK;
+}
+
+int eph_set_beta_knots(eph_ctx *c, int elem, const double *rho_knots, long n_rho, const double *beta_knots,
+                       long n_beta) {
+  if (!c || !rho_knots || !beta_knots) return EPH_ERR_ARG;
+  std::string e = c->beta.set_knots(elem, rho_knots, n_rho, beta_knots, n_beta);
+  if (!e.empty()) return fail(c, EPH_ERR_ARG, e);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // no kernel of the stream reads the tables meanwhile
+  return upload_tables(c);
+}
+
+int eph_set_grid_constants(eph_ctx *c, double C_e, double kappa_e) {
+  if (!c) return EPH_ERR_ARG;
+  if (c->args.T_infile != "NULL")
+    return fail(c, EPH_ERR_STATE, "the grid was read from a file: its cells keep their own C_e and kappa_e");
+  if (!(C_e > 0) || !(kappa_e >= 0)) return fail(c, EPH_ERR_ARG, "C_e must be positive and kappa_e non-negative");
+  Grid &g = c->grid;
+  const size_t nc = (size_t)g.ntotal;
+  c->args.C_e = C_e;
+  c->args.kappa_e = kappa_e;
+  g.C.assign(nc, C_e);
+  g.kappa.assign(nc, kappa_e);
+  std::vector<double> rc(nc);
+  for (size_t i = 0; i < nc; ++i) rc[i] = g.rho[i] * g.C[i];
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  CUDA_TRY(c, cudaMemcpy(c->rhoC.p, rc.data(), nc * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->kappa.p, g.kappa.data(), nc * 8, cudaMemcpyHostToDevice));
+  drop_graph(c);  // the substep count may change
+  set_time_params(c);
+  return EPH_OK;
 }
 
 struct eph_grid {

@@ -103,6 +103,9 @@ struct eph_ctx {
   double phase_ms[EPH_NPHASES] = {0};
   long phase_launches[EPH_NPHASES] = {0};
   long launches = 0;
+  // bumped whenever a device buffer is (re)allocated: graphs captured by
+  // others (the adjoint) hold the old addresses and must be captured again
+  unsigned long long buf_gen = 0;
 
   // one captured engine step replayed by eph_step (eph_set_graph)
   bool use_graph = false;

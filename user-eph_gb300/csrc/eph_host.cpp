@@ -121,25 +121,174 @@ std::string Beta::load(const char *path) {
   rho_r_sq.resize(n_elements);
   beta.resize(n_elements);
   alpha.resize(n_elements);
-  std::vector<double> buf;
+  rho_knots.resize(n_elements);
+  beta_knots.resize(n_elements);
   for (int e = 0; e < n_elements; ++e) {
     unsigned short z;
     if (!(fd >> z)) return "beta file: missing element number";
     numbers[e] = (uint8_t)z;
-    buf.assign(n_rho, 0.0);
+    std::vector<double> rk(n_rho, 0.0), bk(n_beta, 0.0);
     for (long j = 0; j < n_rho; ++j)
-      if (!(fd >> buf[j])) return "beta file: too few rho(r) knots";
-    rho[e].build(dr, buf);
-    for (long j = 0; j < n_rho; ++j) buf[j] = rho[e](std::sqrt((double)(size_t)j * dr_sq));
-    rho_r_sq[e].build(dr_sq, buf);
-    buf.assign(n_beta, 0.0);
+      if (!(fd >> rk[j])) return "beta file: too few rho(r) knots";
     for (long j = 0; j < n_beta; ++j)
-      if (!(fd >> buf[j])) return "beta file: too few beta(rho) knots";
-    beta[e].build(drho, buf);
-    for (long j = 0; j < n_beta; ++j) buf[j] = std::sqrt(buf[j]);
-    alpha[e].build(drho, buf);
+      if (!(fd >> bk[j])) return "beta file: too few beta(rho) knots";
+    std::string err = set_knots(e, rk.data(), n_rho, bk.data(), n_beta);
+    if (!err.empty()) return err;
   }
   return "";
+}
+
+std::string Beta::set_knots(int e, const double *rho_col, long nr, const double *beta_col, long nb) {
+  if (e < 0 || e >= n_elements) return "element index outside the beta file";
+  if (nr != n_rho || nb != n_beta) return "knot counts differ from the beta file's";
+  // eph_beta.h:103-124
+  rho_knots[e].assign(rho_col, rho_col + nr);
+  beta_knots[e].assign(beta_col, beta_col + nb);
+  rho[e].build(dr, rho_knots[e]);
+  std::vector<double> buf(n_rho);
+  for (long j = 0; j < n_rho; ++j) buf[j] = rho[e](std::sqrt((double)(size_t)j * dr_sq));
+  rho_r_sq[e].build(dr_sq, buf);
+  beta[e].build(drho, beta_knots[e]);
+  buf.assign(n_beta, 0.0);
+  for (long j = 0; j < n_beta; ++j) buf[j] = std::sqrt(beta_knots[e][j]);
+  alpha[e].build(drho, buf);
+  return "";
+}
+
+void Beta::knot_gradient(int e, const double *g_rho_r_sq, const double *g_alpha, double *g_rho,
+                         double *g_beta) const {
+  // rho(r^2) table <- samples z_j = rho(r_j), r_j = sqrt(j dr^2)
+  std::vector<double> z(n_rho), zbar(n_rho, 0.0);
+  for (long j = 0; j < n_rho; ++j) z[j] = rho[e](std::sqrt((double)(size_t)j * dr_sq));
+  spline_build_vjp(dr_sq, z, g_rho_r_sq, zbar.data());
+  // z_j = a + r (b + r (c + r d)) of the rho(r) interval holding r_j
+  std::vector<double> cbar((size_t)n_rho * 4, 0.0);
+  for (long j = 0; j < n_rho; ++j) {
+    const double r = std::sqrt((double)(size_t)j * dr_sq);
+    const size_t idx = (size_t)(r * rho[e].inv_dx);
+    if (!(r >= 0.0) || idx >= (size_t)n_rho) continue;  // outside the table: the value is NaN there
+    cbar[4 * idx + 0] += zbar[j];
+    cbar[4 * idx + 1] += zbar[j] * r;
+    cbar[4 * idx + 2] += zbar[j] * r * r;
+    cbar[4 * idx + 3] += zbar[j] * r * r * r;
+  }
+  for (long j = 0; j < n_rho; ++j) g_rho[j] = 0.0;
+  spline_build_vjp(dr, rho_knots[e], cbar.data(), g_rho);
+  // alpha knots are sqrt(beta knots)
+  std::vector<double> a(n_beta), abar(n_beta, 0.0);
+  for (long j = 0; j < n_beta; ++j) a[j] = std::sqrt(beta_knots[e][j]);
+  spline_build_vjp(drho, a, g_alpha, abar.data());
+  for (long j = 0; j < n_beta; ++j) g_beta[j] = a[j] > 0.0 ? 0.5 * abar[j] / a[j] : 0.0;
+}
+
+namespace {
+
+// Forward-mode number: value and one directional derivative.
+struct Dual {
+  double v = 0.0, d = 0.0;
+  Dual() = default;
+  Dual(double a) : v(a) {}
+  Dual(double a, double b) : v(a), d(b) {}
+};
+inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
+inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+inline bool operator==(Dual a, Dual b) { return a.v == b.v; }
+inline bool operator!=(Dual a, Dual b) { return a.v != b.v; }
+inline Dual dabs(Dual a) { return a.v < 0.0 ? -a : (a.v > 0.0 ? a : Dual(0.0, 0.0)); }
+
+// Spline::build (eph_spline.h:31-132) on forward-mode numbers, same steps.
+void build_dual(double dx, const std::vector<Dual> &y, std::vector<Dual> &c) {
+  const size_t points = y.size();
+  c.assign((points + 1) * 4, Dual(0.0));
+  auto A = [&](size_t i) -> Dual & { return c[4 * i + 0]; };
+  auto B = [&](size_t i) -> Dual & { return c[4 * i + 1]; };
+  auto C = [&](size_t i) -> Dual & { return c[4 * i + 2]; };
+  auto D = [&](size_t i) -> Dual & { return c[4 * i + 3]; };
+  const Dual h(dx);
+  for (size_t i = 0; i < points - 1; ++i) B(i) = (y[i + 1] - y[i]) / h;
+  const Dual z1 = Dual(2.0) * B(0) - B(1);
+  const Dual z0 = Dual(2.0) * z1 - B(0);
+  const Dual z2 = Dual(2.0) * B(points - 2) - B(points - 1);
+  const Dual z3 = Dual(2.0) * z2 - B(points - 1);
+  B(points - 1) = z2;
+  for (size_t i = 2; i < points - 2; ++i) {
+    C(i) = dabs(B(i + 1) - B(i));
+    D(i) = dabs(B(i - 1) - B(i - 2));
+  }
+  C(0) = dabs(B(1) - B(0));
+  D(0) = dabs(z1 - z0);
+  C(1) = dabs(B(2) - B(1));
+  D(1) = dabs(B(0) - z1);
+  C(points - 2) = dabs(z2 - B(points - 2));
+  D(points - 2) = dabs(B(points - 3) - B(points - 4));
+  C(points - 1) = dabs(z3 - z2);
+  D(points - 1) = dabs(B(points - 2) - B(points - 3));
+  for (size_t i = 0; i < points; ++i) {
+    Dual d_2, d_1;
+    if (i == 0) {
+      d_2 = z0;
+      d_1 = z1;
+    } else if (i == 1) {
+      d_2 = z1;
+      d_1 = B(i - 1);
+    } else {
+      d_2 = B(i - 2);
+      d_1 = B(i - 1);
+    }
+    const Dual d1 = B(i + 1), d0 = B(i);
+    const Dual w1 = C(i), w0 = D(i);
+    if (d_2 == d_1 && d0 != d1)
+      A(i) = d_1;
+    else if (d0 == d1 && d_2 == d_1)
+      A(i) = d0;
+    else if (d_1 == d0)
+      A(i) = d0;
+    else if (d_2 == d_1 && d0 == d1 && d0 != d_1)
+      A(i) = Dual(0.5) * (d_1 + d0);
+    else
+      A(i) = (d_1 * w1 + d0 * w0) / (w1 + w0);
+  }
+  for (size_t i = 0; i < points - 1; ++i) {
+    const double fi = (double)i, fi1 = (double)(i + 1);
+    const Dual dx3(dx * dx * dx);
+    const Dual x0_1(fi * dx), x0_2(fi * dx * (fi * dx)), x0_3(fi * dx * (fi * dx * (fi * dx)));
+    const Dual x1_1(fi1 * dx), x1_2(fi1 * dx * (fi1 * dx)), x1_3(fi1 * dx * (fi1 * dx * (fi1 * dx)));
+    const Dual two(2.0), three(3.0);
+    D(i) = (-A(i) * x0_1 - A(i + 1) * x0_1 + A(i) * x1_1 + A(i + 1) * x1_1 + two * y[i] - two * y[i + 1]) / dx3;
+    C(i) = (-A(i) + A(i + 1) + three * D(i) * x0_2 - three * D(i) * x1_2) / two / h;
+    B(i) = (C(i) * x0_2 + D(i) * x0_3 - C(i) * x1_2 - D(i) * x1_3 - y[i] + y[i + 1]) / h;
+    A(i) = y[i] - B(i) * x0_1 - C(i) * x0_2 - D(i) * x0_3;
+  }
+  A(points - 1) = y[points - 1];
+  B(points - 1) = Dual(0.0);
+  C(points - 1) = Dual(0.0);
+  D(points - 1) = Dual(0.0);
+  c.resize(points * 4);
+}
+
+}  // namespace
+
+void spline_build_vjp(double dx, const std::vector<double> &y, const double *cbar, double *ybar) {
+  const size_t n = y.size();
+  constexpr size_t PERIOD = 16;  // > the width (6) of the window of knots an interval depends on
+  std::vector<Dual> yd(n), c;
+  for (size_t m = 0; m < PERIOD && m < n; ++m) {
+    for (size_t k = 0; k < n; ++k) yd[k] = Dual(y[k], (k % PERIOD == m) ? 1.0 : 0.0);
+    build_dual(dx, yd, c);
+    // coefficients of interval i depend on knots i-2..i+3 (the two boundary
+    // extrapolations z0..z3 stay inside that window): at most one seeded knot
+    for (size_t i = 0; i < n; ++i) {
+      const long lo = (long)i - 2 > 0 ? (long)i - 2 : 0;
+      long k = lo + (long)((m + PERIOD - (size_t)lo % PERIOD) % PERIOD);
+      if (k > (long)i + 3 || k >= (long)n) continue;
+      double s = 0.0;
+      for (int q = 0; q < 4; ++q) s += c[4 * i + q].d * cbar[4 * i + q];
+      ybar[k] += s;
+    }
+  }
 }
 
 void Linear::build(double in_dx, const std::vector<double> &in_y) {

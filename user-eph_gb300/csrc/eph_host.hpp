@@ -34,13 +34,28 @@ struct Beta {
   long n_rho = 0, n_beta = 0;
   double dr = 0, dr_sq = 0, drho = 0;
   std::vector<Spline> rho, rho_r_sq, beta, alpha;
+  // the file's knot columns per element: rho(r) (n_rho values), beta(rho) (n_beta)
+  std::vector<std::vector<double>> rho_knots, beta_knots;
   // returns an empty string on success, else the reason
   std::string load(const char *path);
+  // replace element e's knot columns and rebuild its four tables as load() does
+  std::string set_knots(int e, const double *rho_col, long nr, const double *beta_col, long nb);
+  // Chain rule through the table construction: from dL/d(coefficients) of the
+  // rho(r^2) table (n_rho x 4) and of the alpha table (n_beta x 4) of element
+  // e to dL/d(knot columns), written to g_rho (n_rho) and g_beta (n_beta).
+  void knot_gradient(int e, const double *g_rho_r_sq, const double *g_alpha, double *g_rho, double *g_beta) const;
   const Spline &table(int which, int elem) const;
   // eph_beta.h:174-197 (zero above rho_cutoff)
   double get_beta(int elem, double r) const;
   double get_alpha(int elem, double r) const;
 };
+
+// Reverse-mode product of Spline::build: given cbar = dL/d(coefficients)
+// (4 per knot) of the table built from knots y with spacing dx, adds
+// dL/dy to ybar.  The construction is local (the coefficients of interval i
+// depend on y[i-2 .. i+3]), so 16 forward-mode passes with interleaved seeds
+// give the exact Jacobian-transpose product for any number of knots.
+void spline_build_vjp(double dx, const std::vector<double> &y, const double *cbar, double *ybar);
 
 enum : int { GRID_CONSTANT = 0, GRID_DYNAMIC = 1, GRID_ZERO_DERIVATIVE = 2 };
 

@@ -102,6 +102,18 @@ SIGNATURES = {
     "eph_grid_substeps": (C.c_uint, [C.c_void_p, C.c_double, _dp]),
     "eph_grid_save_state": (C.c_int, [C.c_void_p, C.c_char_p]),
     "eph_grid_save_temperature": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+    "eph_beta_set_knots": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_long, _dp, C.c_long]),
+    "eph_beta_knot_gradient": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
+    "eph_set_beta_knots": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_long, _dp, C.c_long]),
+    "eph_set_grid_constants": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
+    "eph_adjoint_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "eph_adjoint_destroy": (None, [C.c_void_p]),
+    "eph_adjoint_last_error": (C.c_char_p, [C.c_void_p]),
+    "eph_adjoint_forward": (C.c_int, [C.c_void_p, C.c_long, _dp, _dp]),
+    "eph_adjoint_backward": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "eph_adjoint_gradient": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_long]),
+    "eph_adjoint_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "eph_adjoint_timing": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_long), C.POINTER(C.c_long)]),
 }
 
 
@@ -157,6 +169,26 @@ class BetaFile:
         out = np.zeros((n, 4))
         L.eph_beta_table(self.h, w, elem, out.ctypes.data_as(_dp))
         return out
+
+    def set_knots(self, elem, rho_knots, beta_knots):
+        r = np.ascontiguousarray(rho_knots, dtype=np.float64)
+        b = np.ascontiguousarray(beta_knots, dtype=np.float64)
+        rc = lib().eph_beta_set_knots(self.h, elem, r.ctypes.data_as(_dp), r.size, b.ctypes.data_as(_dp), b.size)
+        if rc:
+            raise EphError(rc, "knot columns do not match the file")
+
+    def knot_gradient(self, elem, g_rho_r_sq, g_alpha):
+        """dL/d(rho(r) knots), dL/d(beta knots) from dL/d(coefficients) of the
+        rho(r^2) and alpha tables (arrays of n x 4)."""
+        gr = np.ascontiguousarray(g_rho_r_sq, dtype=np.float64)
+        ga = np.ascontiguousarray(g_alpha, dtype=np.float64)
+        out_r = np.zeros(gr.size // 4)
+        out_b = np.zeros(ga.size // 4)
+        rc = lib().eph_beta_knot_gradient(self.h, elem, gr.ctypes.data_as(_dp), ga.ctypes.data_as(_dp),
+                                          out_r.ctypes.data_as(_dp), out_b.ctypes.data_as(_dp))
+        if rc:
+            raise EphError(rc, "knot_gradient")
+        return out_r, out_b
 
 
 class Grid:
@@ -226,6 +258,7 @@ class FixEPH:
             md.boxhi[k] = float(boxhi[k])
         md.dt, md.boltz, md.ftm2v, md.skin = dt, boltz, ftm2v, skin
         md.groupbit, md.device, md.mode = groupbit, device, mode
+        self.words = [str(w) for w in words]
         self._argv = (C.c_char_p * len(words))(*[w.encode() for w in words])
         h = C.c_void_p()
         rc = L.eph_create(len(words), self._argv, C.byref(md), C.byref(h))
@@ -358,6 +391,15 @@ class FixEPH:
 
     def set_graph(self, on=True):
         self._check(self.L.eph_set_graph(self.h, 1 if on else 0))
+
+    def set_beta_knots(self, elem, rho_knots, beta_knots):
+        r = np.ascontiguousarray(rho_knots, dtype=np.float64)
+        b = np.ascontiguousarray(beta_knots, dtype=np.float64)
+        self._check(lib().eph_set_beta_knots(self.h, elem, r.ctypes.data_as(_dp), r.size, b.ctypes.data_as(_dp),
+                                             b.size))
+
+    def set_grid_constants(self, C_e, kappa_e):
+        self._check(lib().eph_set_grid_constants(self.h, float(C_e), float(kappa_e)))
 
     def set_timestep(self, n):
         self._check(self.L.eph_set_timestep(self.h, n))
