@@ -255,7 +255,7 @@ def run_batched(args, dev):
 ADJ_CELLS, ADJ_GRID, ADJ_STEPS, ADJ_K, ADJ_DT = 20, (16, 16, 16), 200, 20, 0.001
 
 
-def run_adjoint(args, dev):
+def run_adjoint(args, dev, fd=True):
     """The adjoint workload: fcc Ni 20^3 cells (32,000 atoms), ions at 300 K,
     electrons at 2,000 K on a 16^3 grid, 200 steps of 1 fs, flags 7.  The beta
     file has 16 rho(r) knots and 64 beta(rho) knots.  Loss = sum_t (E[t] -
@@ -277,6 +277,7 @@ def run_adjoint(args, dev):
         # 1e-6 relative finite difference would measure that instead of the gradient
         bf = W.write_beta_file(os.path.join(wd, "adj.beta"), n_rho=16, n_beta=64, drho=0.005,
                                beta_fn=lambda r: 0.02 + 2.0 * r * r)
+        nsteps = args.adjoint_steps
         atoms = W.fcc_lattice(ADJ_CELLS, seed=SEED + 7)
         words = W.fix_args(bf, seed=SEED, flags=7, T_e=2000.0, grid=ADJ_GRID)
         fix = ephgb.FixEPH(words, atoms, dt=ADJ_DT, mode=ephgb.MODE_FAST, device=dev)
@@ -284,19 +285,19 @@ def run_adjoint(args, dev):
         r0, b0 = (c.copy() for c in adj.columns[0])
         hidden = b0 * (1.0 + 0.3 * np.sin(np.arange(b0.size) / 6.0))
         adj.set_knots(0, r0, hidden)
-        target, _ = adj.forward(ADJ_STEPS)
+        target, _ = adj.forward(nsteps)
         adj.set_knots(0, r0, b0)
 
         def loss(r, b, C_e, kappa_e):
             adj.set_knots(0, r, b)
             adj.set_grid_constants(C_e, kappa_e)
-            E, _ = adj.forward(ADJ_STEPS)
+            E, _ = adj.forward(nsteps)
             return float(((E - target) ** 2).sum())
 
         for _ in range(2):  # warm-up
-            E, _ = adj.forward(ADJ_STEPS)
+            E, _ = adj.forward(nsteps)
             adj.backward(2.0 * (E - target), None)
-        E, _ = adj.forward(ADJ_STEPS)
+        E, _ = adj.forward(nsteps)
         L0 = float(((E - target) ** 2).sum())
         adj.backward(2.0 * (E - target), None)
         t = adj.timing()
@@ -310,10 +311,22 @@ def run_adjoint(args, dev):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        plain.step(ADJ_STEPS)
+        plain.step(nsteps)
         e1.record(stream)
         torch.cuda.synchronize()
         plain_ms = e0.elapsed_time(e1)
+        res = {"workload": "fcc Ni 20^3 cells (32,000 atoms), ions 300 K, T_e 2,000 K, FDM 16^3, %d steps of 1 fs, "
+                           "flags 7; 64 beta knots (beta = 0.02 + 2 rho^2), 16 rho(r) knots, C_e, kappa_e; "
+                           "checkpoints every 20 steps" % nsteps,
+               "loss": "sum_t (E[t] - E*[t])^2, E* from a hidden beta(rho)", "loss_value": L0,
+               "forward_ms": t["forward_ms"], "backward_ms": t["backward_ms"], "plain_forward_ms": plain_ms,
+               "adjoint_over_forward": t["backward_ms"] / t["forward_ms"],
+               "forward_plus_adjoint_over_plain_forward": (t["forward_ms"] + t["backward_ms"]) / plain_ms,
+               "forward_launches": t["forward_launches"], "backward_launches": t["backward_launches"],
+               "timing": "CUDA events on the fix's stream (graph replays); backward includes the recomputation "
+                         "from checkpoints"}
+        if not fd:
+            return res
         # central finite differences of the loss, h = 1e-6 relative
         h = 1e-6
         fd = {"rho_knots": np.zeros(r0.size), "beta_knots": np.zeros(b0.size)}
@@ -333,6 +346,16 @@ def run_adjoint(args, dev):
             fd["beta_knots"][k] = (loss(r0, p, C0, K0) - loss(r0, m, C0, K0)) / (2 * d)
         fd["C_e"] = (loss(r0, b0, C0 * (1 + h), K0) - loss(r0, b0, C0 * (1 - h), K0)) / (2 * h * C0)
         fd["kappa_e"] = (loss(r0, b0, C0, K0 * (1 + h)) - loss(r0, b0, C0, K0 * (1 - h))) / (2 * h * K0)
+        # a second estimate for kappa_e with a larger step (the loss is smooth in
+        # kappa_e; rounding along 200 steps dominates the 1e-6 relative difference)
+        fd_k4 = (loss(r0, b0, C0, K0 * (1 + 1e-4)) - loss(r0, b0, C0, K0 * (1 - 1e-4))) / (2e-4 * K0)
+        fd_r5 = np.zeros(r0.size)  # and the rho(r) knots with 1e-5 relative
+        for k in range(r0.size):
+            d = 1e-5 * max(abs(r0[k]), floor)
+            p, m = r0.copy(), r0.copy()
+            p[k] += d
+            m[k] -= d
+            fd_r5[k] = (loss(p, b0, C0, K0) - loss(m, b0, C0, K0)) / (2 * d)
         loss(r0, b0, C0, K0)
         # each difference's rounding noise: 2 eps L / (2 step)
         eps = 2.0 ** -52 * L0
@@ -343,18 +366,12 @@ def run_adjoint(args, dev):
             d = np.abs(np.asarray(g[k]) - fd[k])
             err[k] = float(np.max(d) / np.abs(fd[k]).max())
             err_above_noise[k] = float(np.max(np.maximum(d - 10.0 * eps / steps_h[k], 0.0)) / np.abs(fd[k]).max())
-        return {"workload": "fcc Ni 20^3 cells (32,000 atoms), ions 300 K, T_e 2,000 K, FDM 16^3, 200 steps of 1 fs, "
-                            "flags 7; 64 beta knots (beta = 0.02 + 2 rho^2), 16 rho(r) knots, C_e, kappa_e; "
-                            "checkpoints every 20 steps",
-                "loss": "sum_t (E[t] - E*[t])^2, E* from a hidden beta(rho)", "loss_value": L0,
-                "forward_ms": t["forward_ms"], "backward_ms": t["backward_ms"], "plain_forward_ms": plain_ms,
-                "adjoint_over_forward": t["backward_ms"] / t["forward_ms"],
-                "forward_plus_adjoint_over_plain_forward": (t["forward_ms"] + t["backward_ms"]) / plain_ms,
-                "forward_launches": t["forward_launches"], "backward_launches": t["backward_launches"],
-                "grad_rel_err_vs_fd": err, "grad_rel_err_max": max(err.values()),
-                "grad_rel_err_above_fd_noise": err_above_noise, "fd_h_relative": h,
-                "params": int(r0.size + b0.size + 2),
-                "timing": "CUDA events on the fix's stream; backward includes the recomputation from checkpoints"}
+        res.update({"grad_rel_err_vs_fd": err, "grad_rel_err_max": max(err.values()),
+                    "grad_rel_err_above_fd_noise": err_above_noise, "fd_h_relative": h,
+                    "kappa_e_rel_err_vs_fd_h1e-4": abs(g["kappa_e"] - fd_k4) / abs(fd_k4),
+                    "rho_knots_rel_err_vs_fd_h1e-5": float(np.abs(g["rho_knots"] - fd_r5).max() / np.abs(fd_r5).max()),
+                    "params": int(r0.size + b0.size + 2)})
+        return res
 
 
 def cpu_baseline(threads, steps=1, warm=1):
@@ -391,6 +408,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="omit the batched-replicas leg")
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--no-adjoint", action="store_true", help="omit the adjoint leg")
+    ap.add_argument("--only-adjoint", action="store_true", help="run the adjoint leg alone (profiling)")
+    ap.add_argument("--adjoint-steps", type=int, default=ADJ_STEPS)
+    ap.add_argument("--no-adjoint-fd", action="store_true", help="skip the finite-difference check")
     ap.add_argument("--cells", type=int, default=CELLS, help="fcc cells per edge (profiling cases)")
     ap.add_argument("--grid", type=int, default=GRID[0], help="FDM cells per edge (profiling cases)")
     args = ap.parse_args()
@@ -422,6 +442,9 @@ def main():
 
     import torch
 
+    if args.only_adjoint:
+        print(json.dumps(run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)), fd=not args.no_adjoint_fd)))
+        return
     if world > 1:
         torch.distributed.init_process_group("nccl")
     res = run_gpu(args, rank, world)
@@ -462,7 +485,7 @@ def main():
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
             line["batched"]["value"] = float(t.item())
     if rank == 0 and not args.no_adjoint:
-        line["adjoint"] = run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)))
+        line["adjoint"] = run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)), fd=not args.no_adjoint_fd)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(threads, steps=1, warm=1).items() if k != "seconds"}
     if rank == 0:

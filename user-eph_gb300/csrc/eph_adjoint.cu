@@ -67,15 +67,21 @@ struct GridArgs {
   const signed char *flag;
 };
 
-// value, derivative and knot of a spline at x (index as eph_spline.h:134-142)
+// value, derivative and knot of a spline at x (index as eph_spline.h:134-142).
+// The reverse sweeps are FP64-issue bound: products and sums are fused
+// explicitly (this file is compiled without contraction).
 __device__ __forceinline__ void spline_vd(const D4 *__restrict__ tab, double inv_dx, int n, double x, double &val,
                                           double &der, int &idx) {
   unsigned long long k = trunc_index(x * inv_dx);
   if (k >= (unsigned long long)n) k = (unsigned long long)(n - 1);
   const D4 c = tab[k];
-  val = c.x + x * (c.y + x * (c.z + x * c.w));
-  der = c.y + x * (2.0 * c.z + 3.0 * x * c.w);
+  val = fma(x, fma(x, fma(x, c.w, c.z), c.y), c.x);
+  der = fma(x, fma(3.0 * x, c.w, 2.0 * c.z), c.y);
   idx = (int)k;
+}
+
+__device__ __forceinline__ double dotf(double ax, double ay, double az, double bx, double by, double bz) {
+  return fma(az, bz, fma(ay, by, ax * bx));
 }
 
 // e = x_j (periodic image of the pair code) - x_i, as the density sweep forms it
@@ -186,32 +192,37 @@ __global__ void k_adj_fdm_first(GridArgs G, const double *__restrict__ Tk, const
   u[r] = substep_reverse(G, Tk, src, r, Tb[r] + *tau, srcbar, gC, gK, true);
 }
 
-// lam_k = transpose of the substep's Jacobian applied to u_k; then u_k-1 of
-// the substep before (Tprev = T_k-1), or, after the first substep, the
-// cotangent of the grid at the start of the step (Tb).
-__global__ void k_adj_fdm_back(GridArgs G, const double *__restrict__ u, const double *__restrict__ Tprev,
-                               const double *__restrict__ src, double *__restrict__ u_out, double *__restrict__ Tb,
-                               double *__restrict__ srcbar, double *__restrict__ gC, double *__restrict__ gK) {
+// The transpose of one substep's Jacobian, as 7 weights per cell (self,
+// -x, +x, -y, +y, -z, +z neighbour): lam[r] = u[r] + sum_m W[m][r] u[s_m] with
+// W = dddT_s/dT_r * dt'/(rho_e C_e)_s on DYNAMIC cells s.  The same for every
+// substep while kappa, C_e and the flags stay, so it is built once per pass.
+// On axes of 1 or 2 cells the neighbours coincide; each distinct cell is
+// counted once (in the self or the -axis slot).
+__global__ void k_adj_fdm_weights(GridArgs G, double *__restrict__ W) {
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= G.nc) return;
-  double lam = u[r];
-#pragma unroll
+  double w[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int a = 0; a < 3; ++a) {
     const long st = a == 0 ? 1 : (a == 1 ? G.n[0] : G.n[0] * G.n[1]);
     const long na = G.n[a];
     const long c = (r / st) % na;
-    // the distinct cells of r's line whose axis-a stencil can hold r
     long cand[3];
+    int slot[3];
     int ncand = 0;
-    cand[ncand++] = r;
-    if (na >= 2) cand[ncand++] = c > 0 ? r - st : r + (na - 1) * st;
-    if (na >= 3) cand[ncand++] = c < na - 1 ? r + st : r - (na - 1) * st;
+    cand[ncand] = r;
+    slot[ncand++] = 0;
+    if (na >= 2) {
+      cand[ncand] = c > 0 ? r - st : r + (na - 1) * st;
+      slot[ncand++] = 1 + 2 * a;
+    }
+    if (na >= 3) {
+      cand[ncand] = c < na - 1 ? r + st : r - (na - 1) * st;
+      slot[ncand++] = 2 + 2 * a;
+    }
     const double ih2 = 1.0 / (G.h[a] * G.h[a]);
     for (int m = 0; m < ncand; ++m) {
       const long s = cand[m];
       if (G.flag[s] != 1) continue;  // only DYNAMIC cells move (eph_fdm.h:375-387)
-      const double us = u[s];
-      if (us == 0.0) continue;
       long p, q;
       axis_pq(G, s, a, p, q);
       const double dk = G.kappa[q] - G.kappa[p];
@@ -219,9 +230,30 @@ __global__ void k_adj_fdm_back(GridArgs G, const double *__restrict__ u, const d
       if (q == r) coef += 0.25 * ih2 * dk + G.kappa[s] * ih2;
       if (p == r) coef += -0.25 * ih2 * dk + G.kappa[s] * ih2;
       if (s == r) coef -= 2.0 * G.kappa[s] * ih2;
-      lam += us * G.inner_dt / G.rhoC[s] * coef;
+      w[slot[m]] += coef * G.inner_dt / G.rhoC[s];
     }
   }
+  for (int m = 0; m < 7; ++m) W[(size_t)m * G.nc + r] = w[m];
+}
+
+// lam_k = the transposed substep applied to u_k; then u_k-1 of the substep
+// before (Tprev = T_k-1), or, after the first substep, the cotangent of the
+// grid at the start of the step (Tb).
+__global__ void k_adj_fdm_back(GridArgs G, const double *__restrict__ W, const double *__restrict__ u,
+                               const double *__restrict__ Tprev, const double *__restrict__ src,
+                               double *__restrict__ u_out, double *__restrict__ Tb, double *__restrict__ srcbar,
+                               double *__restrict__ gC, double *__restrict__ gK) {
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= G.nc) return;
+  const long nx = G.n[0], nxy = G.n[0] * G.n[1];
+  const long i = r % nx, j = (r / nx) % G.n[1], k = r / nxy;
+  const long nb[6] = {i > 0 ? r - 1 : r + (nx - 1), i < nx - 1 ? r + 1 : r - (nx - 1),
+                      j > 0 ? r - nx : r + (G.n[1] - 1) * nx, j < G.n[1] - 1 ? r + nx : r - (G.n[1] - 1) * nx,
+                      k > 0 ? r - nxy : r + (G.n[2] - 1) * nxy, k < G.n[2] - 1 ? r + nxy : r - (G.n[2] - 1) * nxy};
+  const double ur = u[r];
+  double lam = fma(W[r], ur, ur);
+#pragma unroll
+  for (int m = 0; m < 6; ++m) lam = fma(W[(size_t)(m + 1) * G.nc + r], u[nb[m]], lam);
   if (Tprev)
     u_out[r] = substep_reverse(G, Tprev, src, r, lam, srcbar, gC, gK, false);
   else
@@ -341,7 +373,8 @@ __global__ void k_adj_tb_apply(long nc, const int *__restrict__ tb_exp, U128 *__
 //   dL/dw_i     = a_i U_i
 //   dL/da_i     = 2 w_i.U_i + xi_i.V_i
 //   dL/drho_i   = dL/da_i (alpha'(rho_i) - a_i) / rho_i
-// and the alpha-table coefficient gradient dL/da_i / rho_i (1, rho, rho^2, rho^3).
+// and the alpha-table coefficient gradient dL/da_i / rho_i (1, rho, rho^2, rho^3)
+// (AMODE 0: added to this block's own partial row, summed once per pass).
 // adjW = {dL/dw_i, dL/drho_i}.
 template <bool FAST, int AMODE>
 __global__ void __launch_bounds__(ABLOCK)
@@ -376,20 +409,20 @@ __global__ void __launch_bounds__(ABLOCK)
       const D4 xj = S.x1[j];
       double ex, ey, ez;
       pair_vector(P, xi, xj, u >> IDX_BITS, ex, ey, ez);
-      const double r2 = ex * ex + ey * ey + ez * ez;
+      const double r2 = dotf(ex, ey, ez, ex, ey, ez);
       double g, gd;
       int idx;
       spline_vd(P.tab_rho_r_sq + (size_t)(int)xj.w * P.n_rho, P.inv_dr_sq, P.n_rho, r2, g, gd, idx);
-      const double H = g / r2;
+      const double H = g * recip_nr(r2);
       const D4 cej = cE[j], crj = cR[j];
-      const double dE = H * (ex * (ce.x - cej.x) + ey * (ce.y - cej.y) + ez * (ce.z - cej.z));
-      const double dR = H * (ex * (cr.x - crj.x) + ey * (cr.y - crj.y) + ez * (cr.z - crj.z));
-      Ux += dE * ex;
-      Uy += dE * ey;
-      Uz += dE * ez;
-      Vx += dR * ex;
-      Vy += dR * ey;
-      Vz += dR * ez;
+      const double dE = H * dotf(ex, ey, ez, ce.x - cej.x, ce.y - cej.y, ce.z - cej.z);
+      const double dR = H * dotf(ex, ey, ez, cr.x - crj.x, cr.y - crj.y, cr.z - crj.z);
+      Ux = fma(dE, ex, Ux);
+      Uy = fma(dE, ey, Uy);
+      Uz = fma(dE, ez, Uz);
+      Vx = fma(dR, ex, Vx);
+      Vy = fma(dR, ey, Vy);
+      Vz = fma(dR, ez, Vz);
     }
   }
   D4 out{0.0, 0.0, 0.0, 0.0};
@@ -399,7 +432,7 @@ __global__ void __launch_bounds__(ABLOCK)
     const D4 Bi = S.Bw[i];
     const double rho = Ai.x;
     const double a = FAST ? Ai.y : Ai.y / rho;
-    const double ab = 2.0 * (Bi.y * Ux + Bi.z * Uy + Bi.w * Uz) + (Ai.z * Vx + Ai.w * Vy + Bi.x * Vz);
+    const double ab = fma(2.0, dotf(Bi.y, Bi.z, Bi.w, Ux, Uy, Uz), dotf(Ai.z, Ai.w, Bi.x, Vx, Vy, Vz));
     out.x = a * Ux;
     out.y = a * Uy;
     out.z = a * Uz;
@@ -408,13 +441,13 @@ __global__ void __launch_bounds__(ABLOCK)
       double al, ald;
       int idx;
       spline_vd(P.tab_alpha + (size_t)ei * P.n_beta, P.inv_drho, P.n_beta, rho, al, ald, idx);
-      out.w = ab * (ald - a) / rho;
       const double q = ab / rho;
+      out.w = q * (ald - a);
       key = ei * P.n_beta + idx;
       c0 = q;
       c1 = q * rho;
-      c2 = q * rho * rho;
-      c3 = q * rho * rho * rho;
+      c2 = c1 * rho;
+      c3 = c2 * rho;
     }
   }
   if (valid) adjW[i] = out;
@@ -424,7 +457,7 @@ __global__ void __launch_bounds__(ABLOCK)
     for (int q = t; q < nt4; q += blockDim.x) {
       double sum = 0.0;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += s_w[w * nt4 + q];
-      gpart[(size_t)blockIdx.x * nt4 + q] = sum;
+      gpart[(size_t)blockIdx.x * nt4 + q] += sum;
     }
   } else if (key >= 0) {
     atomicAdd(gglob + 4 * key + 0, c0);
@@ -443,6 +476,9 @@ __global__ void __launch_bounds__(ABLOCK)
 // r^2 in H and in rho_i, rho_j), dQ/dv_i = F[om]_i, and for its ordered pairs
 // the rho(r^2)-table coefficient gradient (a_i B_i / r^2 + dL/drho_i) (1, r^2,
 // r^4, r^6); then the integrator in reverse: x = x0 + dt v, v = v0 + dtf/m f0.
+// dQ/de at fixed H is P_i V_i - P_j V_j + dv (e.Od) + L [dcE (e.Wd) + dcR (e.Xd)]
+// with V_a = (e.dv) om_a + L [(e.dcE) w_a + (e.dcR) xi_a] and Od, Wd, Xd the
+// P-weighted differences of om, w, xi.
 template <bool FAST, bool MULTI, int RMODE>
 __global__ void __launch_bounds__(ABLOCK)
     k_adj_sweep2(StepParams P, Slot S, const int *__restrict__ mask, const int *__restrict__ type,
@@ -468,66 +504,77 @@ __global__ void __launch_bounds__(ABLOCK)
       const D4 xj = S.x1[j];
       double ex, ey, ez;
       pair_vector(P, xi, xj, u >> IDX_BITS, ex, ey, ez);
-      const double r2 = ex * ex + ey * ey + ez * ez;
+      const double r2 = dotf(ex, ey, ez, ex, ey, ez);
+      const double rinv = recip_nr(r2);
       const int ej = (int)xj.w;
       double gj, gjd;
       int idx;
       spline_vd(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, gj, gjd, idx);
-      const double Hij = gj / r2, Hpij = (gjd - Hij) / r2;
+      const double Hij = gj * rinv, Hpij = (gjd - Hij) * rinv;
       double gid = gjd, Hji = Hij, Hpji = Hpij;
       if (MULTI && ej != ei) {
         double gi;
         int idx2;
         spline_vd(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, gi, gid, idx2);
-        Hji = gi / r2;
-        Hpji = (gid - Hji) / r2;
+        Hji = gi * rinv;
+        Hpji = (gid - Hji) * rinv;
       }
-      const D4 Aj = S.A[j], Bj = S.Bw[j], vj = S.v1[j], cej = cE[j], crj = cR[j], Wj = adjW[j];
+      const D4 Aj = S.A[j], Wj = adjW[j], vj = S.v1[j];
       const bool live_j = Aj.x > 0.0;
       const double aj = live_j ? (FAST ? Aj.y : Aj.y / Aj.x) : 0.0;
       const double dvx = vi.x - vj.x, dvy = vi.y - vj.y, dvz = vi.z - vj.z;
-      const double e_dv = ex * dvx + ey * dvy + ez * dvz;
+      const double e_dv = dotf(ex, ey, ez, dvx, dvy, dvz);
       const double Pi = ai * Hij, Pj = aj * Hji;
-      const double eoi = ex * Wi.x + ey * Wi.y + ez * Wi.z, eoj = ex * Wj.x + ey * Wj.y + ez * Wj.z;
+      const double eoi = dotf(ex, ey, ez, Wi.x, Wi.y, Wi.z), eoj = dotf(ex, ey, ez, Wj.x, Wj.y, Wj.z);
+      const double eOd = fma(Pi, eoi, -Pj * eoj);
       double Bi_ = e_dv * eoi, Bj_ = -e_dv * eoj;
-      const double Odx = Pi * Wi.x - Pj * Wj.x, Ody = Pi * Wi.y - Pj * Wj.y, Odz = Pi * Wi.z - Pj * Wj.z;
-      const double eOd = Pi * eoi - Pj * eoj;
-      double gx = e_dv * Odx + dvx * eOd, gy = e_dv * Ody + dvy * eOd, gz = e_dv * Odz + dvz * eOd;
+      double Vix = e_dv * Wi.x, Viy = e_dv * Wi.y, Viz = e_dv * Wi.z;
+      double Vjx = e_dv * Wj.x, Vjy = e_dv * Wj.y, Vjz = e_dv * Wj.z;
+      double gx = dvx * eOd, gy = dvy * eOd, gz = dvz * eOd;
       if (live_i && live_j) {
+        const D4 Bj = S.Bw[j], cej = cE[j], crj = cR[j];
         const double dEx = cei.x - cej.x, dEy = cei.y - cej.y, dEz = cei.z - cej.z;
         const double dRx = cri.x - crj.x, dRy = cri.y - crj.y, dRz = cri.z - crj.z;
-        const double e_dE = ex * dEx + ey * dEy + ez * dEz, e_dR = ex * dRx + ey * dRy + ez * dRz;
-        const double ewi = ex * Bi.y + ey * Bi.z + ez * Bi.w, ewj = ex * Bj.y + ey * Bj.z + ez * Bj.w;
-        const double exi = ex * Ai.z + ey * Ai.w + ez * Bi.x, exj = ex * Aj.z + ey * Aj.w + ez * Bj.x;
-        Bi_ += ewi * e_dE + exi * e_dR;
-        Bj_ -= ewj * e_dE + exj * e_dR;
-        const double eWd = Pi * ewi - Pj * ewj, eXd = Pi * exi - Pj * exj;
-        gx += e_dE * (Pi * Bi.y - Pj * Bj.y) + dEx * eWd + e_dR * (Pi * Ai.z - Pj * Aj.z) + dRx * eXd;
-        gy += e_dE * (Pi * Bi.z - Pj * Bj.z) + dEy * eWd + e_dR * (Pi * Ai.w - Pj * Aj.w) + dRy * eXd;
-        gz += e_dE * (Pi * Bi.w - Pj * Bj.w) + dEz * eWd + e_dR * (Pi * Bi.x - Pj * Bj.x) + dRz * eXd;
+        const double e_dE = dotf(ex, ey, ez, dEx, dEy, dEz), e_dR = dotf(ex, ey, ez, dRx, dRy, dRz);
+        const double ewi = dotf(ex, ey, ez, Bi.y, Bi.z, Bi.w), ewj = dotf(ex, ey, ez, Bj.y, Bj.z, Bj.w);
+        const double exi = dotf(ex, ey, ez, Ai.z, Ai.w, Bi.x), exj = dotf(ex, ey, ez, Aj.z, Aj.w, Bj.x);
+        Bi_ = fma(ewi, e_dE, fma(exi, e_dR, Bi_));
+        Bj_ = Bj_ - fma(ewj, e_dE, exj * e_dR);
+        Vix = fma(e_dE, Bi.y, fma(e_dR, Ai.z, Vix));
+        Viy = fma(e_dE, Bi.z, fma(e_dR, Ai.w, Viy));
+        Viz = fma(e_dE, Bi.w, fma(e_dR, Bi.x, Viz));
+        Vjx = fma(e_dE, Bj.y, fma(e_dR, Aj.z, Vjx));
+        Vjy = fma(e_dE, Bj.z, fma(e_dR, Aj.w, Vjy));
+        Vjz = fma(e_dE, Bj.w, fma(e_dR, Bj.x, Vjz));
+        const double eWd = fma(Pi, ewi, -Pj * ewj), eXd = fma(Pi, exi, -Pj * exj);
+        gx = fma(dEx, eWd, fma(dRx, eXd, gx));
+        gy = fma(dEy, eWd, fma(dRy, eXd, gy));
+        gz = fma(dEz, eWd, fma(dRz, eXd, gz));
       }
-      const double s2 = ai * Bi_ * Hpij + aj * Bj_ * Hpji + Wi.w * gjd + Wj.w * gid;
-      gx += 2.0 * s2 * ex;
-      gy += 2.0 * s2 * ey;
-      gz += 2.0 * s2 * ez;
-      gxx -= gx;  // e = x_j - x_i
-      gxy -= gy;
-      gxz -= gz;
-      gvx += ex * eOd;
-      gvy += ey * eOd;
-      gvz += ez * eOd;
-      const double cS = ai * Bi_ / r2 + Wi.w;
+      gx = fma(Pi, Vix, fma(-Pj, Vjx, gx));
+      gy = fma(Pi, Viy, fma(-Pj, Vjy, gy));
+      gz = fma(Pi, Viz, fma(-Pj, Vjz, gz));
+      const double aBi = ai * Bi_;
+      const double s2 = 2.0 * fma(aBi, Hpij, fma(aj * Bj_, Hpji, fma(Wi.w, gjd, Wj.w * gid)));
+      gxx -= fma(s2, ex, gx);  // e = x_j - x_i
+      gxy -= fma(s2, ey, gy);
+      gxz -= fma(s2, ez, gz);
+      gvx = fma(ex, eOd, gvx);
+      gvy = fma(ey, eOd, gvy);
+      gvz = fma(ez, eOd, gvz);
+      const double cS = fma(aBi, rinv, Wi.w);
       const int slot = 4 * (ej * P.n_rho + idx);
+      const double c2 = cS * r2, c4 = c2 * r2;
       if (RMODE == 0) {
         s_p[(slot + 0) * nt + t] += cS;
-        s_p[(slot + 1) * nt + t] += cS * r2;
-        s_p[(slot + 2) * nt + t] += cS * r2 * r2;
-        s_p[(slot + 3) * nt + t] += cS * r2 * r2 * r2;
+        s_p[(slot + 1) * nt + t] += c2;
+        s_p[(slot + 2) * nt + t] += c4;
+        s_p[(slot + 3) * nt + t] = fma(c4, r2, s_p[(slot + 3) * nt + t]);
       } else {
         atomicAdd(gglob + slot + 0, cS);
-        atomicAdd(gglob + slot + 1, cS * r2);
-        atomicAdd(gglob + slot + 2, cS * r2 * r2);
-        atomicAdd(gglob + slot + 3, cS * r2 * r2 * r2);
+        atomicAdd(gglob + slot + 1, c2);
+        atomicAdd(gglob + slot + 2, c4);
+        atomicAdd(gglob + slot + 3, c4 * r2);
       }
     }
     const bool integ = !(P.flags & 0x08);
@@ -535,9 +582,9 @@ __global__ void __launch_bounds__(ABLOCK)
     const double xbx = X.x + gxx, xby = X.y + gxy, xbz = X.z + gxz;
     double vbx = V.x + gvx, vby = V.y + gvy, vbz = V.z + gvz;
     if (integ) {
-      vbx += P.dtv * xbx;
-      vby += P.dtv * xby;
-      vbz += P.dtv * xbz;
+      vbx = fma(P.dtv, xbx, vbx);
+      vby = fma(P.dtv, xby, vby);
+      vbz = fma(P.dtv, xbz, vbz);
     }
     const double dtfm = integ ? P.dtfm[type[i]] : 0.0;
     xb[i] = D4{xbx, xby, xbz, 0.0};
@@ -549,12 +596,12 @@ __global__ void __launch_bounds__(ABLOCK)
     for (int q = t; q < nt4; q += nt) {
       double sum = 0.0;
       for (int tt = 0; tt < nt; ++tt) sum += s_p[q * nt + tt];
-      gpart[(size_t)blockIdx.x * nt4 + q] = sum;
+      gpart[(size_t)blockIdx.x * nt4 + q] += sum;
     }
   }
 }
 
-// add the block partials of one step to the running gradient, in block order
+// sum of the blocks' partial rows, in block order
 __global__ void k_adj_reduce(const double *__restrict__ gpart, int nparts, int nt4, double *__restrict__ acc) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nt4) return;
@@ -596,6 +643,7 @@ struct eph_adjoint {
   // adjoint state and work arrays
   DevBuf<D4> xb, vb, fb, cE, cR, W;
   DevBuf<double> Tb, u0, u1, srcbar, gC, gK, rho_e;
+  DevBuf<double> fdmW;  // [7][ncells]: transposed substep stencil, see k_adj_fdm_weights
   DevBuf<double> g_rho, g_alpha, part_rho, part_alpha;
   DevBuf<double> tbc;     // per atom: contribution to the grid's cotangent
   DevBuf<U128> tb_acc;    // per cell: its exact sum
@@ -627,9 +675,12 @@ struct eph_adjoint {
     bool fext = false;
   };
   bool use_graph = true;
-  cudaGraphExec_t fwd_exec = nullptr, bwd_exec = nullptr;
-  Shape fwd_shape, bwd_shape;
-  long fwd_graph_launches = 0, bwd_graph_launches = 0;
+  // passes: 0 forward (records the last segment as it goes), 1 backward that
+  // recomputes every segment, 2 backward that finds the last segment recorded
+  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+  Shape shape[3];
+  long graph_launches[3] = {0, 0, 0};
+  bool last_recorded = false;  // the record slots hold the last segment of the trajectory
 };
 
 namespace {
@@ -741,6 +792,26 @@ Slot slot_view(eph_adjoint *a, int s) {
   return S;
 }
 
+GridArgs grid_args(eph_adjoint *a) {
+  const eph_ctx *c = a->c;
+  const Grid &g = c->grid;
+  GridArgs G;
+  G.n[0] = g.nx;
+  G.n[1] = g.ny;
+  G.n[2] = g.nz;
+  G.nc = a->nc;
+  G.h[0] = g.dx;
+  G.h[1] = g.dy;
+  G.h[2] = g.dz;
+  G.inner_dt = c->inner_dt;
+  G.kappa = c->kappa.p;
+  G.rhoC = c->rhoC.p;
+  G.rho_e = a->rho_e.p;
+  G.S = c->S.p;
+  G.flag = c->gflag.p;
+  return G;
+}
+
 template <bool FAST>
 void launch_sweeps(eph_adjoint *a, const Slot &S) {
   eph_ctx *c = a->c;
@@ -753,10 +824,6 @@ void launch_sweeps(eph_adjoint *a, const Slot &S) {
     k_adj_sweep1<FAST, 1><<<nb, ABLOCK, 0, c->stream>>>(c->P, S, c->mask.p, a->cE.p, a->cR.p, a->W.p,
                                                          a->part_alpha.p, a->g_alpha.p, a->nt4_alpha);
   a->launches += 1;
-  if (a->amode == 0) {
-    k_adj_reduce<<<nb_of(a->nt4_alpha), ABLOCK, 0, c->stream>>>(a->part_alpha.p, nb, a->nt4_alpha, a->g_alpha.p);
-    a->launches += 1;
-  }
   const size_t sh2 = a->rmode == 0 ? sizeof(double) * (size_t)a->nt4_rho * ABLOCK : 0;
 #define ADJ_SWEEP2(M, R)                                                                                    \
   k_adj_sweep2<FAST, M, R><<<nb, ABLOCK, sh2, c->stream>>>(c->P, S, c->mask.p, c->type.p, a->cE.p, a->cR.p, \
@@ -771,49 +838,32 @@ void launch_sweeps(eph_adjoint *a, const Slot &S) {
   }
 #undef ADJ_SWEEP2
   a->launches += 1;
-  if (a->rmode == 0) {
-    k_adj_reduce<<<nb_of(a->nt4_rho), ABLOCK, 0, c->stream>>>(a->part_rho.p, nb, a->nt4_rho, a->g_rho.p);
-    a->launches += 1;
-  }
 }
 
 // reverse of the recorded step in slot s; eb, tau: device addresses of
 // dL/dE and dL/dT_mean / ncells of the step
 int reverse_step(eph_adjoint *a, int s, const double *eb, const double *tau) {
   eph_ctx *c = a->c;
-  const Grid &g = c->grid;
   const long nc = a->nc;
   const int gb = nb_of(nc, 64);
   const double *src = a->r_src.p + (size_t)s * nc;
   if (a->fdm) {
-    GridArgs G;
-    G.n[0] = g.nx;
-    G.n[1] = g.ny;
-    G.n[2] = g.nz;
-    G.nc = nc;
-    G.h[0] = g.dx;
-    G.h[1] = g.dy;
-    G.h[2] = g.dz;
-    G.inner_dt = c->inner_dt;
-    G.kappa = c->kappa.p;
-    G.rhoC = c->rhoC.p;
-    G.rho_e = a->rho_e.p;
-    G.S = c->S.p;
-    G.flag = c->gflag.p;
+    const GridArgs G = grid_args(a);
     const unsigned ns = a->nsub;
     // grid at the start of substep m of this step
     auto Tat = [&](unsigned m) -> const double * {
       return m == 0 ? a->r_T0.p + (size_t)s * nc : a->r_Tsub.p + ((size_t)s * ns + (m - 1)) * (size_t)nc;
     };
     double *ub[2] = {a->u0.p, a->u1.p};
-    k_adj_fdm_first<<<gb, 64, 0, c->stream>>>(G, Tat(ns - 1), src, a->Tb.p, tau, ub[0], a->srcbar.p, a->gC.p,
-                                              a->gK.p);
+    const int gb32 = nb_of(nc, 32);  // small grids: spread the cells over more SMs
+    k_adj_fdm_first<<<gb32, 32, 0, c->stream>>>(G, Tat(ns - 1), src, a->Tb.p, tau, ub[0], a->srcbar.p, a->gC.p,
+                                                a->gK.p);
     a->launches += 1;
     int cur = 0;
     for (int k = (int)ns - 1; k >= 0; --k) {
       const double *Tprev = k >= 1 ? Tat((unsigned)k - 1) : nullptr;
-      k_adj_fdm_back<<<gb, 64, 0, c->stream>>>(G, ub[cur], Tprev, src, ub[cur ^ 1], a->Tb.p, a->srcbar.p, a->gC.p,
-                                               a->gK.p);
+      k_adj_fdm_back<<<gb32, 32, 0, c->stream>>>(G, a->fdmW.p, ub[cur], Tprev, src, ub[cur ^ 1], a->Tb.p,
+                                                 a->srcbar.p, a->gC.p, a->gK.p);
       a->launches += 1;
       cur ^= 1;
     }
@@ -873,10 +923,12 @@ bool same_shape(const eph_adjoint::Shape &x, const eph_adjoint::Shape &y) {
 }
 
 // the forward pass: from the start state, nsteps plain steps with a
-// checkpoint every K steps and E, T_mean of each step
+// checkpoint every K steps and E, T_mean of each step; the steps of the last
+// segment are recorded as they run (the backward pass starts there)
 int issue_forward(eph_adjoint *a, long nsteps) {
   eph_ctx *c = a->c;
   const size_t N = (size_t)a->n, nc = (size_t)a->nc;
+  const long last0 = ((nsteps - 1) / a->K) * a->K;
   int r;
   if ((r = load_state(a, a->s_x.p, a->s_v.p, a->s_f.p, a->s_xh.p, a->s_T.p, a->s_step.p))) return r;
   for (long t = 0; t < nsteps; ++t) {
@@ -886,7 +938,7 @@ int issue_forward(eph_adjoint *a, long nsteps) {
                           a->k_T.p + k * nc, a->k_step.p + k)))
         return r;
     }
-    if ((r = run_step(a, -1))) return r;
+    if ((r = run_step(a, t >= last0 ? (int)(t - last0) : -1))) return r;
     if (a->fric || a->rand) ADJ_TRY(a, d2d(a->d_E.p + t, c->scal.p + 1, 1, c->stream));
     else ADJ_TRY(a, cudaMemsetAsync(a->d_E.p + t, 0, sizeof(double), c->stream));
     k_adj_mean<<<1, 256, 0, c->stream>>>(c->T0.p, a->nc, a->d_Tm.p + t);
@@ -896,8 +948,9 @@ int issue_forward(eph_adjoint *a, long nsteps) {
   return EPH_OK;
 }
 
-// the backward pass over the last trajectory, cotangents in d_eb / d_tau
-int issue_backward(eph_adjoint *a) {
+// the backward pass over the last trajectory, cotangents in d_eb / d_tau;
+// skip_last: the last segment is still recorded from the forward pass
+int issue_backward(eph_adjoint *a, bool skip_last) {
   eph_ctx *c = a->c;
   const size_t N = (size_t)a->n, nc = (size_t)a->nc;
   int r;
@@ -907,31 +960,53 @@ int issue_backward(eph_adjoint *a) {
   ADJ_TRY(a, cudaMemsetAsync(a->g_rho.p, 0, sizeof(double) * (size_t)a->nt4_rho, c->stream));
   ADJ_TRY(a, cudaMemsetAsync(a->g_alpha.p, 0, sizeof(double) * (size_t)a->nt4_alpha, c->stream));
   ADJ_TRY(a, cudaMemsetAsync(a->tb_exp.p, 0, sizeof(int) * (size_t)a->nsteps, c->stream));
+  const int nb = nb_of(a->n);
+  if (a->rmode == 0)
+    ADJ_TRY(a, cudaMemsetAsync(a->part_rho.p, 0, sizeof(double) * (size_t)nb * a->nt4_rho, c->stream));
+  if (a->amode == 0)
+    ADJ_TRY(a, cudaMemsetAsync(a->part_alpha.p, 0, sizeof(double) * (size_t)nb * a->nt4_alpha, c->stream));
+  if (a->fdm) {
+    k_adj_fdm_weights<<<nb_of(a->nc, 64), 64, 0, c->stream>>>(grid_args(a), a->fdmW.p);
+    a->launches += 1;
+  }
   const long nseg = (a->nsteps + a->K - 1) / a->K;
   for (long seg = nseg - 1; seg >= 0; --seg) {
     const long t0 = seg * a->K, t1 = std::min(t0 + a->K, a->nsteps);
-    if ((r = load_state(a, a->k_x.p + seg * N, a->k_v.p + seg * N, a->k_f.p + seg * N, a->k_xh.p + seg * N,
-                        a->k_T.p + seg * nc, a->k_step.p + seg)))
-      return r;
-    for (long t = t0; t < t1; ++t)
-      if ((r = run_step(a, (int)(t - t0)))) return r;
+    if (!(skip_last && seg == nseg - 1)) {
+      if ((r = load_state(a, a->k_x.p + seg * N, a->k_v.p + seg * N, a->k_f.p + seg * N, a->k_xh.p + seg * N,
+                          a->k_T.p + seg * nc, a->k_step.p + seg)))
+        return r;
+      for (long t = t0; t < t1; ++t)
+        if ((r = run_step(a, (int)(t - t0)))) return r;
+    }
     for (long t = t1 - 1; t >= t0; --t)
       if ((r = reverse_step(a, (int)(t - t0), a->d_eb.p + t, a->d_tau.p + t))) return r;
   }
+  // the blocks' partial rows of the table-coefficient gradients, once per pass
+  if (a->amode == 0) {
+    k_adj_reduce<<<nb_of(a->nt4_alpha), ABLOCK, 0, c->stream>>>(a->part_alpha.p, nb, a->nt4_alpha, a->g_alpha.p);
+    a->launches += 1;
+  }
+  if (a->rmode == 0) {
+    k_adj_reduce<<<nb_of(a->nt4_rho), ABLOCK, 0, c->stream>>>(a->part_rho.p, nb, a->nt4_rho, a->g_rho.p);
+    a->launches += 1;
+  }
+  ADJ_TRY(a, cudaGetLastError());
   return EPH_OK;
 }
 
 // Run a pass: replay its graph, capturing it first when none fits; or issue
 // it directly.  The context's profiling is off meanwhile (its event marks
 // cannot live inside a graph).
-int run_pass(eph_adjoint *a, bool backward, long nsteps, cudaEvent_t e0, cudaEvent_t e1) {
+int run_pass(eph_adjoint *a, int pass, long nsteps, cudaEvent_t e0, cudaEvent_t e1) {
   eph_ctx *c = a->c;
   const bool prof = c->profiling;
   c->profiling = false;
   int r = EPH_OK;
-  cudaGraphExec_t &ex = backward ? a->bwd_exec : a->fwd_exec;
-  eph_adjoint::Shape &sh = backward ? a->bwd_shape : a->fwd_shape;
-  long &gl = backward ? a->bwd_graph_launches : a->fwd_graph_launches;
+  cudaGraphExec_t &ex = a->exec[pass];
+  eph_adjoint::Shape &sh = a->shape[pass];
+  long &gl = a->graph_launches[pass];
+  auto issue = [&]() { return pass == 0 ? issue_forward(a, nsteps) : issue_backward(a, pass == 2); };
   if (a->use_graph) {
     const eph_adjoint::Shape now = shape_now(a, nsteps);
     if (!ex || !same_shape(sh, now)) {
@@ -941,7 +1016,7 @@ int run_pass(eph_adjoint *a, bool backward, long nsteps, cudaEvent_t e0, cudaEve
       cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) r = afail(a, EPH_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
       if (!r) {
-        r = backward ? issue_backward(a) : issue_forward(a, nsteps);
+        r = issue();
         cudaGraph_t g = nullptr;
         e = cudaStreamEndCapture(c->stream, &g);
         if (!r && e != cudaSuccess) r = afail(a, EPH_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e));
@@ -966,7 +1041,7 @@ int run_pass(eph_adjoint *a, bool backward, long nsteps, cudaEvent_t e0, cudaEve
   } else {
     a->launches = 0;
     cudaEventRecord(e0, c->stream);
-    r = backward ? issue_backward(a) : issue_forward(a, nsteps);
+    r = issue();
     cudaEventRecord(e1, c->stream);
   }
   c->profiling = prof;
@@ -1018,6 +1093,7 @@ int eph_adjoint_create(eph_ctx *c, int checkpoint_every, eph_adjoint **out) {
     ADJ_TRY(a, b->alloc(N));
   for (DevBuf<double> *b : {&a->s_T, &a->Tb, &a->u0, &a->u1, &a->srcbar, &a->gC, &a->gK, &a->rho_e})
     ADJ_TRY(a, b->alloc(nc));
+  ADJ_TRY(a, a->fdmW.alloc(7 * nc));
   ADJ_TRY(a, a->s_step.alloc(1));
   ADJ_TRY(a, a->tbc.alloc(N));
   ADJ_TRY(a, a->tb_acc.alloc(nc));
@@ -1056,8 +1132,8 @@ void eph_adjoint_destroy(eph_adjoint *a) {
   // waits for the device's outstanding work)
   for (cudaEvent_t e : a->ev)
     if (e) cudaEventDestroy(e);
-  if (a->fwd_exec) cudaGraphExecDestroy(a->fwd_exec);
-  if (a->bwd_exec) cudaGraphExecDestroy(a->bwd_exec);
+  for (cudaGraphExec_t e : a->exec)
+    if (e) cudaGraphExecDestroy(e);
   if (a->h_cot) cudaFreeHost(a->h_cot);
   delete a;
 }
@@ -1081,7 +1157,10 @@ int eph_adjoint_forward(eph_adjoint *a, long nsteps, double *E, double *T_mean) 
     a->nck = nseg;
   }
   if ((r = ensure(a, a->d_E, (size_t)nsteps)) || (r = ensure(a, a->d_Tm, (size_t)nsteps))) return r;
-  if ((r = run_pass(a, false, nsteps, a->ev[0], a->ev[1]))) return r;
+  if (c->nsub != a->nsub || !a->r_x1.p)
+    if ((r = ensure_records(a))) return r;
+  a->last_recorded = false;
+  if ((r = run_pass(a, 0, nsteps, a->ev[0], a->ev[1]))) return r;
   if (E) ADJ_TRY(a, cudaMemcpyAsync(E, a->d_E.p, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, c->stream));
   if (T_mean)
     ADJ_TRY(a, cudaMemcpyAsync(T_mean, a->d_Tm.p, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, c->stream));
@@ -1092,6 +1171,7 @@ int eph_adjoint_forward(eph_adjoint *a, long nsteps, double *E, double *T_mean) 
   a->fwd_launches = a->launches;
   a->nsteps = nsteps;
   a->have_grad = false;
+  a->last_recorded = true;
   return EPH_OK;
 }
 
@@ -1122,7 +1202,10 @@ int eph_adjoint_backward(eph_adjoint *a, const double *dL_dE, const double *dL_d
   }
   ADJ_TRY(a, cudaMemcpyAsync(a->d_eb.p, a->h_cot, sizeof(double) * ns, cudaMemcpyHostToDevice, c->stream));
   ADJ_TRY(a, cudaMemcpyAsync(a->d_tau.p, a->h_cot + ns, sizeof(double) * ns, cudaMemcpyHostToDevice, c->stream));
-  if ((r = run_pass(a, true, ns, a->ev[2], a->ev[3]))) return r;
+  const bool skip_last = a->last_recorded && c->nsub == a->nsub;
+  if ((r = run_pass(a, skip_last ? 2 : 1, ns, a->ev[2], a->ev[3]))) return r;
+  // the records now hold the first segment (or still the last, if only one)
+  a->last_recorded = (ns + a->K - 1) / a->K == 1 && skip_last;
   unsigned herr = 0;
   ADJ_TRY(a, cudaMemcpyAsync(&herr, a->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
   // chain the coefficient gradients to the knot columns on the host
