@@ -374,6 +374,82 @@ def run_adjoint(args, dev, fd=True):
         return res
 
 
+def run_adjoint_fit(args, dev):
+    """Batched adjoint fitting (a reduced form of the 128-replica fitting
+    workload; sizes in `config`): replicas of 16k-64k atoms (whole fcc cells),
+    initial T_e uniform in 1,000-5,000 K, 16^3 grids, 1 fs steps; target mean-T_e
+    curves made by the plain method with a hidden beta(rho) (64 knots, positive,
+    smooth); Adam on the shared log(beta) knots from a flat guess, every
+    iteration one batched forward and one batched backward graph."""
+    import ephgb
+    from ephgb import workloads as W
+    from ephgb.adjoint import Adjoint, AdjointBatch, GRAD_BETA_KNOTS, fit_beta_batch
+
+    R, nsteps, iters = args.fit_replicas, args.fit_steps, args.fit_iters
+    rng = np.random.default_rng(SEED + 11)
+    drho = 0.005
+    kn = np.arange(64) * drho
+    hidden = 0.02 + 2.0 * kn * kn + 0.01 * (1.0 + np.sin(kn / 0.03))
+    with tempfile.TemporaryDirectory() as wd:
+        bf = W.write_beta_file(os.path.join(wd, "fit.beta"), n_rho=16, n_beta=64, drho=drho,
+                               beta_fn=lambda r: np.interp(r, kn, hidden))
+        fixes, adjs, atoms_total = [], [], 0
+        for r in range(R):
+            cells = int(rng.integers(16, 26))  # 4 n^3 = 16,384 .. 62,500 atoms
+            at = W.fcc_lattice(cells, seed=SEED + 100 + r)
+            atoms_total += at.n
+            words = W.fix_args(bf, seed=SEED + r, flags=7, T_e=float(rng.uniform(1000.0, 5000.0)), grid=(16, 16, 16))
+            fix = ephgb.FixEPH(words, at, dt=ADJ_DT, mode=ephgb.MODE_FAST, device=dev)
+            fixes.append(fix)
+            adjs.append(Adjoint(fix, checkpoint_every=ADJ_K))
+        batch = AdjointBatch(adjs)
+        _, target = batch.forward(nsteps)
+        beta0 = np.full(64, hidden.mean())
+        # the knots the replicas' densities reach (non-zero gradient at the start)
+        for a in adjs:
+            a.set_knots(0, None, beta0)
+        _, T = batch.forward(nsteps)
+        batch.backward(None, T - target)
+        g0 = sum(a.gradient(GRAD_BETA_KNOTS) for a in adjs)
+        seen = np.abs(g0) > 1e-12 * np.abs(g0).max()
+        # where the atoms' densities lie: weight of each knot interval
+        rho = np.concatenate([f.get("rho") for f in fixes])
+        hist_w = np.bincount(np.clip((rho / drho).astype(int), 0, 63), minlength=64).astype(float)
+        hist_w /= hist_w.sum()
+        t0 = time.perf_counter()
+        beta, hist = fit_beta_batch(batch, nsteps, target, beta0, iters=iters, lr=0.05)
+        wall = time.perf_counter() - t0
+        tb = batch.timing()
+        # the same passes replica after replica (each its own graphs)
+        for a in adjs:
+            a.set_knots(0, None, beta)
+        t1 = time.perf_counter()
+        for a in adjs:
+            E1, T1 = a.forward(nsteps)
+            a.backward(None, T1 - target[adjs.index(a)])
+        seq = time.perf_counter() - t1
+
+        def err(b):
+            return float(np.linalg.norm((b - hidden)[seen]) / np.linalg.norm(hidden[seen]))
+
+        def werr(b):  # weighted by the share of atoms in each knot interval
+            return float(np.sqrt((hist_w * (b - hidden) ** 2).sum() / (hist_w * hidden ** 2).sum()))
+
+        return {"workload": f"{R} replicas, {atoms_total:,} atoms in all (16k-64k each), T_e0 1,000-5,000 K, FDM 16^3, "
+                            f"{nsteps} steps of 1 fs; 64 shared beta knots, Adam on log(beta), {iters} iterations, "
+                            "flat initial guess",
+                "loss_first": hist[0], "loss_last": hist[-1], "beta_rel_l2_err_initial": err(beta0),
+                "beta_rel_l2_err_final": err(beta), "knots_constrained": int(seen.sum()),
+                "beta_rel_err_density_weighted_initial": werr(beta0),
+                "beta_rel_err_density_weighted_final": werr(beta),
+                "knots_holding_atoms": int((hist_w > 0).sum()), "smoothness_weight": 10.0,
+                "wall_s_per_iteration": wall / iters, "batched_forward_ms": tb["forward_ms"],
+                "batched_backward_ms": tb["backward_ms"],
+                "sequential_forward_plus_backward_s": seq,
+                "batched_speedup_vs_sequential": seq / ((tb["forward_ms"] + tb["backward_ms"]) / 1000.0),
+                "atom_steps_per_s_forward": atoms_total * nsteps / (tb["forward_ms"] / 1000.0)}
+
+
 def cpu_baseline(threads, steps=1, warm=1):
     """The CPU restatement (oracle port) on the same workload: `steps` steps
     of the full system after `warm` warm-up steps; time of the fix's own hooks
@@ -411,6 +487,11 @@ def main():
     ap.add_argument("--only-adjoint", action="store_true", help="run the adjoint leg alone (profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=ADJ_STEPS)
     ap.add_argument("--no-adjoint-fd", action="store_true", help="skip the finite-difference check")
+    ap.add_argument("--no-fit", action="store_true", help="omit the batched adjoint fitting leg")
+    ap.add_argument("--only-fit", action="store_true", help="run the batched adjoint fitting leg alone")
+    ap.add_argument("--fit-replicas", type=int, default=16)
+    ap.add_argument("--fit-steps", type=int, default=100)
+    ap.add_argument("--fit-iters", type=int, default=30)
     ap.add_argument("--cells", type=int, default=CELLS, help="fcc cells per edge (profiling cases)")
     ap.add_argument("--grid", type=int, default=GRID[0], help="FDM cells per edge (profiling cases)")
     args = ap.parse_args()
@@ -442,6 +523,9 @@ def main():
 
     import torch
 
+    if args.only_fit:
+        print(json.dumps(run_adjoint_fit(args, int(os.environ.get("LOCAL_RANK", rank)))))
+        return
     if args.only_adjoint:
         print(json.dumps(run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)), fd=not args.no_adjoint_fd)))
         return
@@ -486,6 +570,8 @@ def main():
             line["batched"]["value"] = float(t.item())
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)), fd=not args.no_adjoint_fd)
+    if rank == 0 and not args.no_fit:
+        line["adjoint_fit"] = run_adjoint_fit(args, int(os.environ.get("LOCAL_RANK", rank)))
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(threads, steps=1, warm=1).items() if k != "seconds"}
     if rank == 0:

@@ -299,6 +299,20 @@ int eph_adjoint_set_graph(eph_adjoint *adj, int on);
 int eph_adjoint_timing(eph_adjoint *adj, double *forward_ms, double *backward_ms, long *forward_launches,
                        long *backward_launches);
 
+/* Several adjoints (of contexts on one device) run together: each pass of
+ * every adjoint is a parallel branch of one CUDA graph, so many small
+ * replicas fill the GPU (batched fitting).  The batch does not own the
+ * adjoints.  E, T_mean, dL_dE, dL_dT_mean: nadj x nsteps, row per adjoint
+ * (NULL allowed); the gradients are read per adjoint with eph_adjoint_gradient. */
+typedef struct eph_adjoint_batch eph_adjoint_batch;
+int eph_adjoint_batch_create(int nadj, eph_adjoint *const *adj, eph_adjoint_batch **out);
+void eph_adjoint_batch_destroy(eph_adjoint_batch *batch);
+const char *eph_adjoint_batch_last_error(const eph_adjoint_batch *batch);
+int eph_adjoint_batch_forward(eph_adjoint_batch *batch, long nsteps, double *E, double *T_mean);
+int eph_adjoint_batch_backward(eph_adjoint_batch *batch, const double *dL_dE, const double *dL_dT_mean);
+int eph_adjoint_batch_timing(eph_adjoint_batch *batch, double *forward_ms, double *backward_ms,
+                             long *forward_launches, long *backward_launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -287,3 +287,33 @@ def test_autograd_function_and_fitting_harness(built, tmp_path):
     assert float(ce.grad) == pytest.approx(g["C_e"], rel=1e-12)
     _, hist = fit_beta(adj, STEPS, target, b0, iters=15, lr=0.05)
     assert hist[-1] < 0.5 * hist[0]
+
+
+def test_batch_equals_the_adjoints_run_alone(built, tmp_path):
+    """Three replicas of different sizes and electron temperatures: the
+    batched passes (one graph each) give every replica's trajectory and
+    gradient bit for bit as its adjoint run alone."""
+    from ephgb.adjoint import AdjointBatch
+
+    beta = W.write_beta_file(str(tmp_path / "b.beta"), n_rho=16, n_beta=24, drho=0.3 / 23, beta_fn=curved_beta)
+    reps = []
+    for k, (cells, T_e) in enumerate(((4, 1500.0), (5, 2500.0), (6, 3500.0))):
+        at = W.fcc_lattice(cells, seed=40 + k)
+        words = W.fix_args(beta, seed=100 + k, flags=7, T_e=T_e, grid=(4, 4, 4))
+        fix = ephgb.FixEPH(words, atoms=at, dt=0.001)
+        reps.append((fix, Adjoint(fix, checkpoint_every=4)))
+    alone = []
+    for fix, adj in reps:
+        E, T = adj.forward(STEPS)
+        wE, wT = weights(E, T, seed=len(alone))
+        alone.append((E, T, wE, wT, adjoint_grads(adj, wE, wT)))
+    batch = AdjointBatch([adj for _, adj in reps])
+    for _ in range(2):  # capture, then replay
+        E, T = batch.forward(STEPS)
+        batch.backward(np.stack([a[2] for a in alone]), np.stack([a[3] for a in alone]))
+        for r, (fix, adj) in enumerate(reps):
+            np.testing.assert_array_equal(E[r], alone[r][0])
+            np.testing.assert_array_equal(T[r], alone[r][1])
+            g = adj.gradients(0)
+            for k in g:
+                np.testing.assert_array_equal(np.asarray(g[k]), np.asarray(alone[r][4][k]), err_msg=k)

@@ -1063,6 +1063,111 @@ int ensure_records(eph_adjoint *a) {
   return EPH_OK;
 }
 
+// ---------------------------------------------------------- pass pieces
+
+// checks and allocations of a forward pass
+int fwd_prepare(eph_adjoint *a, long nsteps) {
+  eph_ctx *c = a->c;
+  if (c->n != a->n || c->kcap != a->kcap)
+    return afail(a, EPH_ERR_STATE, "the context's atoms changed since the adjoint was created");
+  ADJ_TRY(a, cudaSetDevice(c->device));
+  const long nseg = (nsteps + a->K - 1) / a->K;
+  const size_t N = (size_t)a->n, nc = (size_t)a->nc;
+  int r;
+  if (nseg > a->nck) {
+    a->own_gen += 1;
+    for (DevBuf<D4> *b : {&a->k_x, &a->k_v, &a->k_f, &a->k_xh}) ADJ_TRY(a, b->alloc((size_t)nseg * N));
+    ADJ_TRY(a, a->k_T.alloc((size_t)nseg * nc));
+    ADJ_TRY(a, a->k_step.alloc((size_t)nseg));
+    a->nck = nseg;
+  }
+  if ((r = ensure(a, a->d_E, (size_t)nsteps)) || (r = ensure(a, a->d_Tm, (size_t)nsteps))) return r;
+  if (c->nsub != a->nsub || !a->r_x1.p)
+    if ((r = ensure_records(a))) return r;
+  a->last_recorded = false;
+  return EPH_OK;
+}
+
+// after a forward pass on `st`: E and T_mean to the host, device checks
+int fwd_finish(eph_adjoint *a, long nsteps, double *E, double *T_mean, cudaStream_t st) {
+  eph_ctx *c = a->c;
+  int r;
+  if (E) ADJ_TRY(a, cudaMemcpyAsync(E, a->d_E.p, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, st));
+  if (T_mean) ADJ_TRY(a, cudaMemcpyAsync(T_mean, a->d_Tm.p, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, st));
+  ADJ_TRY(a, cudaStreamSynchronize(st));
+  if ((r = ctxi::check_device(c))) return from_ctx(a, r);
+  a->nsteps = nsteps;
+  a->have_grad = false;
+  a->last_recorded = true;
+  return EPH_OK;
+}
+
+// allocations of a backward pass and the cotangents to the device (on `st`)
+int bwd_prepare(eph_adjoint *a, const double *dL_dE, const double *dL_dT_mean, cudaStream_t st, bool *skip_last) {
+  if (a->nsteps < 1) return afail(a, EPH_ERR_STATE, "no trajectory: call eph_adjoint_forward first");
+  eph_ctx *c = a->c;
+  ADJ_TRY(a, cudaSetDevice(c->device));
+  int r;
+  if (c->nsub != a->nsub || !a->r_x1.p)
+    if ((r = ensure_records(a))) return r;
+  const long ns = a->nsteps;
+  if ((r = ensure(a, a->d_eb, (size_t)ns)) || (r = ensure(a, a->d_tau, (size_t)ns)) ||
+      (r = ensure(a, a->tb_exp, (size_t)ns)))
+    return r;
+  if (a->h_cot_n < 2 * ns) {
+    if (a->h_cot) cudaFreeHost(a->h_cot);
+    a->h_cot = nullptr;
+    a->h_cot_n = 0;
+    ADJ_TRY(a, cudaMallocHost(&a->h_cot, sizeof(double) * 2 * (size_t)ns));
+    a->h_cot_n = 2 * ns;
+  }
+  const double inv_nc = 1.0 / (double)a->nc;
+  for (long t = 0; t < ns; ++t) {
+    a->h_cot[t] = dL_dE ? dL_dE[t] : 0.0;
+    a->h_cot[ns + t] = dL_dT_mean ? dL_dT_mean[t] * inv_nc : 0.0;
+  }
+  ADJ_TRY(a, cudaMemcpyAsync(a->d_eb.p, a->h_cot, sizeof(double) * ns, cudaMemcpyHostToDevice, st));
+  ADJ_TRY(a, cudaMemcpyAsync(a->d_tau.p, a->h_cot + ns, sizeof(double) * ns, cudaMemcpyHostToDevice, st));
+  *skip_last = a->last_recorded && c->nsub == a->nsub;
+  return EPH_OK;
+}
+
+// after a backward pass on `st`: gradients to the host, chained to the knots
+int bwd_finish(eph_adjoint *a, bool skip_last, cudaStream_t st) {
+  eph_ctx *c = a->c;
+  const size_t nc = (size_t)a->nc;
+  int r;
+  // the records now hold the first segment (or still the last, if only one)
+  a->last_recorded = (a->nsteps + a->K - 1) / a->K == 1 && skip_last;
+  unsigned herr = 0;
+  const Beta &B = c->beta;
+  std::vector<double> hr((size_t)a->nt4_rho), ha((size_t)a->nt4_alpha), hC(nc), hK(nc);
+  ADJ_TRY(a, cudaMemcpyAsync(&herr, a->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  ADJ_TRY(a, cudaMemcpyAsync(hr.data(), a->g_rho.p, hr.size() * 8, cudaMemcpyDeviceToHost, st));
+  ADJ_TRY(a, cudaMemcpyAsync(ha.data(), a->g_alpha.p, ha.size() * 8, cudaMemcpyDeviceToHost, st));
+  ADJ_TRY(a, cudaMemcpyAsync(hC.data(), a->gC.p, nc * 8, cudaMemcpyDeviceToHost, st));
+  ADJ_TRY(a, cudaMemcpyAsync(hK.data(), a->gK.p, nc * 8, cudaMemcpyDeviceToHost, st));
+  ADJ_TRY(a, cudaStreamSynchronize(st));
+  if ((r = ctxi::check_device(c))) return from_ctx(a, r);
+  if (herr) {
+    cudaMemset(a->d_err.p, 0, sizeof(unsigned));
+    return afail(a, EPH_ERR_RANGE, "device: a grid cotangent sum left the fixed-point range");
+  }
+  a->grad_rho.assign(B.n_elements, std::vector<double>(B.n_rho, 0.0));
+  a->grad_beta.assign(B.n_elements, std::vector<double>(B.n_beta, 0.0));
+  for (int e = 0; e < B.n_elements; ++e)
+    B.knot_gradient(e, hr.data() + (size_t)e * B.n_rho * 4, ha.data() + (size_t)e * B.n_beta * 4,
+                    a->grad_rho[e].data(), a->grad_beta[e].data());
+  a->grad_C = 0.0;
+  a->grad_K = 0.0;
+  for (size_t i = 0; i < nc; ++i) {
+    a->grad_C += hC[i];
+    a->grad_K += hK[i];
+  }
+  a->have_grad = true;
+  return EPH_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1142,100 +1247,28 @@ const char *eph_adjoint_last_error(const eph_adjoint *a) { return a ? a->err.c_s
 
 int eph_adjoint_forward(eph_adjoint *a, long nsteps, double *E, double *T_mean) {
   if (!a || nsteps < 1) return EPH_ERR_ARG;
-  eph_ctx *c = a->c;
-  if (c->n != a->n || c->kcap != a->kcap)
-    return afail(a, EPH_ERR_STATE, "the context's atoms changed since the adjoint was created");
-  ADJ_TRY(a, cudaSetDevice(c->device));
-  const long nseg = (nsteps + a->K - 1) / a->K;
-  const size_t N = (size_t)a->n, nc = (size_t)a->nc;
   int r;
-  if (nseg > a->nck) {
-    a->own_gen += 1;
-    for (DevBuf<D4> *b : {&a->k_x, &a->k_v, &a->k_f, &a->k_xh}) ADJ_TRY(a, b->alloc((size_t)nseg * N));
-    ADJ_TRY(a, a->k_T.alloc((size_t)nseg * nc));
-    ADJ_TRY(a, a->k_step.alloc((size_t)nseg));
-    a->nck = nseg;
-  }
-  if ((r = ensure(a, a->d_E, (size_t)nsteps)) || (r = ensure(a, a->d_Tm, (size_t)nsteps))) return r;
-  if (c->nsub != a->nsub || !a->r_x1.p)
-    if ((r = ensure_records(a))) return r;
-  a->last_recorded = false;
+  if ((r = fwd_prepare(a, nsteps))) return r;
   if ((r = run_pass(a, 0, nsteps, a->ev[0], a->ev[1]))) return r;
-  if (E) ADJ_TRY(a, cudaMemcpyAsync(E, a->d_E.p, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, c->stream));
-  if (T_mean)
-    ADJ_TRY(a, cudaMemcpyAsync(T_mean, a->d_Tm.p, sizeof(double) * nsteps, cudaMemcpyDeviceToHost, c->stream));
-  if ((r = ctxi::check_device(c))) return from_ctx(a, r);
+  if ((r = fwd_finish(a, nsteps, E, T_mean, a->c->stream))) return r;
   float ms = 0.f;
   ADJ_TRY(a, cudaEventElapsedTime(&ms, a->ev[0], a->ev[1]));
   a->fwd_ms = ms;
   a->fwd_launches = a->launches;
-  a->nsteps = nsteps;
-  a->have_grad = false;
-  a->last_recorded = true;
   return EPH_OK;
 }
 
 int eph_adjoint_backward(eph_adjoint *a, const double *dL_dE, const double *dL_dT_mean) {
   if (!a) return EPH_ERR_ARG;
-  if (a->nsteps < 1) return afail(a, EPH_ERR_STATE, "no trajectory: call eph_adjoint_forward first");
-  eph_ctx *c = a->c;
-  ADJ_TRY(a, cudaSetDevice(c->device));
   int r;
-  if (c->nsub != a->nsub || !a->r_x1.p)
-    if ((r = ensure_records(a))) return r;
-  const size_t nc = (size_t)a->nc;
-  const long ns = a->nsteps;
-  if ((r = ensure(a, a->d_eb, (size_t)ns)) || (r = ensure(a, a->d_tau, (size_t)ns)) ||
-      (r = ensure(a, a->tb_exp, (size_t)ns)))
-    return r;
-  if (a->h_cot_n < 2 * ns) {
-    if (a->h_cot) cudaFreeHost(a->h_cot);
-    a->h_cot = nullptr;
-    a->h_cot_n = 0;
-    ADJ_TRY(a, cudaMallocHost(&a->h_cot, sizeof(double) * 2 * (size_t)ns));
-    a->h_cot_n = 2 * ns;
-  }
-  const double inv_nc = 1.0 / (double)a->nc;
-  for (long t = 0; t < ns; ++t) {
-    a->h_cot[t] = dL_dE ? dL_dE[t] : 0.0;
-    a->h_cot[ns + t] = dL_dT_mean ? dL_dT_mean[t] * inv_nc : 0.0;
-  }
-  ADJ_TRY(a, cudaMemcpyAsync(a->d_eb.p, a->h_cot, sizeof(double) * ns, cudaMemcpyHostToDevice, c->stream));
-  ADJ_TRY(a, cudaMemcpyAsync(a->d_tau.p, a->h_cot + ns, sizeof(double) * ns, cudaMemcpyHostToDevice, c->stream));
-  const bool skip_last = a->last_recorded && c->nsub == a->nsub;
-  if ((r = run_pass(a, skip_last ? 2 : 1, ns, a->ev[2], a->ev[3]))) return r;
-  // the records now hold the first segment (or still the last, if only one)
-  a->last_recorded = (ns + a->K - 1) / a->K == 1 && skip_last;
-  unsigned herr = 0;
-  ADJ_TRY(a, cudaMemcpyAsync(&herr, a->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-  // chain the coefficient gradients to the knot columns on the host
-  const Beta &B = c->beta;
-  std::vector<double> hr((size_t)a->nt4_rho), ha((size_t)a->nt4_alpha), hC(nc), hK(nc);
-  ADJ_TRY(a, cudaMemcpyAsync(hr.data(), a->g_rho.p, hr.size() * 8, cudaMemcpyDeviceToHost, c->stream));
-  ADJ_TRY(a, cudaMemcpyAsync(ha.data(), a->g_alpha.p, ha.size() * 8, cudaMemcpyDeviceToHost, c->stream));
-  ADJ_TRY(a, cudaMemcpyAsync(hC.data(), a->gC.p, nc * 8, cudaMemcpyDeviceToHost, c->stream));
-  ADJ_TRY(a, cudaMemcpyAsync(hK.data(), a->gK.p, nc * 8, cudaMemcpyDeviceToHost, c->stream));
-  if ((r = ctxi::check_device(c))) return from_ctx(a, r);
-  if (herr) {
-    cudaMemset(a->d_err.p, 0, sizeof(unsigned));
-    return afail(a, EPH_ERR_RANGE, "device: a grid cotangent sum left the fixed-point range");
-  }
+  bool skip_last = false;
+  if ((r = bwd_prepare(a, dL_dE, dL_dT_mean, a->c->stream, &skip_last))) return r;
+  if ((r = run_pass(a, skip_last ? 2 : 1, a->nsteps, a->ev[2], a->ev[3]))) return r;
+  if ((r = bwd_finish(a, skip_last, a->c->stream))) return r;
   float ms = 0.f;
   ADJ_TRY(a, cudaEventElapsedTime(&ms, a->ev[2], a->ev[3]));
   a->bwd_ms = ms;
   a->bwd_launches = a->launches;
-  a->grad_rho.assign(B.n_elements, std::vector<double>(B.n_rho, 0.0));
-  a->grad_beta.assign(B.n_elements, std::vector<double>(B.n_beta, 0.0));
-  for (int e = 0; e < B.n_elements; ++e)
-    B.knot_gradient(e, hr.data() + (size_t)e * B.n_rho * 4, ha.data() + (size_t)e * B.n_beta * 4,
-                    a->grad_rho[e].data(), a->grad_beta[e].data());
-  a->grad_C = 0.0;
-  a->grad_K = 0.0;
-  for (size_t i = 0; i < nc; ++i) {
-    a->grad_C += hC[i];
-    a->grad_K += hK[i];
-  }
-  a->have_grad = true;
   return EPH_OK;
 }
 
@@ -1277,6 +1310,180 @@ int eph_adjoint_timing(eph_adjoint *a, double *forward_ms, double *backward_ms, 
   if (backward_ms) *backward_ms = a->bwd_ms;
   if (forward_launches) *forward_launches = a->fwd_launches;
   if (backward_launches) *backward_launches = a->bwd_launches;
+  return EPH_OK;
+}
+
+// ----------------------------------------------------------- batched passes
+
+struct eph_adjoint_batch {
+  std::vector<eph_adjoint *> a;
+  cudaStream_t main = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+  std::vector<eph_adjoint::Shape> shape[3];
+  long graph_launches[3] = {0, 0, 0};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double fwd_ms = 0.0, bwd_ms = 0.0;
+  long fwd_launches = 0, bwd_launches = 0;
+  std::string err;
+};
+
+static int bfail(eph_adjoint_batch *b, int code, const std::string &msg) {
+  b->err = msg;
+  return code;
+}
+
+// One pass of every adjoint as parallel branches of one graph launched on
+// b->main (fork event -> each context's stream -> join events).
+static int batch_pass(eph_adjoint_batch *b, int pass, long nsteps, cudaEvent_t e0, cudaEvent_t e1) {
+  std::vector<eph_adjoint::Shape> now;
+  for (eph_adjoint *a : b->a) now.push_back(shape_now(a, nsteps));
+  bool fits = b->exec[pass] && b->shape[pass].size() == now.size();
+  for (size_t r = 0; fits && r < now.size(); ++r) fits = same_shape(b->shape[pass][r], now[r]);
+  // work already queued on the contexts' streams comes first
+  for (eph_adjoint *a : b->a)
+    if (cudaStreamSynchronize(a->c->stream) != cudaSuccess) return bfail(b, EPH_ERR_CUDA, "stream synchronise");
+  std::vector<bool> prof;
+  for (eph_adjoint *a : b->a) {
+    prof.push_back(a->c->profiling);
+    a->c->profiling = false;
+  }
+  int rc = EPH_OK;
+  if (!fits) {
+    if (b->exec[pass]) cudaGraphExecDestroy(b->exec[pass]);
+    b->exec[pass] = nullptr;
+    long total = 0;
+    if (cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal) != cudaSuccess ||
+        cudaEventRecord(b->fork, b->main) != cudaSuccess)
+      rc = bfail(b, EPH_ERR_CUDA, "begin capture");
+    for (size_t r = 0; r < b->a.size() && !rc; ++r) {
+      eph_adjoint *a = b->a[r];
+      if (cudaStreamWaitEvent(a->c->stream, b->fork, 0) != cudaSuccess) {
+        rc = bfail(b, EPH_ERR_CUDA, "fork");
+        break;
+      }
+      a->launches = 0;
+      rc = pass == 0 ? issue_forward(a, nsteps) : issue_backward(a, pass == 2);
+      total += a->launches;
+      if (rc) {
+        b->err = "adjoint " + std::to_string(r) + ": " + a->err;
+        break;
+      }
+      if (cudaEventRecord(b->joins[r], a->c->stream) != cudaSuccess ||
+          cudaStreamWaitEvent(b->main, b->joins[r], 0) != cudaSuccess)
+        rc = bfail(b, EPH_ERR_CUDA, "join");
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->main, &g);
+    if (!rc && e != cudaSuccess) rc = bfail(b, EPH_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e));
+    if (!rc && cudaGraphInstantiate(&b->exec[pass], g, 0) != cudaSuccess)
+      rc = bfail(b, EPH_ERR_CUDA, "cannot instantiate the batched graph");
+    if (g) cudaGraphDestroy(g);
+    if (!rc) {
+      b->shape[pass] = now;
+      b->graph_launches[pass] = total;
+    }
+  }
+  if (!rc) {
+    cudaEventRecord(e0, b->main);
+    if (cudaGraphLaunch(b->exec[pass], b->main) != cudaSuccess) rc = bfail(b, EPH_ERR_CUDA, "graph launch");
+    cudaEventRecord(e1, b->main);
+  }
+  for (size_t r = 0; r < b->a.size(); ++r) b->a[r]->c->profiling = prof[r];
+  return rc;
+}
+
+int eph_adjoint_batch_create(int nadj, eph_adjoint *const *adj, eph_adjoint_batch **out) {
+  if (!out || nadj < 1 || !adj) return EPH_ERR_ARG;
+  *out = nullptr;
+  eph_adjoint_batch *b = new (std::nothrow) eph_adjoint_batch();
+  if (!b) return EPH_ERR_ARG;
+  *out = b;
+  for (int r = 0; r < nadj; ++r) {
+    if (!adj[r]) return bfail(b, EPH_ERR_ARG, "null adjoint");
+    if (adj[r]->c->device != adj[0]->c->device) return bfail(b, EPH_ERR_ARG, "all adjoints of a batch on one device");
+    for (int q = 0; q < r; ++q)
+      if (adj[q] == adj[r] || adj[q]->c == adj[r]->c) return bfail(b, EPH_ERR_ARG, "one adjoint per context");
+    b->a.push_back(adj[r]);
+  }
+  if (cudaSetDevice(adj[0]->c->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+    return bfail(b, EPH_ERR_CUDA, "cannot create the batch stream");
+  b->joins.assign(nadj, nullptr);
+  for (auto &e : b->joins)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return bfail(b, EPH_ERR_CUDA, "events");
+  for (auto &e : b->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return bfail(b, EPH_ERR_CUDA, "events");
+  return EPH_OK;
+}
+
+void eph_adjoint_batch_destroy(eph_adjoint_batch *b) {
+  if (!b) return;
+  if (b->main) cudaStreamSynchronize(b->main);
+  for (cudaGraphExec_t e : b->exec)
+    if (e) cudaGraphExecDestroy(e);
+  for (auto e : b->joins)
+    if (e) cudaEventDestroy(e);
+  for (auto e : b->ev)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->main) cudaStreamDestroy(b->main);
+  delete b;
+}
+
+const char *eph_adjoint_batch_last_error(const eph_adjoint_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int eph_adjoint_batch_forward(eph_adjoint_batch *b, long nsteps, double *E, double *T_mean) {
+  if (!b || nsteps < 1) return EPH_ERR_ARG;
+  int rc;
+  for (size_t r = 0; r < b->a.size(); ++r)
+    if ((rc = fwd_prepare(b->a[r], nsteps))) return bfail(b, rc, "adjoint " + std::to_string(r) + ": " + b->a[r]->err);
+  if ((rc = batch_pass(b, 0, nsteps, b->ev[0], b->ev[1]))) return rc;
+  for (size_t r = 0; r < b->a.size(); ++r)
+    if ((rc = fwd_finish(b->a[r], nsteps, E ? E + r * nsteps : nullptr, T_mean ? T_mean + r * nsteps : nullptr,
+                         b->main)))
+      return bfail(b, rc, "adjoint " + std::to_string(r) + ": " + b->a[r]->err);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
+  b->fwd_ms = ms;
+  b->fwd_launches = b->graph_launches[0];
+  return EPH_OK;
+}
+
+int eph_adjoint_batch_backward(eph_adjoint_batch *b, const double *dL_dE, const double *dL_dT_mean) {
+  if (!b) return EPH_ERR_ARG;
+  const long ns = b->a[0]->nsteps;
+  for (eph_adjoint *a : b->a)
+    if (a->nsteps != ns || ns < 1) return bfail(b, EPH_ERR_STATE, "run eph_adjoint_batch_forward first");
+  int rc;
+  bool all_skip = true;
+  for (size_t r = 0; r < b->a.size(); ++r) {
+    bool sk = false;
+    if ((rc = bwd_prepare(b->a[r], dL_dE ? dL_dE + r * ns : nullptr, dL_dT_mean ? dL_dT_mean + r * ns : nullptr,
+                          b->main, &sk)))
+      return bfail(b, rc, "adjoint " + std::to_string(r) + ": " + b->a[r]->err);
+    all_skip = all_skip && sk;
+  }
+  if ((rc = batch_pass(b, all_skip ? 2 : 1, ns, b->ev[2], b->ev[3]))) return rc;
+  for (size_t r = 0; r < b->a.size(); ++r)
+    if ((rc = bwd_finish(b->a[r], all_skip, b->main)))
+      return bfail(b, rc, "adjoint " + std::to_string(r) + ": " + b->a[r]->err);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, b->ev[2], b->ev[3]);
+  b->bwd_ms = ms;
+  b->bwd_launches = b->graph_launches[all_skip ? 2 : 1];
+  return EPH_OK;
+}
+
+int eph_adjoint_batch_timing(eph_adjoint_batch *b, double *forward_ms, double *backward_ms, long *forward_launches,
+                             long *backward_launches) {
+  if (!b) return EPH_ERR_ARG;
+  if (forward_ms) *forward_ms = b->fwd_ms;
+  if (backward_ms) *backward_ms = b->bwd_ms;
+  if (forward_launches) *forward_launches = b->fwd_launches;
+  if (backward_launches) *backward_launches = b->bwd_launches;
   return EPH_OK;
 }
 

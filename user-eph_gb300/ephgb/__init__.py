@@ -113,6 +113,12 @@ SIGNATURES = {
     "eph_adjoint_backward": (C.c_int, [C.c_void_p, _dp, _dp]),
     "eph_adjoint_gradient": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_long]),
     "eph_adjoint_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "eph_adjoint_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "eph_adjoint_batch_destroy": (None, [C.c_void_p]),
+    "eph_adjoint_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "eph_adjoint_batch_forward": (C.c_int, [C.c_void_p, C.c_long, _dp, _dp]),
+    "eph_adjoint_batch_backward": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "eph_adjoint_batch_timing": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_long), C.POINTER(C.c_long)]),
     "eph_adjoint_timing": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_long), C.POINTER(C.c_long)]),
 }
 

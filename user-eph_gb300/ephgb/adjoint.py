@@ -198,7 +198,90 @@ def fit_beta(adj, nsteps, target_E, beta0, iters=50, lr=0.05, rho_knots=None, C_
             loss = loss + weight_T * ((T - tT) ** 2).sum()
         loss.backward()
         opt.step()
-        hist.append(float(loss))
+        hist.append(float(loss.detach()))
         if log:
             log(it, float(loss))
     return torch.exp(theta).detach().numpy(), hist
+
+
+class AdjointBatch:
+    """Several adjoints run together: every pass of every adjoint is a
+    parallel branch of one CUDA graph (eph_adjoint_batch_*)."""
+
+    def __init__(self, adjoints):
+        self.adjs = list(adjoints)
+        self.L = lib()
+        arr = (C.c_void_p * len(self.adjs))(*[a.h.value for a in self.adjs])
+        h = C.c_void_p()
+        rc = self.L.eph_adjoint_batch_create(len(self.adjs), arr, C.byref(h))
+        self.h = h
+        if rc:
+            raise EphError(rc, self.L.eph_adjoint_batch_last_error(h).decode() if h.value else "")
+        self.nsteps = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.eph_adjoint_batch_destroy(self.h)
+            self.h = None
+
+    def _check(self, rc):
+        if rc:
+            raise EphError(rc, self.L.eph_adjoint_batch_last_error(self.h).decode())
+
+    def forward(self, nsteps):
+        n = len(self.adjs)
+        E = np.zeros((n, nsteps))
+        T = np.zeros((n, nsteps))
+        self._check(self.L.eph_adjoint_batch_forward(self.h, int(nsteps), E.ctypes.data_as(_dp),
+                                                     T.ctypes.data_as(_dp)))
+        self.nsteps = nsteps
+        for a in self.adjs:
+            a.nsteps = nsteps
+        return E, T
+
+    def backward(self, dL_dE=None, dL_dT=None):
+        shape = (len(self.adjs), self.nsteps)
+        a = None if dL_dE is None else np.ascontiguousarray(np.broadcast_to(dL_dE, shape), dtype=np.float64)
+        b = None if dL_dT is None else np.ascontiguousarray(np.broadcast_to(dL_dT, shape), dtype=np.float64)
+        self._check(self.L.eph_adjoint_batch_backward(self.h, None if a is None else a.ctypes.data_as(_dp),
+                                                      None if b is None else b.ctypes.data_as(_dp)))
+
+    def timing(self):
+        f, b = C.c_double(), C.c_double()
+        lf, lb = C.c_long(), C.c_long()
+        self._check(self.L.eph_adjoint_batch_timing(self.h, C.byref(f), C.byref(b), C.byref(lf), C.byref(lb)))
+        return {"forward_ms": f.value, "backward_ms": b.value, "forward_launches": lf.value,
+                "backward_launches": lb.value}
+
+
+def fit_beta_batch(batch, nsteps, target_T, beta0, iters=30, lr=0.05, smooth=10.0, log=None):
+    """Fit the beta(rho) knots shared by every replica of `batch` to target
+    mean-T_e curves (one row per replica) with Adam on log(beta).  Loss =
+    sum over replicas and steps of ((T - T*) / T*_0)^2 + smooth * sum of the
+    squared second differences of log(beta): the curves constrain beta only
+    where the atoms' densities lie, and the penalty keeps the other knots
+    from wandering.  Returns (beta knots, history of the data term)."""
+    import torch
+
+    tT = np.asarray(target_T, dtype=np.float64)
+    scale = 1.0 / (tT[:, :1] ** 2)
+    theta = torch.tensor(np.log(np.asarray(beta0, dtype=np.float64)), requires_grad=True)
+    opt = torch.optim.Adam([theta], lr=lr)
+    hist = []
+    for it in range(iters):
+        beta = np.exp(theta.detach().numpy())
+        for a in batch.adjs:
+            a.set_knots(0, None, beta)
+        _, T = batch.forward(nsteps)
+        d = T - tT
+        hist.append(float((scale * d * d).sum()))
+        batch.backward(None, 2.0 * scale * d)
+        g = sum(a.gradient(GRAD_BETA_KNOTS) for a in batch.adjs)
+        opt.zero_grad()
+        d2 = theta[2:] - 2.0 * theta[1:-1] + theta[:-2]
+        (smooth * (d2 * d2).sum()).backward()
+        theta.grad += torch.from_numpy(g * beta)  # the data term, d/dlog(beta)
+        opt.step()
+        if log:
+            log(it, hist[-1])
+    return np.exp(theta.detach().numpy()), hist
