@@ -154,6 +154,18 @@ int eph_get_counter(eph_ctx *ctx, int which, long *out);
 /* Capacity of a spatial bin and of a per-atom pair list (0 keeps a value). */
 int eph_set_capacity(eph_ctx *ctx, int bin_capacity, int pair_capacity);
 
+/* Lanes per atom of the FAST-mode friction and force sweeps (no reference
+ * counterpart): 0 = chosen from the atom count (the default), or 1, 2, 4, 8.
+ * More lanes keep small systems (tens of thousands of atoms) from waiting on
+ * their loads; the sums' order, and so the last bits, depend on it (EXACT
+ * mode always uses one lane). */
+int eph_set_threads_per_atom(eph_ctx *ctx, int tpa);
+int eph_get_threads_per_atom(eph_ctx *ctx, int *tpa);
+/* Time the sweeps with 1, 2, 4 and 8 lanes per atom on the current pairs
+ * (after at least one step; forces and memories are restored) and keep the
+ * fastest; *chosen gets it (may be NULL). */
+int eph_autotune(eph_ctx *ctx, int *chosen);
+
 /* Timing of the step's phases with CUDA events on the context's stream
  * (no reference counterpart; the reference relies on gprof, lib/Makefile:25-28).
  * Phases: */

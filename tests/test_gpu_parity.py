@@ -125,3 +125,28 @@ def test_tdyn_grid(built, beta_file, tmp_path, mode):
     gpu.save_state(str(tmp_path / "after.restart"))  # C_e, kappa_e follow T in the written state
     text = open(tmp_path / "after.restart").read().splitlines()
     assert text[7].endswith("params.data") and len(text) == 8 + 8 * 6 * 5
+
+
+def test_threads_per_atom_variants(built, beta_file):
+    """FAST-mode sweeps with 1, 2, 4 and 8 lanes per atom give the same
+    forces within rounding (the order of the sums differs), and the autotuner
+    picks one of them and restores the forces it touched."""
+    words, at, dt = scenario("c1_small", beta_file)
+    ng = n_in_group(at)
+    out = {}
+    for tpa in (1, 2, 4, 8):
+        gpu = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_FAST)
+        gpu.set_threads_per_atom(tpa)
+        assert gpu.threads_per_atom() == tpa
+        for s in range(4):
+            gpu.step(1, xi=xi_rows(at, W.gaussian_stream(ng, 5, s)))
+        out[tpa] = {k: gpu.get(k) for k in ("w", "f_eph", "f_rng", "x", "v")}
+        out[tpa]["T"] = gpu.get("T")
+    for tpa in (2, 4, 8):
+        for k, a in out[tpa].items():
+            assert rel_err(a, out[1][k]) <= 1e-13, (tpa, k, rel_err(a, out[1][k]))
+    gpu = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_FAST)
+    gpu.step(1)
+    f_before = gpu.get("f")
+    assert gpu.autotune() in (1, 2, 4, 8)
+    np.testing.assert_array_equal(gpu.get("f"), f_before)

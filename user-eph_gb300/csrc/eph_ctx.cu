@@ -221,9 +221,53 @@ void launch_density_t(eph_ctx *c, int xi_mode) {
 
 template <bool FAST, bool MULTI, bool FRIC, bool RAND>
 void launch_forces_t(eph_ctx *c) {
-  k_forces<FAST, MULTI, FRIC, RAND><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
-      c->P, c->mask.p, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->Te_i.p, c->f.p, c->f_eph.p,
-      c->f_rng.p, c->f_dis.p, c->f_sto.p);
+  const int tpa = FAST ? c->tpa : 1;
+  if (tpa == 1) {
+    k_forces<FAST, MULTI, FRIC, RAND><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+        c->P, c->mask.p, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->Te_i.p, c->f.p, c->f_eph.p,
+        c->f_rng.p, c->f_dis.p, c->f_sto.p);
+    return;
+  }
+#define EPH_FORCES_TPA(T)                                                                                     \
+  k_forces_tpa<MULTI, FRIC, RAND, T><<<nblocks((long)c->n * T), BLOCK, 0, c->stream>>>(                       \
+      c->P, c->mask.p, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->Te_i.p, c->f.p, c->f_eph.p, \
+      c->f_rng.p, c->f_dis.p, c->f_sto.p)
+  if (tpa == 2) EPH_FORCES_TPA(2);
+  else if (tpa == 4) EPH_FORCES_TPA(4);
+  else EPH_FORCES_TPA(8);
+#undef EPH_FORCES_TPA
+}
+
+// lanes per atom of the FAST pair sweeps for n atoms: more lanes where the
+// one-lane sweeps leave the SMs with too few warps to hide their loads
+// (measured on GB300: 4,000 atoms 0.467 -> 0.420 ms per step with 4 lanes;
+// from ~30,000 atoms on the lanes make no difference)
+int auto_tpa(long n) { return n <= 65536 ? 4 : 1; }
+
+void launch_friction_w(eph_ctx *c) {
+  const int nb = nblocks(c->n);
+  if (c->mode != EPH_MODE_FAST) {
+    k_friction_w<false><<<nb, BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
+                                                     c->nshort.p, c->A.p, c->Bw.p);
+    return;
+  }
+  switch (c->tpa) {
+    case 2:
+      k_friction_w_tpa<2><<<nblocks((long)c->n * 2), BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p,
+                                                                            c->pe.p, c->nshort.p, c->A.p, c->Bw.p);
+      break;
+    case 4:
+      k_friction_w_tpa<4><<<nblocks((long)c->n * 4), BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p,
+                                                                            c->pe.p, c->nshort.p, c->A.p, c->Bw.p);
+      break;
+    case 8:
+      k_friction_w_tpa<8><<<nblocks((long)c->n * 8), BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p,
+                                                                            c->pe.p, c->nshort.p, c->A.p, c->Bw.p);
+      break;
+    default:
+      k_friction_w<true><<<nb, BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
+                                                      c->nshort.p, c->A.p, c->Bw.p);
+  }
 }
 
 template <bool FAST, bool FRIC, bool RAND>
@@ -286,12 +330,7 @@ int launch_post_force(eph_ctx *c, int xi_mode) {
   if (c->P.flags & FLAG_FRICTION) {
     PhaseScope ps(c, EPH_PHASE_FRICTION_W);
     ps.launched();
-    if (fast)
-      k_friction_w<true><<<nb, BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
-                                                      c->nshort.p, c->A.p, c->Bw.p);
-    else
-      k_friction_w<false><<<nb, BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
-                                                       c->nshort.p, c->A.p, c->Bw.p);
+    launch_friction_w(c);
   }
   {
     PhaseScope ps(c, EPH_PHASE_FORCES);
@@ -621,6 +660,84 @@ int eph_set_capacity(eph_ctx *c, int bin_capacity, int pair_capacity) {
   return EPH_OK;
 }
 
+int eph_set_threads_per_atom(eph_ctx *c, int tpa) {
+  if (!c) return EPH_ERR_ARG;
+  if (tpa != 0 && tpa != 1 && tpa != 2 && tpa != 4 && tpa != 8)
+    return fail(c, EPH_ERR_ARG, "lanes per atom: 0 (automatic), 1, 2, 4 or 8");
+  drop_graph(c);
+  c->buf_gen += 1;  // graphs captured elsewhere hold the old launch shape
+  c->tpa_auto = tpa == 0;
+  c->tpa = tpa == 0 ? auto_tpa(c->n) : tpa;
+  return EPH_OK;
+}
+
+int eph_get_threads_per_atom(eph_ctx *c, int *tpa) {
+  if (!c || !tpa) return EPH_ERR_ARG;
+  *tpa = c->mode == EPH_MODE_FAST ? c->tpa : 1;
+  return EPH_OK;
+}
+
+int eph_autotune(eph_ctx *c, int *chosen) {
+  if (!c) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r) return r;
+  if (c->mode != EPH_MODE_FAST || c->args.model != 4) {
+    if (chosen) *chosen = 1;
+    return EPH_OK;  // EXACT keeps the reference's order: one lane per atom
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  // the sweeps need a step's pairs
+  unsigned long long steps = 0;
+  CUDA_TRY(c, cudaMemcpy(&steps, c->step_ctr.p, sizeof(steps), cudaMemcpyDeviceToHost));
+  if (steps == 0) return fail(c, EPH_ERR_STATE, "autotune needs one step (or post_force) first");
+  const size_t N = (size_t)c->n;
+  DevBuf<D4> save[5];
+  DevBuf<D4> *bufs[5] = {&c->f, &c->f_eph, &c->f_rng, &c->f_dis, &c->f_sto};
+  for (int k = 0; k < 5; ++k) {
+    CUDA_TRY(c, save[k].alloc(N));
+    CUDA_TRY(c, cudaMemcpyAsync(save[k].p, bufs[k]->p, sizeof(D4) * N, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CUDA_TRY(c, cudaEventCreate(&e0));
+  CUDA_TRY(c, cudaEventCreate(&e1));
+  const bool prof = c->profiling;
+  c->profiling = false;
+  const int keep = c->tpa;
+  int best = 1;
+  float best_ms = 1e30f;
+  for (int tpa : {1, 2, 4, 8}) {
+    c->tpa = tpa;
+    float total = 0.f;
+    for (int rep = 0; rep < 7; ++rep) {
+      CUDA_TRY(c, cudaMemcpyAsync(c->f.p, save[0].p, sizeof(D4) * N, cudaMemcpyDeviceToDevice, c->stream));
+      CUDA_TRY(c, cudaEventRecord(e0, c->stream));
+      if (c->P.flags & FLAG_FRICTION) launch_friction_w(c);
+      if (c->multi) launch_forces_m<true, true>(c);
+      else launch_forces_m<true, false>(c);
+      CUDA_TRY(c, cudaEventRecord(e1, c->stream));
+      CUDA_TRY(c, cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CUDA_TRY(c, cudaEventElapsedTime(&ms, e0, e1));
+      if (rep >= 2) total += ms;  // two warm-up runs
+    }
+    if (total < best_ms) {
+      best_ms = total;
+      best = tpa;
+    }
+  }
+  c->tpa = keep;
+  c->profiling = prof;
+  for (int k = 0; k < 5; ++k)
+    CUDA_TRY(c, cudaMemcpyAsync(bufs[k]->p, save[k].p, sizeof(D4) * N, cudaMemcpyDeviceToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  r = eph_set_threads_per_atom(c, best);
+  if (r) return r;
+  if (chosen) *chosen = best;
+  return EPH_OK;
+}
+
 int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const int *htype, const int *hmask) {
   if (!c) return EPH_ERR_ARG;
   drop_graph(c);
@@ -636,6 +753,7 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
     c->buf_gen += 1;
     c->n = n;
     c->P.n = n;
+    if (c->tpa_auto) c->tpa = auto_tpa(n);
     for (DevBuf<D4> *b : {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->xi, &c->A, &c->Bw, &c->f_dis,
                           &c->f_sto})
       CUDA_TRY(c, b->alloc(N));

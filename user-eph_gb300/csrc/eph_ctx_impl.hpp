@@ -59,6 +59,10 @@ struct eph_ctx {
 
   StepParams P{};
   bool multi = false;
+  // lanes per atom of the FAST-mode friction and force sweeps (1, 2, 4, 8)
+  // and whether it follows the atom count (eph_set_threads_per_atom)
+  int tpa = 1;
+  bool tpa_auto = true;
 
   int n = 0;
   DevBuf<D4> x, v, f, xhold, f_eph, f_rng, xi, fext, A, Bw;

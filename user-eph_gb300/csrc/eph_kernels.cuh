@@ -510,6 +510,160 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
   f[i] = fi;
 }
 
+// ------------------------------------- pair sweeps, several lanes per atom
+
+// FAST mode with TPA lanes per atom (TPA = 2, 4, 8): lane g of an atom takes
+// rows g, g + TPA, ...; the lanes' sums are combined by a butterfly over the
+// TPA neighbouring lanes.  Small systems (tens of thousands of atoms) leave
+// the SMs with a few warps each and the one-lane sweeps wait on their loads;
+// TPA times more warps hide that.  The order of the sums depends on TPA
+// (results within rounding of the one-lane sweeps, the same every run).
+template <int TPA>
+__global__ void __launch_bounds__(128) k_friction_w_tpa(StepParams P, const int *__restrict__ mask,
+                                                         const D4 *__restrict__ v, const unsigned *__restrict__ pj,
+                                                         const D4 *__restrict__ pe, const int *__restrict__ nshort,
+                                                         const D4 *__restrict__ A, D4 *__restrict__ Bw) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt / TPA, g = gt % TPA;
+  bool act = false;
+  D4 Ai{0.0, 0.0, 0.0, 0.0};
+  if (i < P.n) {
+    Ai = A[i];
+    act = (mask[i] & P.groupbit) && pos_double(Ai.x);
+  }
+  double wx = 0.0, wy = 0.0, wz = 0.0;
+  if (act) {
+    const D4 vi = v[i];
+    const int ns = nshort[i];
+    for (int k = g; k < ns; k += TPA) {
+      const size_t slot = (size_t)k * P.n + i;
+      const unsigned j = pj[slot] & IDX_MASK;
+      const D4 e = pe[slot];
+      const D4 vj = v[j];
+      const double s = Ai.y * e.w * dot3_fma(e.x, e.y, e.z, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
+      wx = fma(s, e.x, wx);
+      wy = fma(s, e.y, wy);
+      wz = fma(s, e.z, wz);
+    }
+  }
+#pragma unroll
+  for (int o = TPA / 2; o > 0; o >>= 1) {
+    wx += __shfl_xor_sync(0xffffffffu, wx, o);
+    wy += __shfl_xor_sync(0xffffffffu, wy, o);
+    wz += __shfl_xor_sync(0xffffffffu, wz, o);
+  }
+  if (act && g == 0) {
+    const double xiz = Bw[i].x;
+    Bw[i] = D4{xiz, wx, wy, wz};
+  }
+}
+
+template <bool MULTI, bool FRIC, bool RAND, int TPA>
+__global__ void __launch_bounds__(128) k_forces_tpa(StepParams P, const int *__restrict__ mask,
+                                                     const unsigned *__restrict__ pj, const D4 *__restrict__ pe,
+                                                     const double2 *__restrict__ pg, const int *__restrict__ nshort,
+                                                     const D4 *__restrict__ A, const D4 *__restrict__ Bw,
+                                                     const double *__restrict__ Te_i, D4 *__restrict__ f,
+                                                     D4 *__restrict__ f_eph, D4 *__restrict__ f_rng,
+                                                     D4 *__restrict__ f_dis, D4 *__restrict__ f_sto) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt / TPA, g = gt % TPA;
+  double fex = 0.0, fey = 0.0, fez = 0.0, frx = 0.0, fry = 0.0, frz = 0.0;
+  D4 Ai{0.0, 0.0, 0.0, 0.0};
+  bool live = false;
+  if (i < P.n) {
+    Ai = A[i];
+    live = (mask[i] & P.groupbit) && pos_double(Ai.x);
+  }
+  if (live) {
+    const D4 Bi = Bw[i];
+    const double xix = Ai.z, xiy = Ai.w, xiz = Bi.x;
+    const int ns = nshort[i];
+    for (int k = g; k < ns; k += TPA) {
+      const size_t slot = (size_t)k * P.n + i;
+      const unsigned j = pj[slot] & IDX_MASK;
+      const D4 Aj = A[j];
+      if (!pos_double(Aj.x)) continue;
+      const D4 e = pe[slot];
+      const D4 Bj = Bw[j];
+      const double a = Ai.y * e.w;
+      const double b = Aj.y * (MULTI ? pg[slot].x : e.w);
+      if (FRIC) {
+        const double di = dot3_fma(e.x, e.y, e.z, Bi.y, Bi.z, Bi.w);
+        const double dj = dot3_fma(e.x, e.y, e.z, Bj.y, Bj.z, Bj.w);
+        const double dvar = fma(a, di, -(b * dj));
+        fex = fma(-dvar, e.x, fex);
+        fey = fma(-dvar, e.y, fey);
+        fez = fma(-dvar, e.z, fez);
+      }
+      if (RAND) {
+        const double di = dot3_fma(e.x, e.y, e.z, xix, xiy, xiz);
+        const double dj = dot3_fma(e.x, e.y, e.z, Aj.z, Aj.w, Bj.x);
+        const double dvar = fma(a, di, -(b * dj));
+        frx = fma(dvar, e.x, frx);
+        fry = fma(dvar, e.y, fry);
+        frz = fma(dvar, e.z, frz);
+      }
+    }
+  }
+#pragma unroll
+  for (int o = TPA / 2; o > 0; o >>= 1) {
+    if (FRIC) {
+      fex += __shfl_xor_sync(0xffffffffu, fex, o);
+      fey += __shfl_xor_sync(0xffffffffu, fey, o);
+      fez += __shfl_xor_sync(0xffffffffu, fez, o);
+    }
+    if (RAND) {
+      frx += __shfl_xor_sync(0xffffffffu, frx, o);
+      fry += __shfl_xor_sync(0xffffffffu, fry, o);
+      frz += __shfl_xor_sync(0xffffffffu, frz, o);
+    }
+  }
+  if (i >= P.n || g != 0) return;
+  if (live && RAND) {
+    const double var = P.eta * sqrt(Te_i[i]);
+    frx *= var;
+    fry *= var;
+    frz *= var;
+  }
+  if (P.coloured && live) {  // fix_eph_coloured_exp.cpp:562-568, :619-625
+    if (FRIC) {
+      D4 d = f_dis[i];
+      d.x = d.x * (1. - P.zeta) + P.zeta * fex;
+      d.y = d.y * (1. - P.zeta) + P.zeta * fey;
+      d.z = d.z * (1. - P.zeta) + P.zeta * fez;
+      f_dis[i] = d;
+      fex = d.x;
+      fey = d.y;
+      fez = d.z;
+    }
+    if (RAND) {
+      D4 d = f_sto[i];
+      d.x = d.x * (1. - P.zeta) + P.zeta * frx;
+      d.y = d.y * (1. - P.zeta) + P.zeta * fry;
+      d.z = d.z * (1. - P.zeta) + P.zeta * frz;
+      f_sto[i] = d;
+      frx = d.x;
+      fry = d.y;
+      frz = d.z;
+    }
+  }
+  f_eph[i] = D4{fex, fey, fez, 0.0};
+  f_rng[i] = D4{frx, fry, frz, 0.0};
+  D4 fi = f[i];
+  if (FRIC && !(P.flags & 0x10)) {
+    fi.x += fex;
+    fi.y += fey;
+    fi.z += fez;
+  }
+  if (RAND && !(P.flags & 0x20)) {
+    fi.x += frx;
+    fi.y += fry;
+    fi.z += frz;
+  }
+  f[i] = fi;
+}
+
 // --------------------------------------------------------- model 1 (TTM)
 
 // force_ttm (fix_eph.cpp:468-503): a local Langevin thermostat with the

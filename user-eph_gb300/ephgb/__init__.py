@@ -73,6 +73,9 @@ SIGNATURES = {
     "eph_get_counter": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_long)]),
     "eph_set_capacity": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "eph_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "eph_set_threads_per_atom": (C.c_int, [C.c_void_p, C.c_int]),
+    "eph_get_threads_per_atom": (C.c_int, [C.c_void_p, _ip]),
+    "eph_autotune": (C.c_int, [C.c_void_p, _ip]),
     "eph_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.POINTER(C.c_char_p)),
                                    C.POINTER(eph_md), C.POINTER(C.c_void_p)]),
     "eph_batch_destroy": (None, [C.c_void_p]),
@@ -397,6 +400,19 @@ class FixEPH:
 
     def set_graph(self, on=True):
         self._check(self.L.eph_set_graph(self.h, 1 if on else 0))
+
+    def set_threads_per_atom(self, tpa):
+        self._check(self.L.eph_set_threads_per_atom(self.h, int(tpa)))
+
+    def threads_per_atom(self):
+        out = C.c_int()
+        self._check(self.L.eph_get_threads_per_atom(self.h, C.byref(out)))
+        return out.value
+
+    def autotune(self):
+        out = C.c_int()
+        self._check(self.L.eph_autotune(self.h, C.byref(out)))
+        return out.value
 
     def set_beta_knots(self, elem, rho_knots, beta_knots):
         r = np.ascontiguousarray(rho_knots, dtype=np.float64)
