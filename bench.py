@@ -442,6 +442,44 @@ def run_adjoint_fit(args, dev):
                 "atom_steps_per_s_forward": atoms_total * nsteps / (tb["forward_ms"] / 1000.0)}
 
 
+def run_md_eam(args, dev):
+    """Full MD: the bench workload with the engine's eam/alloy pair force
+    (Sutton-Chen Ni tables, 6 A cut-off) added to fix eph: atom-steps/s of the
+    whole step and the pair force's share (phase timing)."""
+    import torch
+
+    import ephgb
+    from ephgb import workloads as W
+
+    with tempfile.TemporaryDirectory() as wd:
+        words, atoms = make_system(wd)
+        eam = W.write_eam_sutton_chen(os.path.join(wd, "SC_Ni.eam"))
+        fix = ephgb.FixEPH(words, atoms, dt=DT, mode=ephgb.MODE_FAST, device=dev, eam=(eam, ["Ni"]))
+        stream = torch.cuda.Stream()
+        fix.set_stream(stream.cuda_stream)
+        fix.set_graph(True)
+        fix.step(args.warmup)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k = args.md_steps
+        e0.record(stream)
+        fix.step(k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        fix.set_profiling(True)
+        fix.step(10)
+        fix.synchronize()
+        ph = fix.phase_times()
+        fix.set_profiling(False)
+        total = sum(v[0] for v in ph.values())
+        return {"workload": WORKLOAD + " + eam/alloy Sutton-Chen Ni (6 A cut-off)", "atoms": atoms.n, "steps": k,
+                "value": atoms.n * k / (ms / 1000.0), "unit": "MD atom-steps/s (pair force + fix eph)",
+                "ms_per_step": ms / k, "pair_share": ph["pair"][0] / total,
+                "phases_ms_per_step": {p: round(v[0] / 10, 4) for p, v in ph.items()},
+                "pair_energy_per_atom": fix.pair_energy() / atoms.n}
+
+
 def cpu_baseline(threads, steps=1, warm=1):
     """The CPU restatement (oracle port) on the same workload: `steps` steps
     of the full system after `warm` warm-up steps; time of the fix's own hooks
@@ -480,6 +518,9 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=ADJ_STEPS)
     ap.add_argument("--no-adjoint-fd", action="store_true", help="skip the finite-difference check")
     ap.add_argument("--no-fit", action="store_true", help="omit the batched adjoint fitting leg")
+    ap.add_argument("--no-md", action="store_true", help="omit the full-MD (EAM pair force) leg")
+    ap.add_argument("--only-md", action="store_true", help="run the full-MD leg alone")
+    ap.add_argument("--md-steps", type=int, default=50)
     ap.add_argument("--only-fit", action="store_true", help="run the batched adjoint fitting leg alone")
     ap.add_argument("--fit-replicas", type=int, default=16)
     ap.add_argument("--fit-steps", type=int, default=100)
@@ -515,6 +556,9 @@ def main():
 
     import torch
 
+    if args.only_md:
+        print(json.dumps(run_md_eam(args, int(os.environ.get("LOCAL_RANK", rank)))))
+        return
     if args.only_fit:
         print(json.dumps(run_adjoint_fit(args, int(os.environ.get("LOCAL_RANK", rank)))))
         return
@@ -562,6 +606,8 @@ def main():
             line["batched"]["value"] = float(t.item())
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)), fd=not args.no_adjoint_fd)
+    if rank == 0 and not args.no_md:
+        line["md_eam"] = run_md_eam(args, int(os.environ.get("LOCAL_RANK", rank)))
     if rank == 0 and not args.no_fit:
         line["adjoint_fit"] = run_adjoint_fit(args, int(os.environ.get("LOCAL_RANK", rank)))
     if rank == 0 and not args.no_cpu_baseline:

@@ -154,6 +154,17 @@ int eph_get_counter(eph_ctx *ctx, int which, long *out);
 /* Capacity of a spatial bin and of a per-atom pair list (0 keeps a value). */
 int eph_set_capacity(eph_ctx *ctx, int bin_capacity, int pair_capacity);
 
+/* Pair force of the standalone engine (eph_step, batches): eam/alloy from a
+ * setfl file, elements[t-1] the file's element for LAMMPS type t (as
+ * `pair_coeff * * file E1 E2 ...`).  Evaluated each step on the GPU between
+ * initial_integrate and post_force, added to EPH_FIELD_F_EXT if one is set.
+ * Call before eph_set_atoms.  No reference counterpart: the reference fix gets
+ * the pair force from LAMMPS (Tests/MD_Run/run.lmp: pair_style eam/alloy);
+ * the hook functions are unaffected. */
+int eph_set_pair_eam(eph_ctx *ctx, const char *path, int ntypes, const char *const *elements);
+/* embedding + pair energy of the last step's pair force (0 without one) */
+int eph_pair_energy(eph_ctx *ctx, double *E);
+
 /* Lanes per atom of the FAST-mode friction and force sweeps (no reference
  * counterpart): 0 = chosen from the atom count (the default), or 1, 2, 4, 8.
  * More lanes keep small systems (tens of thousands of atoms) from waiting on
@@ -176,7 +187,8 @@ int eph_autotune(eph_ctx *ctx, int *chosen);
 #define EPH_PHASE_FORCES 4     /* force_prl stages 2 + 3 and the force update */
 #define EPH_PHASE_DEPOSIT 5    /* energy deposition + energy total */
 #define EPH_PHASE_FDM 6        /* EPH_FDM::solve substeps */
-#define EPH_NPHASES 7
+#define EPH_PHASE_PAIR 7       /* the engine's pair force (eph_set_pair_eam) */
+#define EPH_NPHASES 8
 /* on != 0 starts recording (and zeroes the totals); off stops. */
 int eph_set_profiling(eph_ctx *ctx, int on);
 /* milliseconds and kernel launches per phase since profiling was switched on

@@ -1,0 +1,92 @@
+"""The engine's eam/alloy pair force on the GPU (eph_set_pair_eam): against a
+numpy restatement that reads the setfl file and builds its tables on its own
+(oracle/eam_ref.py), against the gradient of its own energy, at rest in the
+perfect lattice, and energy conservation of plain NVE.  Parity with LAMMPS's
+pair_style eam/alloy itself is unpinned (LAMMPS is not available); the
+tables follow the same cubic Hermite scheme with five-point slopes."""
+import numpy as np
+import pytest
+
+import ephgb
+from ephgb import workloads as W
+from oracle.eam_ref import energy_forces, read_setfl
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setfl(tmp_path_factory):
+    return W.write_eam_sutton_chen(str(tmp_path_factory.mktemp("eam") / "SC_Ni.eam"))
+
+
+def forces_at(setfl, beta_file, at, mode=ephgb.MODE_FAST):
+    """EAM forces and energy at the atoms' positions: one step of a fix that
+    applies nothing (flags 0) from zero velocities and forces (the box must
+    be at least three cut-offs, 6 A, wide: 6^3 fcc cells)"""
+    a = W.Atoms(x=at.x.copy(), v=np.zeros_like(at.v), type=at.type, mask=at.mask, boxlo=at.boxlo, boxhi=at.boxhi,
+                mass=at.mass)
+    fix = ephgb.FixEPH(W.fix_args(beta_file, flags=0, grid=(4, 4, 4)), a, dt=0.001, mode=mode,
+                       eam=(setfl, ["Ni"]))
+    fix.step(1)
+    np.testing.assert_array_equal(fix.get("x"), a.x)  # v = f = 0: the step did not move them
+    return fix.get("f"), fix.pair_energy()
+
+
+def test_matches_the_numpy_restatement(built, setfl, beta_file):
+    at = W.fcc_lattice(6, jitter=0.08, seed=61)
+    f, E = forces_at(setfl, beta_file, at)
+    En, fn = energy_forces(read_setfl(setfl), at.x, at.type, {1: 0}, at.boxhi - at.boxlo)
+    assert abs(E - En) <= 1e-12 * abs(En)
+    assert np.abs(f - fn).max() <= 1e-11 * np.abs(fn).max()
+
+
+def test_forces_are_minus_the_energy_gradient(built, setfl, beta_file):
+    at = W.fcc_lattice(6, jitter=0.08, seed=62)
+    f, _ = forces_at(setfl, beta_file, at)
+    h = 1e-5
+    for i, k in ((3, 0), (77, 1), (250, 2), (863, 0)):
+        xp = at.x.copy()
+        xp[i, k] += h
+        _, Ep = forces_at(setfl, beta_file, W.Atoms(x=xp, v=at.v, type=at.type, mask=at.mask, boxlo=at.boxlo,
+                                                    boxhi=at.boxhi, mass=at.mass))
+        xm = at.x.copy()
+        xm[i, k] -= h
+        _, Em = forces_at(setfl, beta_file, W.Atoms(x=xm, v=at.v, type=at.type, mask=at.mask, boxlo=at.boxlo,
+                                                    boxhi=at.boxhi, mass=at.mass))
+        assert abs(f[i, k] + (Ep - Em) / (2 * h)) <= 1e-6 * np.abs(f).max(), (i, k)
+
+
+def test_perfect_lattice_is_at_rest(built, setfl, beta_file):
+    at = W.fcc_lattice(6, jitter=0.0, seed=63)
+    f, E = forces_at(setfl, beta_file, at)
+    assert np.abs(f).max() <= 1e-10
+    assert -4.5 < E / at.n < -4.0  # Sutton-Chen Ni cohesion with the 6 A cut-off
+
+
+def test_nve_conserves_energy(built, setfl, beta_file):
+    at = W.fcc_lattice(6, temperature=600.0, seed=64)
+    fix = ephgb.FixEPH(W.fix_args(beta_file, flags=0, grid=(4, 4, 4)), at, dt=0.001, eam=(setfl, ["Ni"]))
+    m = at.mass[1]
+    energies = []
+    for _ in range(20):
+        fix.step(10)
+        v = fix.get("v")
+        ke = 0.5 * m * W.MVV2E * (v * v).sum()
+        energies.append(ke + fix.pair_energy())
+    energies = np.array(energies)
+    assert np.abs(energies - energies[0]).max() / at.n <= 2e-5  # eV per atom over 200 fs
+
+
+def test_with_the_fix_and_graph_replay(built, setfl, beta_file):
+    """fix eph (friction + random + grid) on top of the pair force: graph
+    replays equal direct launches bit for bit"""
+    at = W.fcc_lattice(6, seed=65)
+    W.add_pka(at, 500.0, seed=3)
+    out = []
+    for graph in (False, True):
+        fix = ephgb.FixEPH(W.fix_args(beta_file, flags=7, grid=(6, 6, 6)), at, dt=0.0005, eam=(setfl, ["Ni"]))
+        fix.set_graph(graph)
+        fix.step(40)
+        out.append((fix.get("x"), fix.get("v"), fix.get("T"), fix.pair_energy()))
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)

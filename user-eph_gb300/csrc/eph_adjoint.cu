@@ -1029,6 +1029,8 @@ int run_pass(eph_adjoint *a, int pass, long nsteps, cudaEvent_t e0, cudaEvent_t 
       if (!r) {
         sh = now;
         gl = a->launches;
+      } else {
+        cudaGetLastError();  // a failed capture leaves its error behind for the next caller
       }
     }
     if (!r) {
@@ -1179,6 +1181,7 @@ int eph_adjoint_create(eph_ctx *c, int checkpoint_every, eph_adjoint **out) {
   if (c->args.model != 4) return ctxi::fail(c, EPH_ERR_UNSUPPORTED_MODEL, "the adjoint follows force_prl (model 4)");
   if (c->args.coloured) return ctxi::fail(c, EPH_ERR_UNSUPPORTED_MODEL, "the adjoint follows fix eph, not eph/coloured/exp");
   if (c->td.tdyn) return ctxi::fail(c, EPH_ERR_STATE, "the adjoint needs a grid without temperature-dependent cells");
+  if (c->eam) return ctxi::fail(c, EPH_ERR_UNSUPPORTED_MODEL, "the adjoint does not differentiate the EAM pair force");
   if (c->beta.n_elements * c->beta.n_beta > 65536)
     return ctxi::fail(c, EPH_ERR_CAPACITY, "alpha tables too large for the adjoint's accumulators");
   eph_adjoint *a = new (std::nothrow) eph_adjoint();
@@ -1383,6 +1386,8 @@ static int batch_pass(eph_adjoint_batch *b, int pass, long nsteps, cudaEvent_t e
     if (!rc) {
       b->shape[pass] = now;
       b->graph_launches[pass] = total;
+    } else {
+      cudaGetLastError();
     }
   }
   if (!rc) {

@@ -132,42 +132,6 @@ int check_device(eph_ctx *c) {
   return fail(c, EPH_ERR_RANGE, "device: energy deposit outside the fixed-point range");
 }
 
-cudaEvent_t take_event(eph_ctx *c) {
-  if (!c->event_pool.empty()) {
-    cudaEvent_t e = c->event_pool.back();
-    c->event_pool.pop_back();
-    return e;
-  }
-  cudaEvent_t e = nullptr;
-  cudaEventCreate(&e);
-  return e;
-}
-
-// Brackets the launches of one phase with CUDA events on the context's
-// stream when profiling is on; counts the kernel launches either way.
-struct PhaseScope {
-  eph_ctx *c;
-  int phase;
-  cudaEvent_t b = nullptr;
-  PhaseScope(eph_ctx *ctx, int ph) : c(ctx), phase(ph) {
-    if (c->profiling) {
-      b = take_event(c);
-      cudaEventRecord(b, c->stream);
-    }
-  }
-  void launched(int k = 1) {
-    c->launches += k;
-    c->phase_launches[phase] += k;
-  }
-  ~PhaseScope() {
-    if (c->profiling && b) {
-      cudaEvent_t e = take_event(c);
-      cudaEventRecord(e, c->stream);
-      c->marks.push_back({phase, b, e});
-    }
-  }
-};
-
 void collect_marks(eph_ctx *c) {
   for (auto &m : c->marks) {
     float ms = 0.f;
@@ -297,16 +261,25 @@ void launch_forces_m(eph_ctx *c) {
 
 // post_force: bins, density, friction pre-vector, forces
 int launch_post_force(eph_ctx *c, int xi_mode) {
+  int r = launch_bin(c);
+  if (r) return r;
+  return launch_pair_sweeps(c, xi_mode);
+}
+
+int launch_bin(eph_ctx *c) {
   const int nb = nblocks(c->n);
-  {
-    PhaseScope ps(c, EPH_PHASE_BIN);
-    ps.launched();
-    CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
-    k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
-                                       c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 1);
-    ps.launched();
-    k_bin_sort<<<nblocks(c->nbins), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p, c->bins.p);
-  }
+  PhaseScope ps(c, EPH_PHASE_BIN);
+  ps.launched();
+  CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
+  k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
+                                     c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 1);
+  ps.launched();
+  k_bin_sort<<<nblocks(c->nbins), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p, c->bins.p);
+  CUDA_TRY(c, cudaGetLastError());
+  return EPH_OK;
+}
+
+int launch_pair_sweeps(eph_ctx *c, int xi_mode) {
   const bool fast = c->mode == EPH_MODE_FAST;
   {
     PhaseScope ps(c, EPH_PHASE_DENSITY);
@@ -436,12 +409,18 @@ int write_T_output(eph_ctx *c) {
 int record_step(eph_ctx *c, int xi_mode) {
   int r;
   if ((r = launch_initial(c, 1))) return r;
-  // force clear + the external (pair) force
-  if (c->have_fext)
-    CUDA_TRY(c, cudaMemcpyAsync(c->f.p, c->fext.p, sizeof(D4) * (size_t)c->n, cudaMemcpyDeviceToDevice, c->stream));
-  else
-    CUDA_TRY(c, cudaMemsetAsync(c->f.p, 0, sizeof(D4) * (size_t)c->n, c->stream));
-  if ((r = launch_post_force(c, xi_mode))) return r;
+  if (c->eam) {
+    // the engine's pair force on this step's positions (Verlet: after the
+    // wrap and the neighbour bins, before post_force)
+    if ((r = launch_bin(c)) || (r = launch_eam(c)) || (r = launch_pair_sweeps(c, xi_mode))) return r;
+  } else {
+    // force clear + the external (pair) force
+    if (c->have_fext)
+      CUDA_TRY(c, cudaMemcpyAsync(c->f.p, c->fext.p, sizeof(D4) * (size_t)c->n, cudaMemcpyDeviceToDevice, c->stream));
+    else
+      CUDA_TRY(c, cudaMemsetAsync(c->f.p, 0, sizeof(D4) * (size_t)c->n, c->stream));
+    if ((r = launch_post_force(c, xi_mode))) return r;
+  }
   if ((r = launch_final(c))) return r;
   return launch_end_of_step(c);
 }
@@ -468,6 +447,7 @@ int capture_step(eph_ctx *c, int xi_mode) {
   c->launches = before;
   if (r || e != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
+    cudaGetLastError();  // a failed capture leaves its error behind for the next caller
     return r ? r : fail(c, EPH_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
   }
   c->graph = g;
@@ -639,6 +619,7 @@ void eph_destroy(eph_ctx *c) {
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->h_bounds) cudaFreeHost(c->h_bounds);
+  eam_free(c);
   delete c;
 }
 
@@ -749,6 +730,7 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
   CUDA_TRY(c, cudaSetDevice(c->device));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   const size_t N = (size_t)n;
+  int r0;
   if (n != c->n) {  // (re)allocate the per-atom storage
     c->buf_gen += 1;
     c->n = n;
@@ -789,6 +771,7 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
     CUDA_TRY(c, c->pe.alloc((size_t)c->kcap * N));
     CUDA_TRY(c, c->pg.alloc((size_t)c->kcap * N));
   }
+  if ((r0 = eam_resize(c))) return r0;
   if (!c->tmap.p) CUDA_TRY(c, c->tmap.alloc(65));
   if (!c->bin_count.p) CUDA_TRY(c, c->bin_count.alloc((size_t)c->nbins));
   // atoms

@@ -40,6 +40,8 @@ inline int nblocks(long n, int b = BLOCK) { return (int)((n + b - 1) / b); }
 
 using namespace ephgb;
 
+struct EamDevice;  // the engine's eam/alloy pair force (eph_eam.cu)
+
 struct eph_ctx {
   std::string err;
   int device = 0;
@@ -92,6 +94,8 @@ struct eph_ctx {
   DevBuf<U128> acc, part, gsum;
   unsigned nsub = 1;
   double inner_dt = 0;
+  // eam/alloy pair force of the standalone engine (eph_set_pair_eam), or none
+  EamDevice *eam = nullptr;
   // set by the adjoint while it records a step: substep k of the grid solve
   // writes its output to fdm_rec + k * ncells instead of the ping-pong buffer
   double *fdm_rec = nullptr;
@@ -141,6 +145,49 @@ int launch_initial(eph_ctx *c, int check_wrap);
 int launch_post_force(eph_ctx *c, int xi_mode);
 int launch_final(eph_ctx *c);
 int launch_end_of_step(eph_ctx *c);
+// post_force in two parts: spatial binning (and the wrap), then the sweeps
+int launch_bin(eph_ctx *c);
+int launch_pair_sweeps(eph_ctx *c, int xi_mode);
+// the engine's pair force for this step into f (plus the external force)
+int launch_eam(eph_ctx *c);
+int eam_resize(eph_ctx *c);  // per-atom buffers of the pair force for c->n atoms
+void eam_free(eph_ctx *c);
+
+inline cudaEvent_t take_event(eph_ctx *c) {
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets the launches of one phase with CUDA events on the context's
+// stream when profiling is on; counts the kernel launches either way.
+struct PhaseScope {
+  eph_ctx *c;
+  int phase;
+  cudaEvent_t b = nullptr;
+  PhaseScope(eph_ctx *ctx, int ph) : c(ctx), phase(ph) {
+    if (c->profiling) {
+      b = take_event(c);
+      cudaEventRecord(b, c->stream);
+    }
+  }
+  void launched(int k = 1) {
+    c->launches += k;
+    c->phase_launches[phase] += k;
+  }
+  ~PhaseScope() {
+    if (c->profiling && b) {
+      cudaEvent_t e = take_event(c);
+      cudaEventRecord(e, c->stream);
+      c->marks.push_back({phase, b, e});
+    }
+  }
+};
 
 }  // namespace ctxi
 }  // namespace ephgb

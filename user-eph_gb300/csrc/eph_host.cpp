@@ -534,4 +534,73 @@ int parse_fix_args(int narg, const char *const *arg, FixArgs *a, std::string *wh
   return EPH_OK;
 }
 
+void hermite_table(const std::vector<double> &y, std::vector<double> &coef) {
+  const size_t n = y.size();
+  coef.assign(4 * n, 0.0);
+  if (n == 0) return;
+  if (n == 1) {
+    coef[0] = y[0];
+    return;
+  }
+  std::vector<double> s(n);
+  s[0] = y[1] - y[0];
+  s[n - 1] = y[n - 1] - y[n - 2];
+  if (n > 2) {
+    s[1] = 0.5 * (y[2] - y[0]);
+    s[n - 2] = 0.5 * (y[n - 1] - y[n - 3]);
+  }
+  for (size_t m = 2; m + 2 < n; ++m) s[m] = ((y[m - 2] - y[m + 2]) + 8.0 * (y[m + 1] - y[m - 1])) / 12.0;
+  for (size_t m = 0; m + 1 < n; ++m) {
+    const double d = y[m + 1] - y[m];
+    coef[4 * m + 0] = y[m];
+    coef[4 * m + 1] = s[m];
+    coef[4 * m + 2] = 3.0 * d - 2.0 * s[m] - s[m + 1];
+    coef[4 * m + 3] = s[m] + s[m + 1] - 2.0 * d;
+  }
+  coef[4 * (n - 1) + 0] = y[n - 1];
+  coef[4 * (n - 1) + 1] = s[n - 1];
+}
+
+std::string Eam::load(const char *path) {
+  std::ifstream fd(path);
+  if (!fd) return std::string("cannot open setfl file ") + path;
+  std::string line;
+  for (int k = 0; k < 3; ++k)
+    if (!std::getline(fd, line)) return "setfl file: missing comment lines";
+  if (!std::getline(fd, line)) return "setfl file: missing element line";
+  {
+    std::istringstream ss(line);
+    if (!(ss >> nel) || nel < 1 || nel > 16) return "setfl file: bad element count";
+    names.resize(nel);
+    for (auto &nm : names)
+      if (!(ss >> nm)) return "setfl file: fewer element names than elements";
+  }
+  if (!(fd >> nrho >> drho >> nr >> dr >> rc) || nrho < 5 || nr < 5 || !(drho > 0) || !(dr > 0) || !(rc > 0))
+    return "setfl file: bad table header";
+  mass.assign(nel, 0.0);
+  F.assign(nel, {});
+  f.assign(nel, {});
+  for (int e = 0; e < nel; ++e) {
+    double z, a;
+    std::string lat;
+    if (!(fd >> z >> mass[e] >> a >> lat)) return "setfl file: bad element header";
+    F[e].resize(nrho);
+    for (auto &v : F[e])
+      if (!(fd >> v)) return "setfl file: too few F(rho) values";
+    f[e].resize(nr);
+    for (auto &v : f[e])
+      if (!(fd >> v)) return "setfl file: too few f(r) values";
+  }
+  z2r.assign(nel * (nel + 1) / 2, {});
+  for (int a = 0; a < nel; ++a)
+    for (int b = 0; b <= a; ++b) {
+      auto &t = z2r[a * (a + 1) / 2 + b];
+      t.resize(nr);
+      for (auto &v : t)
+        if (!(fd >> v)) return "setfl file: too few r*phi(r) values";
+    }
+  return "";
+}
+
 }  // namespace ephgb
+

@@ -100,6 +100,28 @@ struct Grid {
   int save_temperature(const char *path, int n) const;
 };
 
+// Cubic Hermite table of knots y (spacing h): per interval m the coefficients
+// {c0, c1, c2, c3} of y(p) = c0 + p (c1 + p (c2 + p c3)) in the local
+// coordinate p = x/h - m in [0, 1]; knot slopes from the five-point central
+// difference (one-sided at the ends); the last entry continues the last knot
+// linearly.  dy/dx = (c1 + p (2 c2 + 3 p c3)) / h.
+void hermite_table(const std::vector<double> &y, std::vector<double> &coef);
+
+// eam/alloy potential read from a setfl file (the LAMMPS format: 3 comment
+// lines; "N el1 el2 ..."; "Nrho drho Nr dr cutoff"; per element "Z mass a
+// lattice", Nrho values of F(rho), Nr values of f(r); then r*phi(r) for every
+// pair a >= b, Nr values each).
+struct Eam {
+  int nel = 0;
+  std::vector<std::string> names;
+  std::vector<double> mass;
+  long nrho = 0, nr = 0;
+  double drho = 0, dr = 0, rc = 0;
+  std::vector<std::vector<double>> F, f;  // knots per element
+  std::vector<std::vector<double>> z2r;   // r*phi knots per pair a*(a+1)/2 + b, a >= b
+  std::string load(const char *path);
+};
+
 // Parsed `fix ID group eph seed flags model rho_e C_e kappa_e T_e NX NY NZ
 // T_infile freq T_out beta_file A B ...` (fix_eph.cpp:36-58, :61-241).
 struct FixArgs {

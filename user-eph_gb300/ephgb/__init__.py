@@ -29,7 +29,7 @@ FIELDS = {"x": (0, 3), "v": (1, 3), "f": (2, 3), "xi": (3, 3), "f_eph": (4, 3), 
           "w": (7, 3), "array": (8, 8), "T": (9, None), "f_ext": (10, 3)}
 SPLINES = {"rho_r": 0, "rho_r_sq": 1, "beta": 2, "alpha": 3}
 COUNTERS = {"rho_cutoff": 0, "T_clamp": 1, "build": 2, "wrap": 3}
-PHASES = ("integrate", "bin", "density", "friction_w", "forces", "deposit", "fdm")
+PHASES = ("integrate", "bin", "density", "friction_w", "forces", "deposit", "fdm", "pair")
 
 
 class EphError(RuntimeError):
@@ -73,6 +73,8 @@ SIGNATURES = {
     "eph_get_counter": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_long)]),
     "eph_set_capacity": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "eph_set_graph": (C.c_int, [C.c_void_p, C.c_int]),
+    "eph_set_pair_eam": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_char_p)]),
+    "eph_pair_energy": (C.c_int, [C.c_void_p, _dp]),
     "eph_set_threads_per_atom": (C.c_int, [C.c_void_p, C.c_int]),
     "eph_get_threads_per_atom": (C.c_int, [C.c_void_p, _ip]),
     "eph_autotune": (C.c_int, [C.c_void_p, _ip]),
@@ -251,7 +253,7 @@ class FixEPH:
     device-resident."""
 
     def __init__(self, words, atoms=None, dt=0.001, mass=None, boxlo=None, boxhi=None, skin=1.0,
-                 boltz=workloads.BOLTZ, ftm2v=workloads.FTM2V, groupbit=1, device=0, mode=MODE_FAST):
+                 boltz=workloads.BOLTZ, ftm2v=workloads.FTM2V, groupbit=1, device=0, mode=MODE_FAST, eam=None):
         L = lib()
         self.L = L
         if atoms is not None:
@@ -275,6 +277,8 @@ class FixEPH:
         self._check(rc)
         self.n = 0
         self.ncells = grid_cells(words)
+        if eam is not None:  # (setfl path, [element per type])
+            self.set_pair_eam(*eam)
         if atoms is not None:
             self.set_atoms(atoms.x, atoms.v, atoms.type, atoms.mask)
 
@@ -400,6 +404,16 @@ class FixEPH:
 
     def set_graph(self, on=True):
         self._check(self.L.eph_set_graph(self.h, 1 if on else 0))
+
+    def set_pair_eam(self, path, elements):
+        """eam/alloy pair force for eph_step (call before set_atoms)"""
+        arr = (C.c_char_p * len(elements))(*[e.encode() for e in elements])
+        self._check(self.L.eph_set_pair_eam(self.h, path.encode(), len(elements), arr))
+
+    def pair_energy(self):
+        out = C.c_double()
+        self._check(self.L.eph_pair_energy(self.h, C.byref(out)))
+        return out.value
 
     def set_threads_per_atom(self, tpa):
         self._check(self.L.eph_set_threads_per_atom(self.h, int(tpa)))

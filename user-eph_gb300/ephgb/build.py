@@ -24,7 +24,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompile
                      "-I" + INCLUDE]
 CXX_FLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-std=c++17", "-I" + INCLUDE]
 
-SOURCES = [("eph_ctx.cu", "nvcc"), ("eph_adjoint.cu", "nvcc"), ("eph_noalloc.cu", "nvcc"), ("eph_host.cpp", "cxx")]
+SOURCES = [("eph_ctx.cu", "nvcc"), ("eph_adjoint.cu", "nvcc"), ("eph_eam.cu", "nvcc"), ("eph_noalloc.cu", "nvcc"), ("eph_host.cpp", "cxx")]
 
 
 def _newer(target, deps):

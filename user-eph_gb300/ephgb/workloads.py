@@ -212,3 +212,50 @@ def write_grid_parameters(path, n=1001, dT=10.0, C0=3.5e-6, T0=3000.0, kappa0=0.
         for c, k in zip(C, K):
             f.write(f"{c:.6e} {k:.6e}\n")
     return path
+
+
+# Sutton-Chen parameters for Ni (A. P. Sutton and J. Chen, Phil. Mag. Lett. 61,
+# 139 (1990)): E = eps [1/2 sum_ij (a/r)^n - c sum_i sqrt(rho_i)], rho_i =
+# sum_j (a/r)^m — an EAM form with phi(r) = eps (a/r)^n, f(r) = (a/r)^m,
+# F(rho) = -c eps sqrt(rho).
+SC_NI = dict(eps=1.5707e-2, a=3.52, c=39.432, n=9, m=6)
+
+
+def _taper(r, r_on, rc):
+    """1 below r_on, 0 from rc on, C2 smoothstep between."""
+    x = np.clip((r - r_on) / (rc - r_on), 0.0, 1.0)
+    return 1.0 - x ** 3 * (10.0 - 15.0 * x + 6.0 * x * x)
+
+
+def write_eam_sutton_chen(path: str, rc: float = 6.0, r_on: float = 5.0, nr: int = 3001, nrho: int = 2001,
+                          rho_max: float = 500.0, r_core: float = 1.5, p=SC_NI, element="Ni", z=28,
+                          mass=NI_MASS) -> str:
+    """Write a setfl (eam/alloy) file of the Sutton-Chen Ni potential, cut
+    smoothly between r_on and rc.  Below r_core the tabulated r*phi(r) and
+    f(r) continue linearly (finite, repulsive)."""
+    dr = rc / (nr - 1)
+    drho = rho_max / (nrho - 1)
+    r = np.arange(nr) * dr
+    rr = np.maximum(r, r_core)
+    s = _taper(rr, r_on, rc)
+    f = (p["a"] / rr) ** p["m"] * s
+    zphi = rr * p["eps"] * (p["a"] / rr) ** p["n"] * s
+    # linear continuation below r_core (slopes at r_core)
+    k = r < r_core
+    h = 1e-6
+    fs = ((p["a"] / (r_core + h)) ** p["m"] - (p["a"] / (r_core - h)) ** p["m"]) / (2 * h)
+    zs = ((r_core + h) * p["eps"] * (p["a"] / (r_core + h)) ** p["n"] -
+          (r_core - h) * p["eps"] * (p["a"] / (r_core - h)) ** p["n"]) / (2 * h)
+    f[k] = f[k] + fs * (r[k] - r_core)
+    zphi[k] = zphi[k] + zs * (r[k] - r_core)
+    F = -p["c"] * p["eps"] * np.sqrt(np.arange(nrho) * drho)
+    with open(path, "w") as fd:
+        fd.write("# Sutton-Chen Ni (Sutton & Chen 1990), eam/alloy tables\n")
+        fd.write(f"# eps {p['eps']} eV, a {p['a']} A, c {p['c']}, n {p['n']}, m {p['m']}; "
+                 f"C2 cut-off between {r_on} and {rc} A\n#\n")
+        fd.write(f"1 {element}\n")
+        fd.write(f"{nrho} {drho!r} {nr} {dr!r} {rc!r}\n")
+        fd.write(f"{z} {mass!r} {p['a']!r} fcc\n")
+        for arr in (F, f, zphi):
+            fd.write("\n".join(repr(float(v)) for v in arr) + "\n")
+    return path
