@@ -39,6 +39,11 @@ extern "C" {
 /* where a buffer lives */
 #define EPH_HOST 0
 #define EPH_DEVICE 1
+/* host pointer, copy queued on the context's stream only: the host buffer
+ * must stay valid and unchanged (put) or unread (get) until the next call that
+ * synchronises (eph_get with EPH_HOST, eph_synchronize, eph_compute_vector);
+ * use pinned memory for it to overlap anything */
+#define EPH_HOST_ASYNC 2
 
 /* source of the Gaussian deviates xi of the random force */
 #define EPH_XI_DEVICE_RNG 0 /* counter-based Philox4x32-10 on the device, seeded by the fix seed */
@@ -99,7 +104,7 @@ const char *eph_status_string(int status);
  * engine's atom storage. */
 int eph_set_atoms(eph_ctx *ctx, int n, const double *x, const double *v, const int *type, const int *mask);
 
-/* Copy a field in or out (where = EPH_HOST or EPH_DEVICE pointer). */
+/* Copy a field in or out (where = EPH_HOST, EPH_HOST_ASYNC or EPH_DEVICE pointer). */
 int eph_put(eph_ctx *ctx, int field, const double *src, int where);
 int eph_get(eph_ctx *ctx, int field, double *dst, int where);
 

@@ -150,3 +150,38 @@ def test_threads_per_atom_variants(built, beta_file):
     f_before = gpu.get("f")
     assert gpu.autotune() in (1, 2, 4, 8)
     np.testing.assert_array_equal(gpu.get("f"), f_before)
+
+
+def test_async_host_copies(built, beta_file):
+    """Hooks driven with queued host copies (EPH_HOST_ASYNC, one
+    synchronisation per step) give what the synchronous copies give."""
+    import torch
+
+    words, at, dt = scenario("c1_small", beta_file)
+    n = at.n
+    out = []
+    for asynchronous in (False, True):
+        fix = ephgb.FixEPH(words, at, dt=dt)
+        x = torch.from_numpy(at.x.copy()).pin_memory().numpy()
+        v = torch.from_numpy(at.v.copy()).pin_memory().numpy()
+        f = torch.zeros((n, 3), dtype=torch.float64).pin_memory().numpy()
+        for _ in range(4):
+            fix.put("x", x, asynchronous)
+            fix.put("v", v, asynchronous)
+            fix.put("f", f, asynchronous)
+            fix.initial_integrate()
+            fix.post_force()
+            fix.final_integrate()
+            fix.end_of_step()
+            if asynchronous:
+                fix.get_async("x", x)
+                fix.get_async("v", v)
+                fix.get_async("f", f)
+                fix.synchronize()
+            else:
+                fix.get("x", out=x)
+                fix.get("v", out=v)
+                fix.get("f", out=f)
+        out.append((x.copy(), v.copy(), f.copy(), fix.get("T")))
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)

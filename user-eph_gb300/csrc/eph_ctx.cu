@@ -805,6 +805,7 @@ int eph_put(eph_ctx *c, int field, const double *src, int where) {
     const size_t nc = (size_t)c->grid.ntotal;
     CUDA_TRY(c, cudaMemcpyAsync(c->T0.p, src, nc * 8,
                                 where == EPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+    if (where == EPH_HOST) CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return EPH_OK;
   }
   int r = require_atoms(c);
@@ -827,7 +828,8 @@ int eph_put(eph_ctx *c, int field, const double *src, int where) {
     default: return fail(c, EPH_ERR_ARG, "field cannot be written");
   }
   const double *s = src;
-  if (where == EPH_HOST) {
+  const bool host = where == EPH_HOST || where == EPH_HOST_ASYNC;
+  if (host) {
     CUDA_TRY(c, cudaMemcpyAsync(c->stage.p, src, sizeof(double) * 3 * (size_t)c->n, cudaMemcpyHostToDevice,
                                 c->stream));
     s = c->stage.p;
@@ -848,7 +850,8 @@ int eph_get(eph_ctx *c, int field, double *dst, int where) {
   int r = require_atoms(c);
   if (r) return r;
   const int n = c->n;
-  double *d = where == EPH_HOST ? c->stage.p : dst;
+  const bool host = where == EPH_HOST || where == EPH_HOST_ASYNC;
+  double *d = host ? c->stage.p : dst;
   size_t count = 3 * (size_t)n;
   switch (field) {
     case EPH_FIELD_X: k_unpack3<<<nblocks(n), BLOCK, 0, c->stream>>>(n, c->x.p, d); break;
@@ -870,8 +873,8 @@ int eph_get(eph_ctx *c, int field, double *dst, int where) {
     default: return fail(c, EPH_ERR_ARG, "field cannot be read");
   }
   CUDA_TRY(c, cudaGetLastError());
-  if (where == EPH_HOST)
-    CUDA_TRY(c, cudaMemcpyAsync(dst, c->stage.p, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+  if (host) CUDA_TRY(c, cudaMemcpyAsync(dst, c->stage.p, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+  if (where == EPH_HOST_ASYNC) return EPH_OK;  // complete (and checked) at the next synchronising call
   return check_device(c);
 }
 

@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(128)
     double ex, ey, ez;
     image_vector(P, xi, x[j], u >> IDX_BITS, ex, ey, ez);
     const double r2 = fma(ez, ez, fma(ey, ey, ex * ex));
-    const double r = sqrt(r2), rinv = recip_nr(r), q = r * E.inv_dr;
+    const double rinv = rsqrt(r2), r = r2 * rinv, q = r * E.inv_dr;
     const int b = E.map[type[j]];
     double fb, dfb, fa, dfa, z, dz;
     herm(E.f + (size_t)b * E.nr, E.nr, q, fb, dfb);

@@ -23,7 +23,7 @@ EPH_OK = 0
 STATUS = {0: "EPH_OK", 1: "EPH_ERR_ARG", 2: "EPH_ERR_FILE", 3: "EPH_ERR_UNSUPPORTED_MODEL", 4: "EPH_ERR_CAPACITY",
           5: "EPH_ERR_TIMEOUT", 6: "EPH_ERR_CUDA", 7: "EPH_ERR_STATE", 8: "EPH_ERR_RANGE"}
 MODE_EXACT, MODE_FAST = 0, 1
-HOST, DEVICE = 0, 1
+HOST, DEVICE, HOST_ASYNC = 0, 1, 2
 XI_DEVICE_RNG, XI_GIVEN = 0, 1
 FIELDS = {"x": (0, 3), "v": (1, 3), "f": (2, 3), "xi": (3, 3), "f_eph": (4, 3), "f_rng": (5, 3), "rho": (6, 1),
           "w": (7, 3), "array": (8, 8), "T": (9, None), "f_ext": (10, 3)}
@@ -302,13 +302,25 @@ class FixEPH:
         self.n = x.shape[0]
 
     # ---- data movement
-    def put(self, field, arr):
+    def put(self, field, arr, asynchronous=False):
+        """asynchronous: the copy is queued; `arr` (a contiguous float64
+        array, ideally pinned) must stay unchanged until the next
+        synchronising call"""
         fid, _ = FIELDS[field]
         if hasattr(arr, "data_ptr"):  # torch tensor on the device
             self._check(self.L.eph_put(self.h, fid, C.c_void_p(arr.data_ptr()), DEVICE))
             return
         a = np.ascontiguousarray(arr, dtype=np.float64)
-        self._check(self.L.eph_put(self.h, fid, _ptr(a), HOST))
+        if asynchronous and a is not arr:
+            raise ValueError("an asynchronous put needs a contiguous float64 array")
+        self._check(self.L.eph_put(self.h, fid, _ptr(a), HOST_ASYNC if asynchronous else HOST))
+
+    def get_async(self, field, out):
+        """queue a copy into `out` (contiguous float64, ideally pinned); it
+        is complete after the next synchronising call"""
+        fid, _ = FIELDS[field]
+        self._check(self.L.eph_get(self.h, fid, _ptr(out), HOST_ASYNC))
+        return out
 
     def get(self, field, out=None):
         fid, k = FIELDS[field]

@@ -132,20 +132,22 @@ void FixEPHGB::setup(int) { upload_atoms(); }
 void FixEPHGB::initial_integrate(int) {
   if (eph_flag & 0x08) return;
   if (nlocal_dev != atom->nlocal) upload_atoms();
-  check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST), "put x");
-  check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "put v");
-  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "put f");
+  // queued copies; the engine's arrays are read again only after the
+  // synchronising get at the end of the hook
+  check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "put x");
+  check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST_ASYNC), "put v");
+  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
   check(eph_initial_integrate(ctx), "initial_integrate");
-  check(eph_get(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST), "get x");
+  check(eph_get(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "get x");
   check(eph_get(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "get v");
 }
 
 void FixEPHGB::post_force(int) {
   // the engine re-neighboured this step: atoms may be re-sorted or wrapped
   if (neighbor->ago == 0 || nlocal_dev != atom->nlocal) upload_atoms();
-  check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST), "put x");
-  check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "put v");
-  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "put f");
+  check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "put x");
+  check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST_ASYNC), "put v");
+  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
   int source = EPH_XI_DEVICE_RNG;
   if (xi_on_host && (eph_flag & 0x02)) {
     // the engine's own Gaussian stream, three per in-group atom in atom
@@ -164,7 +166,7 @@ void FixEPHGB::post_force(int) {
 
 void FixEPHGB::final_integrate() {
   if (eph_flag & 0x08) return;
-  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "put f");
+  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
   check(eph_final_integrate(ctx), "final_integrate");
   check(eph_get(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "get v");
 }
