@@ -484,6 +484,47 @@ def run_md_eam(args, dev):
                 "pair_energy_per_atom": fix.pair_energy() / atoms.n}
 
 
+def run_c1(args, dev, threads):
+    """The reference's CPU-runnable case: fcc Ni 10^3 cells (4,000 atoms),
+    300 K, dt 1 fs, 10^3 grid, flags 7 — 1,000 steps on the GPU (graph
+    replay) against the CPU restatement on one host core and on all of them
+    (a bounded sample of steps)."""
+    import torch
+
+    import ephgb
+    from ephgb import workloads as W
+    from oracle.bindings import OracleFix
+
+    with tempfile.TemporaryDirectory() as wd:
+        bf = W.write_beta_file(os.path.join(wd, "synth.beta"))
+        at = W.fcc_lattice(10, seed=SEED)
+        words = W.fix_args(bf, seed=SEED, flags=7, grid=(10, 10, 10))
+        fix = ephgb.FixEPH(words, at, dt=0.001, device=dev)
+        stream = torch.cuda.Stream()
+        fix.set_stream(stream.cuda_stream)
+        fix.set_graph(True)
+        fix.step(20)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fix.step(1000)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        gpu = at.n * 1000 / (e0.elapsed_time(e1) / 1000.0)
+        cpu = {}
+        for th in (1, threads):
+            ref = OracleFix(words, at, 0.001, threads=th)
+            ref.step(None)
+            t0 = ref.seconds(0)
+            for _ in range(100):
+                ref.step(None)
+            cpu[th] = at.n * 100 / (ref.seconds(0) - t0)
+        return {"workload": "fcc Ni 10^3 cells (4,000 atoms), 300 K, dt 1 fs, FDM 10^3, flags 7, model 4",
+                "value": gpu, "unit": METRIC, "gpu_steps": 1000, "cpu_1_core": cpu[1], "cpu_all_cores": cpu[threads],
+                "cores": threads, "cpu_sample": "100 steps, fix hooks only", "speedup_vs_all_cores": gpu / cpu[threads],
+                "ms_per_step": at.n / gpu * 1000.0}
+
+
 def cpu_baseline(threads, steps=1, warm=1):
     """The CPU restatement (oracle port) on the same workload: `steps` steps
     of the full system after `warm` warm-up steps; time of the fix's own hooks
@@ -523,6 +564,7 @@ def main():
     ap.add_argument("--no-adjoint-fd", action="store_true", help="skip the finite-difference check")
     ap.add_argument("--no-fit", action="store_true", help="omit the batched adjoint fitting leg")
     ap.add_argument("--no-md", action="store_true", help="omit the full-MD (EAM pair force) leg")
+    ap.add_argument("--no-c1", action="store_true", help="omit the 4,000-atom CPU-runnable case")
     ap.add_argument("--only-md", action="store_true", help="run the full-MD leg alone")
     ap.add_argument("--md-steps", type=int, default=50)
     ap.add_argument("--only-fit", action="store_true", help="run the batched adjoint fitting leg alone")
@@ -610,6 +652,8 @@ def main():
             line["batched"]["value"] = float(t.item())
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)), fd=not args.no_adjoint_fd)
+    if rank == 0 and not args.no_c1:
+        line["c1"] = run_c1(args, int(os.environ.get("LOCAL_RANK", rank)), threads)
     if rank == 0 and not args.no_md:
         line["md_eam"] = run_md_eam(args, int(os.environ.get("LOCAL_RANK", rank)))
     if rank == 0 and not args.no_fit:

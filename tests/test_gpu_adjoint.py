@@ -317,3 +317,68 @@ def test_batch_equals_the_adjoints_run_alone(built, tmp_path):
             g = adj.gradients(0)
             for k in g:
                 np.testing.assert_array_equal(np.asarray(g[k]), np.asarray(alone[r][4][k]), err_msg=k)
+
+
+def test_two_element_gradient(built, tmp_path):
+    """A Ni/Fe beta file (the tables of both elements in the pair terms):
+    the knot gradients of each element against central differences."""
+    beta = W.write_beta_file(str(tmp_path / "NiFe.beta"), elements=("Ni", "Fe"), numbers=(28, 26), n_rho=16,
+                             n_beta=24, drho=0.3 / 23, beta_fn=curved_beta)
+    at = W.fcc_lattice(5, seed=71)
+    at.type = np.where(np.arange(at.n) % 4 == 1, 2, 1).astype(np.int32)
+    at.mass = np.array([0.0, W.NI_MASS, 55.845])
+    words = W.fix_args(beta, flags=7, T_e=2000.0, grid=(4, 4, 4), elements=("Ni", "Fe"))
+    fix = ephgb.FixEPH(words, atoms=at, dt=0.001)
+    adj = Adjoint(fix, checkpoint_every=5)
+    E, T = adj.forward(STEPS)
+    wE, wT = weights(E, T)
+    adj.backward(wE, wT)
+    scale = loss_scale(E, T, wE, wT)
+    eps = 2.0 ** -52 * scale
+    grads = [adj.gradients(elem) for elem in (0, 1)]  # before the forward passes of the differences
+    for elem in (0, 1):
+        g = grads[elem]
+        r0, b0 = (c.copy() for c in adj.columns[elem])
+
+        def loss(r, b):
+            adj.set_knots(elem, r, b)
+            E2, T2 = adj.forward(STEPS)
+            return float(wE @ E2 + wT @ T2)
+
+        fd_b, noise_b = np.zeros(b0.size), np.zeros(b0.size)
+        for k in range(b0.size):
+            d = 1e-6 * b0[k]
+            p, m = b0.copy(), b0.copy()
+            p[k] += d
+            m[k] -= d
+            fd_b[k] = (loss(r0, p) - loss(r0, m)) / (2 * d)
+            noise_b[k] = eps / d
+        floor = np.abs(r0[r0 != 0]).min()
+        fd_r, noise_r = np.zeros(r0.size), np.zeros(r0.size)
+        for k in range(r0.size):
+            d = 1e-6 * max(abs(r0[k]), floor)
+            p, m = r0.copy(), r0.copy()
+            p[k] += d
+            m[k] -= d
+            fd_r[k] = (loss(p, b0) - loss(m, b0)) / (2 * d)
+            noise_r[k] = eps / d
+        adj.set_knots(elem, r0, b0)
+        errs = compare({"beta_knots": g["beta_knots"], "rho_knots": g["rho_knots"]},
+                       {"beta_knots": fd_b, "rho_knots": fd_r}, {"beta_knots": noise_b, "rho_knots": noise_r})
+        assert max(errs.values()) <= TOL, (elem, errs)
+
+
+@pytest.mark.parametrize("case", ["model1", "coloured", "eam"])
+def test_unsupported_contexts_are_refused(built, tmp_path, case):
+    beta = W.write_beta_file(str(tmp_path / "b.beta"), n_rho=16, n_beta=24, drho=0.3 / 23)
+    at = W.fcc_lattice(6, seed=81)
+    words = W.fix_args(beta, flags=7, grid=(4, 4, 4), model=1 if case == "model1" else 4)
+    eam = None
+    if case == "coloured":
+        words[2], words[5] = "eph/coloured/exp", "0.005"
+    if case == "eam":
+        eam = (W.write_eam_sutton_chen(str(tmp_path / "sc.eam")), ["Ni"])
+    fix = ephgb.FixEPH(words, atoms=at, dt=0.001, eam=eam)
+    with pytest.raises(ephgb.EphError) as e:
+        Adjoint(fix)
+    assert e.value.status == 3  # EPH_ERR_UNSUPPORTED_MODEL

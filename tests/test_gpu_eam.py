@@ -90,3 +90,21 @@ def test_with_the_fix_and_graph_replay(built, setfl, beta_file):
         out.append((fix.get("x"), fix.get("v"), fix.get("T"), fix.pair_energy()))
     for a, b in zip(out[0], out[1]):
         np.testing.assert_array_equal(a, b)
+
+
+def test_setup_errors(built, setfl, beta_file, tmp_path):
+    words = W.fix_args(beta_file, flags=0, grid=(4, 4, 4))
+    at = W.fcc_lattice(6, seed=66)
+    with pytest.raises(ephgb.EphError) as e:
+        ephgb.FixEPH(words, at, dt=0.001, eam=(str(tmp_path / "missing.eam"), ["Ni"]))
+    assert e.value.status == 2  # EPH_ERR_FILE
+    with pytest.raises(ephgb.EphError) as e:
+        ephgb.FixEPH(words, at, dt=0.001, eam=(setfl, ["Cu"]))
+    assert e.value.status == 1  # EPH_ERR_ARG: element not in the file
+    with pytest.raises(ephgb.EphError) as e:
+        ephgb.FixEPH(words, W.fcc_lattice(5, seed=66), dt=0.001, eam=(setfl, ["Ni"]))
+    assert e.value.status == 1  # box narrower than three 6 A cut-offs
+    fix = ephgb.FixEPH(words, at, dt=0.001)
+    with pytest.raises(ephgb.EphError) as e:
+        fix.set_pair_eam(setfl, ["Ni"])
+    assert e.value.status == 7  # EPH_ERR_STATE: after the atoms
