@@ -175,12 +175,25 @@ int launch_final(eph_ctx *c) {
   return EPH_OK;
 }
 
-template <bool FAST, bool MULTI>
-void launch_density_t(eph_ctx *c, int xi_mode) {
-  k_density<FAST, MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+// FAST mode with one lane per atom folds stage 1 (the friction pre-vector)
+// into the density sweep
+bool fused_friction(const eph_ctx *c) {
+  return c->mode == EPH_MODE_FAST && c->tpa == 1 && c->args.model == 4 && (c->P.flags & FLAG_FRICTION) &&
+         c->fuse_w;
+}
+
+template <bool FAST, bool MULTI, bool FUSE>
+void launch_density_f(eph_ctx *c, int xi_mode) {
+  k_density<FAST, MULTI, FUSE><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
       c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p,
       c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,
-      c->wrapflag.p, c->d_err.p, c->counters.p);
+      c->wrapflag.p, c->d_err.p, c->counters.p, c->v.p);
+}
+
+template <bool FAST, bool MULTI>
+void launch_density_t(eph_ctx *c, int xi_mode) {
+  if (FAST && fused_friction(c)) launch_density_f<FAST, MULTI, true>(c, xi_mode);
+  else launch_density_f<FAST, MULTI, false>(c, xi_mode);
 }
 
 template <bool FAST, bool MULTI, bool FRIC, bool RAND>
@@ -300,7 +313,7 @@ int launch_pair_sweeps(eph_ctx *c, int xi_mode) {
     CUDA_TRY(c, cudaGetLastError());
     return EPH_OK;
   }
-  if (c->P.flags & FLAG_FRICTION) {
+  if ((c->P.flags & FLAG_FRICTION) && !fused_friction(c)) {
     PhaseScope ps(c, EPH_PHASE_FRICTION_W);
     ps.launched();
     launch_friction_w(c);

@@ -65,6 +65,8 @@ struct eph_ctx {
   // and whether it follows the atom count (eph_set_threads_per_atom)
   int tpa = 1;
   bool tpa_auto = true;
+  // FAST mode, one lane per atom: stage 1 folded into the density sweep
+  bool fuse_w = true;
 
   int n = 0;
   DevBuf<D4> x, v, f, xhold, f_eph, f_rng, xi, fext, A, Bw;

@@ -190,7 +190,12 @@ __global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_coun
 // Candidates: the first CAND_SMEM rows of an atom live in shared memory
 // ([CAND_SMEM][blockDim]), further ones in the atom's own rows of pj (read
 // back before pass 2 overwrites them: pair slot <= candidate slot).
-template <bool FAST, bool MULTI>
+// FUSE_W (FAST mode): the friction pre-vector of stage 1 in the same pass,
+// w_i = (alpha_i / rho_i) sum_j H_ij (e.(v_i - v_j)) e with H_ij = rho_j(r^2)/r^2 —
+// it needs only this atom's density, so the sum rides along with rho and the
+// separate sweep over the pair cache is saved (the density pass leaves FP64
+// issue slots free while its candidate pass runs).
+template <bool FAST, bool MULTI, bool FUSE_W = false>
 __global__ void __launch_bounds__(128) k_density(
     StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
     const BinEntry *__restrict__ bins, const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(128) k_density(
     D4 *__restrict__ pe, double2 *__restrict__ pg, int *__restrict__ nshort, D4 *__restrict__ A,
     D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell,
     double *__restrict__ Te_i, int *__restrict__ wrapflag, unsigned *__restrict__ err,
-    unsigned long long *__restrict__ counters) {
+    unsigned long long *__restrict__ counters, const D4 *__restrict__ v = nullptr) {
   __shared__ unsigned s_cand[CAND_SMEM * 128];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int t = threadIdx.x, nt = blockDim.x;
@@ -279,6 +284,9 @@ __global__ void __launch_bounds__(128) k_density(
   }
   __syncwarp();
   // pass 2: exact FP64 test, density and pair cache, in lockstep
+  D4 vi{0.0, 0.0, 0.0, 0.0};
+  if (FUSE_W && active) vi = v[i];
+  double Sx = 0.0, Sy = 0.0, Sz = 0.0;
   const int nmax = __reduce_max_sync(0xffffffffu, nc);
   for (int k = 0; k < nmax; ++k) {
     if (k < nc) {
@@ -306,8 +314,16 @@ __global__ void __launch_bounds__(128) k_density(
         pj[slot] = u;
         if (FAST) {
           const double inv_r2 = recip_nr(r2);
-          pe[slot] = D4{ex, ey, ez, rji * inv_r2};
+          const double H = rji * inv_r2;
+          pe[slot] = D4{ex, ey, ez, H};
           if (MULTI) pg[slot] = make_double2(rij * inv_r2, 0.0);
+          if (FUSE_W) {
+            const D4 vj = v[j];
+            const double s = H * dot3_fma(ex, ey, ez, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
+            Sx = fma(s, ex, Sx);
+            Sy = fma(s, ey, Sy);
+            Sz = fma(s, ez, Sz);
+          }
         } else {
           pe[slot] = D4{ex, ey, ez, r2};
           pg[slot] = make_double2(rji, rij);
@@ -343,7 +359,10 @@ __global__ void __launch_bounds__(128) k_density(
     Te_i[i] = T_e[c];
   }
   A[i] = D4{rho, alpha, xi3[0], xi3[1]};
-  Bw[i] = D4{xi3[2], 0.0, 0.0, 0.0};
+  if (FUSE_W && active && pos_double(rho))  // k_friction_w's rule: w stays 0 unless rho_i > 0
+    Bw[i] = D4{xi3[2], alpha * Sx, alpha * Sy, alpha * Sz};
+  else
+    Bw[i] = D4{xi3[2], 0.0, 0.0, 0.0};
   rho_out[i] = rho;
   beta_out[i] = beta;
 }
