@@ -20,8 +20,10 @@ TOL = 1e-12
 ATOM_KEYS = ("rho", "w", "f_eph", "f_rng", "f", "x", "v", "array")
 
 
-def run_pair(words, at, dt, mode, steps, check, seed=5):
+def run_pair(words, at, dt, mode, steps, check, seed=5, tpa=0):
     gpu = ephgb.FixEPH(words, at, dt=dt, mode=mode)
+    if tpa:
+        gpu.set_threads_per_atom(tpa)
     ref = OracleFix(words, at, dt)
     ng = n_in_group(at)
     rnd = int(words[4], 0) & 2
@@ -57,8 +59,12 @@ def test_exact_mode_bitwise_first_step(built, beta_file, beta_file_2el, name):
     run_pair(words, at, dt, ephgb.MODE_EXACT, 6 if name != "pka" else 30, check)
 
 
+@pytest.mark.parametrize("tpa", [0, 1])
 @pytest.mark.parametrize("name", SCENARIOS)
-def test_fast_mode_within_tolerance(built, beta_file, beta_file_2el, name):
+def test_fast_mode_within_tolerance(built, beta_file, beta_file_2el, name, tpa):
+    """tpa 0: lanes per atom from the atom count (4 for these small systems);
+    tpa 1: one lane per atom, stage 1 folded into the density sweep (as at the
+    bench size)"""
     words, at, dt = scenario(name, beta_file, beta_file_2el)
 
     def check(s, gpu, ref):
@@ -66,7 +72,7 @@ def test_fast_mode_within_tolerance(built, beta_file, beta_file_2el, name):
             assert rel_err(gpu.get(k), ref.get(k)) <= TOL, (s, k, rel_err(gpu.get(k), ref.get(k)))
         assert rel_err(gpu.get("T"), ref.get("T")) <= TOL
 
-    run_pair(words, at, dt, ephgb.MODE_FAST, 6 if name != "pka" else 30, check)
+    run_pair(words, at, dt, ephgb.MODE_FAST, 6 if name != "pka" else 30, check, tpa=tpa)
 
 
 def test_c1_config_fast_and_exact(built, beta_file):
