@@ -3,6 +3,7 @@
 // on one CUDA stream.  Device layout (n atoms, K = pair capacity):
 //   x, v, f, xhold, f_eph, f_rng, xi   D4[n]       (x.w holds the element index)
 //   A, Bw                              D4[n]       per-atom records read by neighbours
+//   Mm, G                              D4[2n]      FAST one-lane sweeps: M_i, gathered records
 //   pj, pe, pg                         [K][n]      in-cutoff pairs of the step
 //   bins                               [nbins][bcap] BinEntry
 //   grid T (two buffers), kappa, rho_e*C_e, S, flag, dT, fixed-point deposits
@@ -187,7 +188,7 @@ void launch_density_f(eph_ctx *c, int xi_mode) {
   k_density<FAST, MULTI, FUSE><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
       c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p,
       c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,
-      c->wrapflag.p, c->d_err.p, c->counters.p, c->v.p);
+      c->wrapflag.p, c->d_err.p, c->counters.p, c->v.p, c->Mm.p, c->G.p);
 }
 
 template <bool FAST, bool MULTI>
@@ -199,6 +200,12 @@ void launch_density_t(eph_ctx *c, int xi_mode) {
 template <bool FAST, bool MULTI, bool FRIC, bool RAND>
 void launch_forces_t(eph_ctx *c) {
   const int tpa = FAST ? c->tpa : 1;
+  if (FAST && FRIC && fused_friction(c)) {
+    k_forces_m<MULTI, RAND><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+        c->P, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->Mm.p, c->G.p, c->Te_i.p, c->f.p, c->f_eph.p, c->f_rng.p,
+        c->f_dis.p, c->f_sto.p);
+    return;
+  }
   if (tpa == 1) {
     k_forces<FAST, MULTI, FRIC, RAND><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
         c->P, c->mask.p, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->Te_i.p, c->f.p, c->f_eph.p,
@@ -756,6 +763,8 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
     // follows the atom index afterwards
     CUDA_TRY(c, cudaMemsetAsync(c->f_dis.p, 0, sizeof(D4) * N, c->stream));
     CUDA_TRY(c, cudaMemsetAsync(c->f_sto.p, 0, sizeof(D4) * N, c->stream));
+    CUDA_TRY(c, c->Mm.alloc(2 * N));
+    CUDA_TRY(c, c->G.alloc(2 * N));
     CUDA_TRY(c, c->type.alloc(N));
     CUDA_TRY(c, c->mask.alloc(N));
     CUDA_TRY(c, c->nshort.alloc(N));

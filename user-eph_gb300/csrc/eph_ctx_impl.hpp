@@ -71,6 +71,9 @@ struct eph_ctx {
   int n = 0;
   DevBuf<D4> x, v, f, xhold, f_eph, f_rng, xi, fext, A, Bw;
   DevBuf<D4> f_dis, f_sto;  // coloured-noise memory (eph/coloured/exp)
+  // FAST mode, one lane per atom: M_i (2 x n: {xx,xy,xz,yy}, {yz,zz}) and the
+  // gathered records G_i ({a w, a xi_x}, {a xi_y, a xi_z, rho}, interleaved)
+  DevBuf<D4> Mm, G;
   bool have_fext = false, have_xi = false;
   DevBuf<int> type, mask, nshort, cell, tmap;
   DevBuf<double> rho, beta_i, Te_i, stage;

@@ -150,85 +150,16 @@ __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, 
 
 // -------------------------------------------------------- density sweep
 
-// Sort every bin's entries by atom index (one thread per bin, a handful of
-// entries each), so the candidate order below is fixed run to run.
-__global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbins) return;
-  int cnt = bin_count[b];
-  cnt = cnt < bcap ? cnt : bcap;
-  BinEntry *e = bins + (size_t)b * bcap;
-  for (int k = 1; k < cnt; ++k) {
-    const BinEntry v = e[k];
-    const unsigned key = v.idx & IDX_MASK;
-    int p = k;
-    while (p > 0 && (e[p - 1].idx & IDX_MASK) > key) {
-      e[p] = e[p - 1];
-      --p;
-    }
-    e[p] = v;
-  }
-}
-
-// calculate_environment (fix_eph.cpp:431-466) plus everything per atom the
-// later sweeps need.  One thread per atom, warps kept converged: a warp FP64
-// instruction costs the same whether 1 or 32 lanes are active, so the FP64
-// work must run in lockstep.
-//   pass 1 (FP32/integer): candidates from the 27 bins around the atom with an
-//     FP32 distance test padded by 1e-4 of rc^2, kept in shared memory; EXACT
-//     mode keeps them in ascending neighbour index (the order of the
-//     reference's list, so sums round identically), FAST mode in the fixed
-//     bin-stencil order of index-sorted bins
-//   pass 2 (FP64): the exact test r^2 < rc^2 with e = (x_j + image) - x_i, the
-//     density sum, and the pair cache of the in-cutoff pairs
-// Pair cache row k of atom i sits at k*n + i (coalesced across the warp):
-//   pj: neighbour index | image code << 27
-//   pe: e_ij and (EXACT) r^2 or (FAST) rho_j(r^2)/r^2
-//   pg: (EXACT) rho_j(r^2), rho_i(r^2); (FAST, several elements) rho_i(r^2)/r^2
-// A[i] = {rho_i, alpha_i (EXACT) | alpha_i/rho_i (FAST), xi_x, xi_y}
-// Bw[i] = {xi_z, w_i} (w written by the friction sweep)
-// Candidates: the first CAND_SMEM rows of an atom live in shared memory
-// ([CAND_SMEM][blockDim]), further ones in the atom's own rows of pj (read
-// back before pass 2 overwrites them: pair slot <= candidate slot).
-// FUSE_W (FAST mode): the friction pre-vector of stage 1 in the same pass,
-// w_i = (alpha_i / rho_i) sum_j H_ij (e.(v_i - v_j)) e with H_ij = rho_j(r^2)/r^2 —
-// it needs only this atom's density, so the sum rides along with rho and the
-// separate sweep over the pair cache is saved (the density pass leaves FP64
-// issue slots free while its candidate pass runs).
-template <bool FAST, bool MULTI, bool FUSE_W = false>
-__global__ void __launch_bounds__(128) k_density(
-    StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
-    const BinEntry *__restrict__ bins, const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
-    const D4 *__restrict__ xi_given, int xi_mode, const double *__restrict__ T_e, unsigned *__restrict__ pj,
-    D4 *__restrict__ pe, double2 *__restrict__ pg, int *__restrict__ nshort, D4 *__restrict__ A,
-    D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell,
-    double *__restrict__ Te_i, int *__restrict__ wrapflag, unsigned *__restrict__ err,
-    unsigned long long *__restrict__ counters, const D4 *__restrict__ v = nullptr) {
-  __shared__ unsigned s_cand[CAND_SMEM * 128];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int t = threadIdx.x, nt = blockDim.x;
-  if (i == 0) *wrapflag = 0;  // the binning kernel has read it
-  const bool valid = i < P.n;
-  const bool active = valid && (mask[i] & P.groupbit) != 0;
-  auto cget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : pj[(size_t)k * P.n + i]; };
-  auto cset = [&](int k, unsigned u) {
-    if (k < CAND_SMEM)
-      s_cand[k * nt + t] = u;
-    else
-      pj[(size_t)k * P.n + i] = u;
-  };
-  D4 xi = D4{0.0, 0.0, 0.0, 0.0};
-  if (valid) xi = x[i];
-  const int ei = (int)xi.w;
-  double rho = 0.0;
-  int ns = 0, nc = 0;
-  int4 Bi = make_int4(0, 0, 0, 0);
-  float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (active) {
-    Bi = atom_bin[i];
-    oi = atom_off[i];
-  }
-  // pass 1: candidates, FP32/integer work only, warp-uniform loop bounds
+// Pass 1 of the density sweep for atom i: the candidates j of the 27 bins
+// around its own whose FP32 distance passes the widened cut-off, appended
+// through cset (FAST: in the fixed bin-stencil order; EXACT: kept in
+// ascending neighbour index by insertion).  Returns their number.
+template <bool FAST, class Get, class Set>
+__device__ __forceinline__ int collect_candidates(const StepParams &P, int i, bool active, int4 Bi, float4 oi,
+                                                  const int *__restrict__ bin_count,
+                                                  const BinEntry *__restrict__ bins, unsigned *__restrict__ err,
+                                                  Get cget, Set cset) {
+  int nc = 0;
   for (int dz = -1; dz <= 1; ++dz) {
     const int Tz = Bi.z + dz, tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
     const int kz = Tz < 0 ? -1 : (Tz >= P.nb[2] ? 1 : 0);
@@ -282,11 +213,98 @@ __global__ void __launch_bounds__(128) k_density(
       }
     }
   }
+  return nc;
+}
+
+
+// Sort every bin's entries by atom index (one thread per bin, a handful of
+// entries each), so the candidate order below is fixed run to run.
+__global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  int cnt = bin_count[b];
+  cnt = cnt < bcap ? cnt : bcap;
+  BinEntry *e = bins + (size_t)b * bcap;
+  for (int k = 1; k < cnt; ++k) {
+    const BinEntry v = e[k];
+    const unsigned key = v.idx & IDX_MASK;
+    int p = k;
+    while (p > 0 && (e[p - 1].idx & IDX_MASK) > key) {
+      e[p] = e[p - 1];
+      --p;
+    }
+    e[p] = v;
+  }
+}
+
+// calculate_environment (fix_eph.cpp:431-466) plus everything per atom the
+// later sweeps need.  One thread per atom, warps kept converged: a warp FP64
+// instruction costs the same whether 1 or 32 lanes are active, so the FP64
+// work must run in lockstep.
+//   pass 1 (FP32/integer): candidates from the 27 bins around the atom with an
+//     FP32 distance test padded by 1e-4 of rc^2, kept in shared memory; EXACT
+//     mode keeps them in ascending neighbour index (the order of the
+//     reference's list, so sums round identically), FAST mode in the fixed
+//     bin-stencil order of index-sorted bins
+//   pass 2 (FP64): the exact test r^2 < rc^2 with e = (x_j + image) - x_i, the
+//     density sum, and the pair cache of the in-cutoff pairs
+// Pair cache row k of atom i sits at k*n + i (coalesced across the warp):
+//   pj: neighbour index | image code << 27
+//   pe: e_ij and (EXACT) r^2 or (FAST) rho_j(r^2)/r^2
+//   pg: (EXACT) rho_j(r^2), rho_i(r^2); (FAST, several elements) rho_i(r^2)/r^2
+// A[i] = {rho_i, alpha_i (EXACT) | alpha_i/rho_i (FAST), xi_x, xi_y}
+// Bw[i] = {xi_z, w_i} (w written by the friction sweep)
+// Candidates: the first CAND_SMEM rows of an atom live in shared memory
+// ([CAND_SMEM][blockDim]), further ones in the atom's own rows of pj (read
+// back before pass 2 overwrites them: pair slot <= candidate slot).
+// FUSE_W (FAST mode): the friction pre-vector of stage 1 in the same pass,
+// w_i = (alpha_i / rho_i) sum_j H_ij (e.(v_i - v_j)) e with H_ij = rho_j(r^2)/r^2 —
+// it needs only this atom's density, so the sum rides along with rho and the
+// separate sweep over the pair cache is saved.  FUSE_W also leaves M_i and
+// the records G_i for k_forces_m.
+template <bool FAST, bool MULTI, bool FUSE_W = false>
+__global__ void __launch_bounds__(128) k_density(
+    StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
+    const BinEntry *__restrict__ bins, const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
+    const D4 *__restrict__ xi_given, int xi_mode, const double *__restrict__ T_e, unsigned *__restrict__ pj,
+    D4 *__restrict__ pe, double2 *__restrict__ pg, int *__restrict__ nshort, D4 *__restrict__ A,
+    D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell,
+    double *__restrict__ Te_i, int *__restrict__ wrapflag, unsigned *__restrict__ err,
+    unsigned long long *__restrict__ counters, const D4 *__restrict__ v = nullptr, D4 *__restrict__ Mm = nullptr,
+    D4 *__restrict__ G = nullptr) {
+  __shared__ unsigned s_cand[CAND_SMEM * 128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
+  if (i == 0) *wrapflag = 0;  // the binning kernel has read it
+  const bool valid = i < P.n;
+  const bool active = valid && (mask[i] & P.groupbit) != 0;
+  auto cget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : pj[(size_t)k * P.n + i]; };
+  auto cset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM)
+      s_cand[k * nt + t] = u;
+    else
+      pj[(size_t)k * P.n + i] = u;
+  };
+  D4 xi = D4{0.0, 0.0, 0.0, 0.0};
+  if (valid) xi = x[i];
+  const int ei = (int)xi.w;
+  double rho = 0.0;
+  int ns = 0, nc = 0;
+  // pass 1: candidates, FP32/integer work only, warp-uniform loop bounds
+  {
+    int4 Bi = make_int4(0, 0, 0, 0);
+    float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) {
+      Bi = atom_bin[i];
+      oi = atom_off[i];
+    }
+    nc = collect_candidates<FAST>(P, i, active, Bi, oi, bin_count, bins, err, cget, cset);
+  }
   __syncwarp();
   // pass 2: exact FP64 test, density and pair cache, in lockstep
-  D4 vi{0.0, 0.0, 0.0, 0.0};
-  if (FUSE_W && active) vi = v[i];
+  // FUSE_W: M_i = sum_j H_ij e e^T over all pairs and S_i = sum_j H_ij (e.v_j) e
   double Sx = 0.0, Sy = 0.0, Sz = 0.0;
+  double mxx = 0.0, mxy = 0.0, mxz = 0.0, myy = 0.0, myz = 0.0, mzz = 0.0;
   const int nmax = __reduce_max_sync(0xffffffffu, nc);
   for (int k = 0; k < nmax; ++k) {
     if (k < nc) {
@@ -319,10 +337,17 @@ __global__ void __launch_bounds__(128) k_density(
           if (MULTI) pg[slot] = make_double2(rij * inv_r2, 0.0);
           if (FUSE_W) {
             const D4 vj = v[j];
-            const double s = H * dot3_fma(ex, ey, ez, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
-            Sx = fma(s, ex, Sx);
-            Sy = fma(s, ey, Sy);
-            Sz = fma(s, ez, Sz);
+            const double hx = H * ex, hy = H * ey, hz = H * ez;
+            mxx = fma(hx, ex, mxx);
+            mxy = fma(hx, ey, mxy);
+            mxz = fma(hx, ez, mxz);
+            myy = fma(hy, ey, myy);
+            myz = fma(hy, ez, myz);
+            mzz = fma(hz, ez, mzz);
+            const double d = dot3_fma(ex, ey, ez, vj.x, vj.y, vj.z);
+            Sx = fma(d, hx, Sx);
+            Sy = fma(d, hy, Sy);
+            Sz = fma(d, hz, Sz);
           }
         } else {
           pe[slot] = D4{ex, ey, ez, r2};
@@ -359,10 +384,25 @@ __global__ void __launch_bounds__(128) k_density(
     Te_i[i] = T_e[c];
   }
   A[i] = D4{rho, alpha, xi3[0], xi3[1]};
-  if (FUSE_W && active && pos_double(rho))  // k_friction_w's rule: w stays 0 unless rho_i > 0
-    Bw[i] = D4{xi3[2], alpha * Sx, alpha * Sy, alpha * Sz};
-  else
+  if (FUSE_W) {
+    // w_i = a_i (M_i v_i - S_i), a_i = alpha_i/rho_i; k_friction_w's rule: w
+    // stays 0 unless rho_i > 0.  For k_forces_m: M_i, and the records
+    // G_i = {a_i w_i, a_i xi_i, rho_i} that the neighbours gather.
+    double wx = 0.0, wy = 0.0, wz = 0.0;
+    if (active && pos_double(rho)) {
+      const D4 vi = v[i];
+      wx = alpha * (fma(mxx, vi.x, fma(mxy, vi.y, mxz * vi.z)) - Sx);
+      wy = alpha * (fma(mxy, vi.x, fma(myy, vi.y, myz * vi.z)) - Sy);
+      wz = alpha * (fma(mxz, vi.x, fma(myz, vi.y, mzz * vi.z)) - Sz);
+    }
+    Bw[i] = D4{xi3[2], wx, wy, wz};
+    Mm[i] = D4{mxx, mxy, mxz, myy};
+    Mm[(size_t)P.n + i] = D4{myz, mzz, 0.0, 0.0};
+    G[2 * (size_t)i] = D4{alpha * wx, alpha * wy, alpha * wz, alpha * xi3[0]};
+    G[2 * (size_t)i + 1] = D4{alpha * xi3[1], alpha * xi3[2], active ? rho : 0.0, 0.0};
+  } else {
     Bw[i] = D4{xi3[2], 0.0, 0.0, 0.0};
+  }
   rho_out[i] = rho;
   beta_out[i] = beta;
 }
@@ -412,6 +452,53 @@ __global__ void __launch_bounds__(128) k_friction_w(StepParams P, const int *__r
 }
 
 // ------------------------------------------------ friction + random sweep
+
+// The end of post_force for atom i: the coloured-noise memory of
+// eph/coloured/exp (fix_eph_coloured_exp.cpp:562-568, :619-625), f_EPH and
+// f_RNG, and their addition to the engine's force unless NOFRICTION /
+// NORANDOM keep them out (fix_eph.cpp:892-906).
+template <bool FRIC, bool RAND>
+__device__ __forceinline__ void store_forces(const StepParams &P, int i, bool live, double fex, double fey,
+                                             double fez, double frx, double fry, double frz, D4 *__restrict__ f,
+                                             D4 *__restrict__ f_eph, D4 *__restrict__ f_rng, D4 *__restrict__ f_dis,
+                                             D4 *__restrict__ f_sto) {
+  if (P.coloured && live) {
+    if (FRIC) {
+      D4 d = f_dis[i];
+      d.x = d.x * (1. - P.zeta) + P.zeta * fex;
+      d.y = d.y * (1. - P.zeta) + P.zeta * fey;
+      d.z = d.z * (1. - P.zeta) + P.zeta * fez;
+      f_dis[i] = d;
+      fex = d.x;
+      fey = d.y;
+      fez = d.z;
+    }
+    if (RAND) {
+      D4 d = f_sto[i];
+      d.x = d.x * (1. - P.zeta) + P.zeta * frx;
+      d.y = d.y * (1. - P.zeta) + P.zeta * fry;
+      d.z = d.z * (1. - P.zeta) + P.zeta * frz;
+      f_sto[i] = d;
+      frx = d.x;
+      fry = d.y;
+      frz = d.z;
+    }
+  }
+  f_eph[i] = D4{fex, fey, fez, 0.0};
+  f_rng[i] = D4{frx, fry, frz, 0.0};
+  D4 fi = f[i];
+  if (FRIC && !(P.flags & 0x10)) {
+    fi.x += fex;
+    fi.y += fey;
+    fi.z += fez;
+  }
+  if (RAND && !(P.flags & 0x20)) {
+    fi.x += frx;
+    fi.y += fry;
+    fi.z += frz;
+  }
+  f[i] = fi;
+}
 
 // force_prl stages 2 and 3 (fix_eph.cpp:748-836) in one pass over the pairs,
 // then the force update of post_force (fix_eph.cpp:892-906):
@@ -491,42 +578,85 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
       frz *= var;
     }
   }
-  if (P.coloured && live) {  // fix_eph_coloured_exp.cpp:562-568, :619-625
-    if (FRIC) {
-      D4 d = f_dis[i];
-      d.x = d.x * (1. - P.zeta) + P.zeta * fex;
-      d.y = d.y * (1. - P.zeta) + P.zeta * fey;
-      d.z = d.z * (1. - P.zeta) + P.zeta * fez;
-      f_dis[i] = d;
-      fex = d.x;
-      fey = d.y;
-      fez = d.z;
+  store_forces<FRIC, RAND>(P, i, live, fex, fey, fez, frx, fry, frz, f, f_eph, f_rng, f_dis, f_sto);
+}
+
+// Stages 2 and 3 in FAST mode with one lane per atom, after k_density<.., true>
+// (same sums as k_forces, split into the atom's own part and the
+// neighbours' part).  With W_i = a_i w_i, X_i = a_i xi_i (a_i = alpha_i/rho_i)
+// and M_i = sum_j H_ij e e^T over all of the atom's pairs:
+//   f_EPH_i = -M_i W_i + sum_{j live} H_ji (e.W_j) e + sum_{j not live} H_ij (e.W_i) e
+//   f_RNG_i = eta sqrt(T_e) [M_i X_i - sum_{j live} H_ji (e.X_j) e - sum_{j not live} H_ij (e.X_i) e]
+// ("live": rho_j > 0, the reference's test; the last sums take back the
+// pairs it skips).  Per pair 14 FP64 instructions instead of 24.
+template <bool MULTI, bool RAND>
+__global__ void __launch_bounds__(128) k_forces_m(StepParams P, const unsigned *__restrict__ pj,
+                                                  const D4 *__restrict__ pe, const double2 *__restrict__ pg,
+                                                  const int *__restrict__ nshort, const D4 *__restrict__ Mm,
+                                                  const D4 *__restrict__ G, const double *__restrict__ Te_i,
+                                                  D4 *__restrict__ f, D4 *__restrict__ f_eph, D4 *__restrict__ f_rng,
+                                                  D4 *__restrict__ f_dis, D4 *__restrict__ f_sto) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  double fex = 0.0, fey = 0.0, fez = 0.0, frx = 0.0, fry = 0.0, frz = 0.0;
+  const bool live = pos_double(G[2 * (size_t)i + 1].z);  // rho_i > 0 (0 outside the group)
+  if (live) {
+    double cex = 0.0, cey = 0.0, cez = 0.0, crx = 0.0, cry = 0.0, crz = 0.0;
+    const int ns = nshort[i];
+    bool skipped = false;
+    for (int k = 0; k < ns; ++k) {
+      const size_t slot = (size_t)k * P.n + i;
+      const unsigned j = pj[slot] & IDX_MASK;
+      const D4 e = pe[slot];
+      const D4 Gj1 = G[2 * (size_t)j], Gj2 = G[2 * (size_t)j + 1];
+      if (!pos_double(Gj2.z)) {  // a pair the reference skips (handled below)
+        skipped = true;
+        continue;
+      }
+      const double Hji = MULTI ? pg[slot].x : e.w;  // rho_i(r^2)/r^2
+      const double sw = Hji * dot3_fma(e.x, e.y, e.z, Gj1.x, Gj1.y, Gj1.z);
+      fex = fma(sw, e.x, fex);
+      fey = fma(sw, e.y, fey);
+      fez = fma(sw, e.z, fez);
+      if (RAND) {
+        const double sx = Hji * dot3_fma(e.x, e.y, e.z, Gj1.w, Gj2.x, Gj2.y);
+        frx = fma(sx, e.x, frx);
+        fry = fma(sx, e.y, fry);
+        frz = fma(sx, e.z, frz);
+      }
     }
+    const D4 Gi1 = G[2 * (size_t)i], Gi2 = G[2 * (size_t)i + 1];
+    if (skipped) {  // rare: the skipped pairs' shares of M_i come back out (a second
+                    // pass keeps this work out of the main loop's instruction stream)
+      for (int k = 0; k < ns; ++k) {
+        const size_t slot = (size_t)k * P.n + i;
+        const unsigned j = pj[slot] & IDX_MASK;
+        if (pos_double(G[2 * (size_t)j + 1].z)) continue;
+        const D4 e = pe[slot];
+        const double sw = e.w * dot3_fma(e.x, e.y, e.z, Gi1.x, Gi1.y, Gi1.z);
+        cex = fma(sw, e.x, cex);
+        cey = fma(sw, e.y, cey);
+        cez = fma(sw, e.z, cez);
+        if (RAND) {
+          const double sx = e.w * dot3_fma(e.x, e.y, e.z, Gi1.w, Gi2.x, Gi2.y);
+          crx = fma(sx, e.x, crx);
+          cry = fma(sx, e.y, cry);
+          crz = fma(sx, e.z, crz);
+        }
+      }
+    }
+    const D4 M1 = Mm[i], M2 = Mm[(size_t)P.n + i];  // {xx, xy, xz, yy}, {yz, zz}
+    fex += cex - fma(M1.x, Gi1.x, fma(M1.y, Gi1.y, M1.z * Gi1.z));
+    fey += cey - fma(M1.y, Gi1.x, fma(M1.w, Gi1.y, M2.x * Gi1.z));
+    fez += cez - fma(M1.z, Gi1.x, fma(M2.x, Gi1.y, M2.y * Gi1.z));
     if (RAND) {
-      D4 d = f_sto[i];
-      d.x = d.x * (1. - P.zeta) + P.zeta * frx;
-      d.y = d.y * (1. - P.zeta) + P.zeta * fry;
-      d.z = d.z * (1. - P.zeta) + P.zeta * frz;
-      f_sto[i] = d;
-      frx = d.x;
-      fry = d.y;
-      frz = d.z;
+      const double var = P.eta * sqrt(Te_i[i]);
+      frx = var * (fma(M1.x, Gi1.w, fma(M1.y, Gi2.x, M1.z * Gi2.y)) - crx - frx);
+      fry = var * (fma(M1.y, Gi1.w, fma(M1.w, Gi2.x, M2.x * Gi2.y)) - cry - fry);
+      frz = var * (fma(M1.z, Gi1.w, fma(M2.x, Gi2.x, M2.y * Gi2.y)) - crz - frz);
     }
   }
-  f_eph[i] = D4{fex, fey, fez, 0.0};
-  f_rng[i] = D4{frx, fry, frz, 0.0};
-  D4 fi = f[i];
-  if (FRIC && !(P.flags & 0x10)) {
-    fi.x += fex;
-    fi.y += fey;
-    fi.z += fez;
-  }
-  if (RAND && !(P.flags & 0x20)) {
-    fi.x += frx;
-    fi.y += fry;
-    fi.z += frz;
-  }
-  f[i] = fi;
+  store_forces<true, RAND>(P, i, live, fex, fey, fez, frx, fry, frz, f, f_eph, f_rng, f_dis, f_sto);
 }
 
 // ------------------------------------- pair sweeps, several lanes per atom
@@ -645,42 +775,7 @@ __global__ void __launch_bounds__(128) k_forces_tpa(StepParams P, const int *__r
     fry *= var;
     frz *= var;
   }
-  if (P.coloured && live) {  // fix_eph_coloured_exp.cpp:562-568, :619-625
-    if (FRIC) {
-      D4 d = f_dis[i];
-      d.x = d.x * (1. - P.zeta) + P.zeta * fex;
-      d.y = d.y * (1. - P.zeta) + P.zeta * fey;
-      d.z = d.z * (1. - P.zeta) + P.zeta * fez;
-      f_dis[i] = d;
-      fex = d.x;
-      fey = d.y;
-      fez = d.z;
-    }
-    if (RAND) {
-      D4 d = f_sto[i];
-      d.x = d.x * (1. - P.zeta) + P.zeta * frx;
-      d.y = d.y * (1. - P.zeta) + P.zeta * fry;
-      d.z = d.z * (1. - P.zeta) + P.zeta * frz;
-      f_sto[i] = d;
-      frx = d.x;
-      fry = d.y;
-      frz = d.z;
-    }
-  }
-  f_eph[i] = D4{fex, fey, fez, 0.0};
-  f_rng[i] = D4{frx, fry, frz, 0.0};
-  D4 fi = f[i];
-  if (FRIC && !(P.flags & 0x10)) {
-    fi.x += fex;
-    fi.y += fey;
-    fi.z += fez;
-  }
-  if (RAND && !(P.flags & 0x20)) {
-    fi.x += frx;
-    fi.y += fry;
-    fi.z += frz;
-  }
-  f[i] = fi;
+  store_forces<FRIC, RAND>(P, i, live, fex, fey, fez, frx, fry, frz, f, f_eph, f_rng, f_dis, f_sto);
 }
 
 // --------------------------------------------------------- model 1 (TTM)
