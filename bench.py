@@ -118,19 +118,36 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def density_bytes(n_atoms, n_pairs):
+    """Algorithmic HBM bytes of one launch of the density sweep (k_density,
+    FAST, one element, stage 1 folded in): per atom read x_i, v_i (64 B), mask
+    (4), bin and offset (32), T_e at the atom (8); written pair count (4), A_i,
+    Bw_i (64), M_i (64), G_i (64), rho, beta, T_e at the atom (24), cell (4);
+    per in-cutoff pair the cached index (4) and e_ij with rho_j(r^2)/r^2 (32)
+    written.  The neighbours' positions and velocities and the bins are L2
+    hits and not counted."""
+    return 332 * n_atoms + 36 * n_pairs
+
+
 def forces_bytes(n_atoms, n_pairs):
-    """Algorithmic HBM bytes of one launch of the force sweep (k_forces, FAST,
-    one element): per atom A_i, Bw_i (64 B), pair count (4), T_e at the atom
-    (8), f read and written (64), f_EPH and f_RNG written (64); per in-cutoff
-    pair the cached index (4) and e_ij with rho_j(r^2)/r^2 (32).  The
-    neighbours' records (A_j, Bw_j) are L2 hits and not counted."""
-    return 204 * n_atoms + 36 * n_pairs
+    """Algorithmic HBM bytes of one launch of the force sweep (k_forces_m,
+    FAST, one element): per atom G_i and M_i (128 B), pair count (4), T_e at
+    the atom (8), f read and written (64), f_EPH and f_RNG written (64); per
+    in-cutoff pair the cached index (4) and e_ij with rho_j(r^2)/r^2 (32).
+    The neighbours' records G_j are L2 hits and not counted."""
+    return 268 * n_atoms + 36 * n_pairs
 
 
-# DRAM bytes per atom of one k_forces launch measured by ncu on the 32^3-cell
-# case (profiles/sweeps_fcc_131k.md: 219.8 MB for 131,072 atoms); traffic of a
-# launch scales with the atom count at fixed pairs per atom.
-FORCES_DRAM_BYTES_PER_ATOM = 219.8e6 / 131072
+# DRAM bytes of one launch (dram__bytes_read.sum + dram__bytes_write.sum,
+# one-pass ncu capture of the bench workload itself, 2,048,000 atoms at 42.0
+# pairs per atom, profiles/launch_list_cascade_2048k.md) over the algorithmic
+# bytes of that launch; the bench's traffic figure is this ratio times the
+# algorithmic bytes at its own pair count.
+DENSITY_DRAM_OVER_ALGORITHMIC = (0.31433e9 + 3.50e9) / density_bytes(2048000, 86014654)
+FORCES_DRAM_OVER_ALGORITHMIC = (3.47e9 + 0.18816e9) / forces_bytes(2048000, 86014654)
+# FP64-pipe utilisation of the two sweeps (ncu, profiles/sweeps_fcc_131k.md)
+DENSITY_FP64_PIPE = 0.687
+FORCES_FP64_PIPE = 0.848
 
 
 def run_gpu(args, rank, world):
@@ -616,10 +633,17 @@ def main():
     res = run_gpu(args, rank, world)
     n = res["n"]
     value = world * n * args.steps / (res["ms"] / 1000.0)
-    ms_f, nl_f = res["phases"]["forces"]
     hbm, peak_src = peaks()
-    t_launch = ms_f / max(nl_f, 1) / 1000.0
-    achieved = forces_bytes(n, res["n_pairs"]) / t_launch / 1e9
+
+    def roofline(phase, kernel, nbytes, dram_ratio, fp64_pipe):
+        ms_p, nl_p = res["phases"][phase]
+        t_launch = ms_p / max(nl_p, 1) / 1000.0
+        achieved = nbytes / t_launch / 1e9
+        return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": peak_src, "traffic": dram_ratio * nbytes,
+                "algorithmic_bytes": nbytes, "launch_ms": t_launch * 1000.0, "fp64_pipe_frac_ncu": fp64_pipe,
+                "note": "bound by FP64 issue, not HBM: GB300 issues ~0.6e12 FP64 thread-instructions/s "
+                        "(2 per SM per clock); ncu puts this kernel's FP64 pipe at %.0f%%" % (100 * fp64_pipe)}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -629,13 +653,10 @@ def main():
                    "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 52 // 2 ** 20),
                    "mode": "fast", "xi": "device Philox4x32-10"},
         "gpu_launches": res["launches"],
-        "roofline": {"bound": "hbm", "kernel": "k_forces", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": peak_src,
-                     "traffic": FORCES_DRAM_BYTES_PER_ATOM * n,
-                     "algorithmic_bytes": forces_bytes(n, res["n_pairs"]),
-                     "fp64_pipe_frac_ncu": 0.874,
-                     "note": "bound by FP64 issue, not HBM: ncu puts k_forces at 87% of the FP64 pipe; "
-                             "GB300 issues ~0.5e12 FP64 instructions/s (measured)"},
+        "roofline": roofline("density", "k_density", density_bytes(n, res["n_pairs"]),
+                             DENSITY_DRAM_OVER_ALGORITHMIC, DENSITY_FP64_PIPE),
+        "roofline_forces": roofline("forces", "k_forces_m", forces_bytes(n, res["n_pairs"]),
+                                    FORCES_DRAM_OVER_ALGORITHMIC, FORCES_FP64_PIPE),
         "phases_ms": {k: round(v[0], 3) for k, v in res["phases"].items()},
         "clocks": res["clocks"],
         "pairs_per_atom": res["n_pairs"] / n,
