@@ -111,14 +111,23 @@ __device__ __forceinline__ double spline_eval(const D4 *__restrict__ tab, double
   return c.x + x * (c.y + x * (c.z + x * c.w));
 }
 
-// 1/x for FAST mode: the hardware estimate refined by two Newton-Raphson
-// steps r <- r + r (1 - x r) (quadratic convergence); x > 0 and normal.
+// 1/x for FAST mode, x > 0 inside the normal float range (x = r^2 here):
+// x truncated to float by its bits (exponent rebased, top 23 mantissa bits),
+// the FP32 hardware reciprocal estimate (rcp.approx.ftz.f32, ~2^-23), widened
+// back to double by its bits, then one Newton-Raphson step
+// r <- r + r (1 - x r), which squares the relative error: ~2^-44 against
+// the correctly rounded 1/x.  Two FP64 instructions; the rest runs on the
+// integer and FP32 pipes, which GB300 has ~60 times more of.
 __device__ __forceinline__ double recip_nr(double x) {
-  double r;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-  r = fma(r, fma(-x, r, 1.0), r);
-  r = fma(r, fma(-x, r, 1.0), r);
-  return r;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned fb = (hi & 0x80000000u) | ((((hi >> 20) & 0x7ffu) - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(fb)));
+  const unsigned rb = __float_as_uint(rf);
+  const unsigned rhi = (rb & 0x80000000u) | ((((rb >> 23) & 0xffu) + 896u) << 20) | ((rb & 0x7fffffu) >> 3);
+  const double r = __longlong_as_double((long long)(((unsigned long long)rhi << 32) | (unsigned long long)(rb << 29)));
+  return fma(r, fma(-x, r, 1.0), r);
 }
 
 __device__ __forceinline__ double dot3(double ax, double ay, double az, double bx, double by, double bz) {
