@@ -465,6 +465,8 @@ def run_adjoint_fit(args, dev):
         t0 = time.perf_counter()
         beta, hist = fit_beta_batch(batch, nsteps, target, beta0, iters=iters, lr=0.05)
         wall = time.perf_counter() - t0
+        import torch
+        free, total = torch.cuda.mem_get_info(dev)
         tb = batch.timing()
         # the same passes replica after replica (each its own graphs)
         for a in adjs:
@@ -493,7 +495,8 @@ def run_adjoint_fit(args, dev):
                 "batched_backward_ms": tb["backward_ms"],
                 "sequential_forward_plus_backward_s": seq,
                 "batched_speedup_vs_sequential": seq / ((tb["forward_ms"] + tb["backward_ms"]) / 1000.0),
-                "atom_steps_per_s_forward": atoms_total * nsteps / (tb["forward_ms"] / 1000.0)}
+                "atom_steps_per_s_forward": atoms_total * nsteps / (tb["forward_ms"] / 1000.0),
+                "device_memory_in_use_gb": (total - free) / 1e9}
 
 
 def run_md_eam(args, dev):
