@@ -34,7 +34,7 @@ def scenario(name, beta_file, beta_file_2el=None):
     if name == "c1_small":  # the C1 setting on 5^3 cells
         at = W.fcc_lattice(5, seed=11)
         return W.fix_args(beta_file, grid=(5, 5, 5)), at, 0.001
-    if name == "c1":  # BASELINE config 0: 10^3 cells, 4000 atoms, 10^3 grid
+    if name == "c1":  # the CPU-runnable case: 10^3 cells, 4000 atoms, 10^3 grid
         at = W.fcc_lattice(10, seed=12)
         return W.fix_args(beta_file, grid=(10, 10, 10)), at, 0.001
     if name == "friction_only":

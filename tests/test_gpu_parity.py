@@ -6,7 +6,7 @@ step every per-atom array is bit-identical to the oracle; the grid sums its
 deposits exactly (fixed point) instead of in atom order, so T_e (and from the
 second step on everything that depends on T_e) agrees to rounding.  FAST mode
 factors alpha/rho and rho(r^2)/r^2 and uses FMA.  Tolerance for both: the
-spec bar, 1e-12 relative, norm-wise (max |a - b| / max |b|) per array."""
+parity bar, 1e-12 relative, norm-wise (max |a - b| / max |b|) per array."""
 import numpy as np
 import pytest
 
@@ -76,7 +76,7 @@ def test_fast_mode_within_tolerance(built, beta_file, beta_file_2el, name, tpa):
 
 
 def test_c1_config_fast_and_exact(built, beta_file):
-    """BASELINE configs[0] (4,000 atoms, 10^3 grid) for 20 steps."""
+    """The 4,000-atom CPU-runnable case (10^3 grid) for 20 steps."""
     words, at, dt = scenario("c1", beta_file)
     for mode in (ephgb.MODE_EXACT, ephgb.MODE_FAST):
         def check(s, gpu, ref):
