@@ -62,8 +62,9 @@ struct GridArgs {
   long n[3];
   long nc;
   double h[3];
+  double ih2[3];  // 1/h^2 per axis
   double inner_dt;
-  const double *kappa, *rhoC, *rho_e, *S;
+  const double *kappa, *rhoC, *irhoC, *rho_e, *S;  // irhoC = 1/(rho_e C_e)
   const signed char *flag;
 };
 
@@ -153,7 +154,7 @@ __device__ __forceinline__ void cell_ddT(const GridArgs &G, const double *__rest
   for (int a = 0; a < 3; ++a) {
     long p, q;
     axis_pq(G, r, a, p, q);
-    const double ih2 = 1.0 / (G.h[a] * G.h[a]);
+    const double ih2 = G.ih2[a];
     const double l = (T[q] + T[p] - 2.0 * T[r]) * ih2;
     ddT += (G.kappa[q] - G.kappa[p]) * (T[q] - T[p]) * 0.25 * ih2 + G.kappa[r] * l;
     lap += l;
@@ -171,12 +172,12 @@ __device__ __forceinline__ double substep_reverse(const GridArgs &G, const doubl
   cell_ddT(G, Tk, r, ddT, lap);
   const bool dyn = G.flag[r] == 1;
   const double rate = ddT + src[r] + G.S[r];
-  const double pre = dyn ? Tk[r] + rate / G.rhoC[r] * G.inner_dt : Tk[r];
+  const double pre = dyn ? Tk[r] + rate * G.irhoC[r] * G.inner_dt : Tk[r];
   const double u = pre >= 0.0 ? lam : 0.0;
   double w = 0.0;
   if (dyn) {
-    w = u * G.inner_dt / G.rhoC[r];
-    gC[r] -= w * rate * G.rho_e[r] / G.rhoC[r];
+    w = u * G.inner_dt * G.irhoC[r];
+    gC[r] -= w * rate * G.rho_e[r] * G.irhoC[r];
     gK[r] += w * lap;
   }
   srcbar[r] = first ? w : srcbar[r] + w;
@@ -219,7 +220,7 @@ __global__ void k_adj_fdm_weights(GridArgs G, double *__restrict__ W) {
       cand[ncand] = c < na - 1 ? r + st : r - (na - 1) * st;
       slot[ncand++] = 2 + 2 * a;
     }
-    const double ih2 = 1.0 / (G.h[a] * G.h[a]);
+    const double ih2 = G.ih2[a];
     for (int m = 0; m < ncand; ++m) {
       const long s = cand[m];
       if (G.flag[s] != 1) continue;  // only DYNAMIC cells move (eph_fdm.h:375-387)
@@ -230,7 +231,7 @@ __global__ void k_adj_fdm_weights(GridArgs G, double *__restrict__ W) {
       if (q == r) coef += 0.25 * ih2 * dk + G.kappa[s] * ih2;
       if (p == r) coef += -0.25 * ih2 * dk + G.kappa[s] * ih2;
       if (s == r) coef -= 2.0 * G.kappa[s] * ih2;
-      w[slot[m]] += coef * G.inner_dt / G.rhoC[s];
+      w[slot[m]] += coef * G.inner_dt * G.irhoC[s];
     }
   }
   for (int m = 0; m < 7; ++m) W[(size_t)m * G.nc + r] = w[m];
@@ -803,9 +804,11 @@ GridArgs grid_args(eph_adjoint *a) {
   G.h[0] = g.dx;
   G.h[1] = g.dy;
   G.h[2] = g.dz;
+  for (int k = 0; k < 3; ++k) G.ih2[k] = 1.0 / (G.h[k] * G.h[k]);
   G.inner_dt = c->inner_dt;
   G.kappa = c->kappa.p;
   G.rhoC = c->rhoC.p;
+  G.irhoC = c->irhoC.p;
   G.rho_e = a->rho_e.p;
   G.S = c->S.p;
   G.flag = c->gflag.p;

@@ -51,6 +51,13 @@ int upload_tables(eph_ctx *c) {
   return EPH_OK;
 }
 
+// 1/(rho_e C_e) per cell for the FAST substeps (IEEE quotients, as on the device)
+cudaError_t upload_inverse(eph_ctx *c, const std::vector<double> &rc) {
+  std::vector<double> inv(rc.size());
+  for (size_t i = 0; i < rc.size(); ++i) inv[i] = 1.0 / rc[i];
+  return cudaMemcpy(c->irhoC.p, inv.data(), inv.size() * 8, cudaMemcpyHostToDevice);
+}
+
 int upload_grid(eph_ctx *c) {
   Grid &g = c->grid;
   const size_t nc = (size_t)g.ntotal;
@@ -58,6 +65,7 @@ int upload_grid(eph_ctx *c) {
   CUDA_TRY(c, c->T1.alloc(nc));
   CUDA_TRY(c, c->kappa.alloc(nc));
   CUDA_TRY(c, c->rhoC.alloc(nc));
+  CUDA_TRY(c, c->irhoC.alloc(nc));
   CUDA_TRY(c, c->S.alloc(nc));
   CUDA_TRY(c, c->dT.alloc(nc));
   CUDA_TRY(c, c->gflag.alloc(nc));
@@ -71,6 +79,7 @@ int upload_grid(eph_ctx *c) {
   CUDA_TRY(c, cudaMemcpy(c->T0.p, g.T.data(), nc * 8, cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->kappa.p, g.kappa.data(), nc * 8, cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->rhoC.p, rc.data(), nc * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, upload_inverse(c, rc));
   CUDA_TRY(c, cudaMemcpy(c->S.p, g.S.data(), nc * 8, cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->gflag.p, fl.data(), nc, cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemset(c->dT.p, 0, nc * 8));
@@ -378,17 +387,18 @@ int launch_end_of_step(eph_ctx *c) {
       ps.launched(2);
     }
     ps.launched((int)c->nsub);
+    const double3 ih2 = make_double3(1.0 / (g.dx * g.dx), 1.0 / (g.dy * g.dy), 1.0 / (g.dz * g.dz));
     double *src = c->T0.p, *dst = c->T1.p;
     for (unsigned s = 0; s < c->nsub; ++s) {
       if (c->fdm_rec) dst = c->fdm_rec + (size_t)s * (size_t)g.ntotal;
       if (c->mode == EPH_MODE_FAST)
         k_fdm_substep<true><<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(
             g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt, src, dst, c->kappa.p, c->rhoC.p, c->S.p, c->gflag.p,
-            c->dT.p, c->acc.p, s == 0, c->counters.p, c->td);
+            c->dT.p, c->acc.p, s == 0, c->counters.p, c->td, ih2, c->irhoC.p);
       else
         k_fdm_substep<false><<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(
             g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt, src, dst, c->kappa.p, c->rhoC.p, c->S.p, c->gflag.p,
-            c->dT.p, c->acc.p, s == 0, c->counters.p, c->td);
+            c->dT.p, c->acc.p, s == 0, c->counters.p, c->td, ih2, c->irhoC.p);
       if (c->fdm_rec) src = dst;
       else std::swap(src, dst);
     }
@@ -1332,6 +1342,7 @@ int eph_set_grid_constants(eph_ctx *c, double C_e, double kappa_e) {
   CUDA_TRY(c, cudaSetDevice(c->device));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   CUDA_TRY(c, cudaMemcpy(c->rhoC.p, rc.data(), nc * 8, cudaMemcpyHostToDevice));
+  CUDA_TRY(c, upload_inverse(c, rc));
   CUDA_TRY(c, cudaMemcpy(c->kappa.p, g.kappa.data(), nc * 8, cudaMemcpyHostToDevice));
   drop_graph(c);  // the substep count may change
   set_time_params(c);

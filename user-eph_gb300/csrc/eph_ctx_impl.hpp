@@ -88,7 +88,7 @@ struct eph_ctx {
 
   DevBuf<D4> tab_rho_r_sq, tab_beta, tab_alpha;
 
-  DevBuf<double> T0, T1, kappa, rhoC, S, dT;
+  DevBuf<double> T0, T1, kappa, rhoC, irhoC, S, dT;
   // temperature-dependent cells: per-cell C_e and rho_e, the parameter tables
   DevBuf<double> gC, grho, E_y, E_dy, bounds;
   DevBuf<D4> C_T, K_T;

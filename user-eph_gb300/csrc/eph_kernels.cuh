@@ -951,7 +951,10 @@ __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, d
                               const double *__restrict__ kappa, const double *__restrict__ rhoC,
                               const double *__restrict__ S, const signed char *__restrict__ flag,
                               double *__restrict__ dT, U128 *__restrict__ acc, int first,
-                              unsigned long long *__restrict__ counters, TdynTables td) {
+                              unsigned long long *__restrict__ counters, TdynTables td, double3 ih2,
+                              const double *__restrict__ irhoC) {
+  // FAST: ih2 = 1/h^2 per axis and irhoC = 1/(rho_e C_e) per cell come
+  // precomputed (the same correctly rounded quotients as 1.0 / x here)
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long ntotal = nx * ny * nz;
   if (r >= ntotal) return;
@@ -973,6 +976,7 @@ __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, d
     const long qr[3] = {(i < nx - 1) ? r + 1 : r - (nx - 1), (j < ny - 1) ? r + nx : r - (ny - 1) * nx,
                         (k < nz - 1) ? r + nx * ny : r - (nz - 1) * nx * ny};
     const double h[3] = {dx, dy, dz};
+    const double ih2s[3] = {ih2.x, ih2.y, ih2.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       p = pr[a];
@@ -980,7 +984,7 @@ __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, d
       if (flag[q] == 2) q = r;
       else if (flag[p] == 2) p = r;
       if (FAST) {  // reciprocals instead of the reference's divisions (within 1e-15 of them)
-        const double ih2 = 1.0 / (h[a] * h[a]);
+        const double ih2 = ih2s[a];
         ddT = fma((kappa[q] - kappa[p]) * (T[q] - T[p]), 0.25 * ih2, ddT);
         ddT = fma(kappa[r] * ih2, T[q] + T[p] - 2.0 * T[r], ddT);
       } else {
@@ -991,7 +995,7 @@ __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, d
   }
   double t = T[r];
   if (FAST && flag[r] == 1 && !(td.tdyn && td.tdyn[r] == 1)) {
-    t = fma((ddT + dTr + S[r]) * inner_dt, 1.0 / rhoC[r], t);
+    t = fma((ddT + dTr + S[r]) * inner_dt, irhoC[r], t);
   } else if (flag[r] == 1) {
     if (td.tdyn && td.tdyn[r] == 1) {  // eph_fdm.h:378-382: through E_e(T)
       double E = linear_eval(td, t);
