@@ -253,15 +253,16 @@ __global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_coun
 //   pe: e_ij and (EXACT) r^2 or (FAST) rho_j(r^2)/r^2
 //   pg: (EXACT) rho_j(r^2), rho_i(r^2); (FAST, several elements) rho_i(r^2)/r^2
 // A[i] = {rho_i, alpha_i (EXACT) | alpha_i/rho_i (FAST), xi_x, xi_y}
-// Bw[i] = {xi_z, w_i} (w written by the friction sweep)
+// Bw[i] = {xi_z, w_i} (w written by the friction sweep, or here with FUSE_W)
 // Candidates: the first CAND_SMEM rows of an atom live in shared memory
 // ([CAND_SMEM][blockDim]), further ones in the atom's own rows of pj (read
 // back before pass 2 overwrites them: pair slot <= candidate slot).
-// FUSE_W (FAST mode): the friction pre-vector of stage 1 in the same pass,
-// w_i = (alpha_i / rho_i) sum_j H_ij (e.(v_i - v_j)) e with H_ij = rho_j(r^2)/r^2 —
-// it needs only this atom's density, so the sum rides along with rho and the
-// separate sweep over the pair cache is saved.  FUSE_W also leaves M_i and
-// the records G_i for k_forces_m.
+// FUSE_W (FAST mode, one lane per atom): the friction pre-vector of stage 1
+// in the same pass — it needs only this atom's density, so its sums ride
+// along with rho and the separate sweep over the pair cache is saved:
+// M_i = sum_j H_ij e e^T and S_i = sum_j H_ij (e.v_j) e (H_ij = rho_j(r^2)/r^2),
+// then w_i = (alpha_i / rho_i) (M_i v_i - S_i).  It also leaves M_i and the
+// records G_i = {a_i w_i, a_i xi_i, rho_i} for k_forces_m.
 template <bool FAST, bool MULTI, bool FUSE_W = false>
 __global__ void __launch_bounds__(128) k_density(
     StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
