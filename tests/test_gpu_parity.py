@@ -158,6 +158,24 @@ def test_threads_per_atom_variants(built, beta_file):
     np.testing.assert_array_equal(gpu.get("f"), f_before)
 
 
+@pytest.mark.parametrize("tpa", [2, 4, 8])
+def test_folded_sweeps_with_lanes(built, beta_file, tpa):
+    """From 16,384 atoms on, FAST mode folds stage 1 and M_i into the density
+    sweep at any number of lanes per atom (k_forces_m with TPA lanes): 16^3
+    fcc cells against the oracle for 3 steps."""
+    at = W.fcc_lattice(16, seed=21)
+    assert at.n == 16384
+    words = W.fix_args(beta_file, grid=(8, 8, 8))
+
+    def check(s, gpu, ref):
+        for k in ATOM_KEYS:
+            assert rel_err(gpu.get(k), ref.get(k)) <= TOL, (s, k, rel_err(gpu.get(k), ref.get(k)))
+        assert rel_err(gpu.get("T"), ref.get("T")) <= TOL
+
+    gpu, _ = run_pair(words, at, 0.001, ephgb.MODE_FAST, 3, check, tpa=tpa)
+    assert gpu.threads_per_atom() == tpa
+
+
 def test_async_host_copies(built, beta_file):
     """Hooks driven with queued host copies (EPH_HOST_ASYNC, one
     synchronisation per step) give what the synchronous copies give."""

@@ -185,11 +185,16 @@ int launch_final(eph_ctx *c) {
   return EPH_OK;
 }
 
-// FAST mode with one lane per atom folds stage 1 (the friction pre-vector)
-// into the density sweep
+// FAST mode folds stage 1 (the friction pre-vector) and M_i into the density
+// sweep, and stages 2 and 3 run as k_forces_m (any number of lanes per atom).
+// Below 16,384 atoms with several lanes per atom the separate stage-1 sweep
+// stays: there the one-lane density sweep is the latency bottleneck and
+// stage 1 is better split over the lanes (measured on GB300: 4,000 atoms
+// 0.290 ms per step separate, 0.304 ms folded; 32,000 atoms and up faster
+// folded).
 bool fused_friction(const eph_ctx *c) {
-  return c->mode == EPH_MODE_FAST && c->tpa == 1 && c->args.model == 4 && (c->P.flags & FLAG_FRICTION) &&
-         c->fuse_w;
+  return c->mode == EPH_MODE_FAST && c->args.model == 4 && (c->P.flags & FLAG_FRICTION) && c->fuse_w &&
+         (c->tpa == 1 || c->n >= 16384);
 }
 
 template <bool FAST, bool MULTI, bool FUSE>
@@ -210,9 +215,15 @@ template <bool FAST, bool MULTI, bool FRIC, bool RAND>
 void launch_forces_t(eph_ctx *c) {
   const int tpa = FAST ? c->tpa : 1;
   if (FAST && FRIC && fused_friction(c)) {
-    k_forces_m<MULTI, RAND><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
-        c->P, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->Mm.p, c->G.p, c->Te_i.p, c->f.p, c->f_eph.p, c->f_rng.p,
-        c->f_dis.p, c->f_sto.p);
+#define EPH_FORCES_M(T)                                                                                      \
+  k_forces_m<MULTI, RAND, T><<<nblocks((long)c->n * T), BLOCK, 0, c->stream>>>(                               \
+      c->P, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->Mm.p, c->G.p, c->Te_i.p, c->f.p, c->f_eph.p, c->f_rng.p, \
+      c->f_dis.p, c->f_sto.p)
+    if (tpa == 1) EPH_FORCES_M(1);
+    else if (tpa == 2) EPH_FORCES_M(2);
+    else if (tpa == 4) EPH_FORCES_M(4);
+    else EPH_FORCES_M(8);
+#undef EPH_FORCES_M
     return;
   }
   if (tpa == 1) {
@@ -722,7 +733,8 @@ int eph_autotune(eph_ctx *c, int *chosen) {
     for (int rep = 0; rep < 7; ++rep) {
       CUDA_TRY(c, cudaMemcpyAsync(c->f.p, save[0].p, sizeof(D4) * N, cudaMemcpyDeviceToDevice, c->stream));
       CUDA_TRY(c, cudaEventRecord(e0, c->stream));
-      if (c->P.flags & FLAG_FRICTION) launch_friction_w(c);
+      // with stage 1 folded into the density sweep only the force sweep has lanes
+      if ((c->P.flags & FLAG_FRICTION) && !fused_friction(c)) launch_friction_w(c);
       if (c->multi) launch_forces_m<true, true>(c);
       else launch_forces_m<true, false>(c);
       CUDA_TRY(c, cudaEventRecord(e1, c->stream));

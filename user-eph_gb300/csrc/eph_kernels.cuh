@@ -582,50 +582,70 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
   store_forces<FRIC, RAND>(P, i, live, fex, fey, fez, frx, fry, frz, f, f_eph, f_rng, f_dis, f_sto);
 }
 
-// Stages 2 and 3 in FAST mode with one lane per atom, after k_density<.., true>
-// (same sums as k_forces, split into the atom's own part and the
-// neighbours' part).  With W_i = a_i w_i, X_i = a_i xi_i (a_i = alpha_i/rho_i)
+// Stages 2 and 3 in FAST mode after k_density<.., true> (same sums as
+// k_forces, split into the atom's own part and the neighbours' part); TPA
+// lanes per atom take rows g, g + TPA, ... of the neighbours' part and
+// combine by a butterfly, as k_forces_tpa does.  With W_i = a_i w_i, X_i = a_i xi_i (a_i = alpha_i/rho_i)
 // and M_i = sum_j H_ij e e^T over all of the atom's pairs:
 //   f_EPH_i = -M_i W_i + sum_{j live} H_ji (e.W_j) e + sum_{j not live} H_ij (e.W_i) e
 //   f_RNG_i = eta sqrt(T_e) [M_i X_i - sum_{j live} H_ji (e.X_j) e - sum_{j not live} H_ij (e.X_i) e]
 // ("live": rho_j > 0, the reference's test; the last sums take back the
 // pairs it skips).  Per pair 14 FP64 instructions instead of 24.
-template <bool MULTI, bool RAND>
+template <bool MULTI, bool RAND, int TPA = 1>
 __global__ void __launch_bounds__(128) k_forces_m(StepParams P, const unsigned *__restrict__ pj,
                                                   const D4 *__restrict__ pe, const double2 *__restrict__ pg,
                                                   const int *__restrict__ nshort, const D4 *__restrict__ Mm,
                                                   const D4 *__restrict__ G, const double *__restrict__ Te_i,
                                                   D4 *__restrict__ f, D4 *__restrict__ f_eph, D4 *__restrict__ f_rng,
                                                   D4 *__restrict__ f_dis, D4 *__restrict__ f_sto) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
+  const long gt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(gt / TPA), g = (int)(gt % TPA);
+  if (TPA == 1 && i >= P.n) return;  // with TPA > 1 every lane joins the butterfly
   double fex = 0.0, fey = 0.0, fez = 0.0, frx = 0.0, fry = 0.0, frz = 0.0;
-  const bool live = pos_double(G[2 * (size_t)i + 1].z);  // rho_i > 0 (0 outside the group)
+  bool live = false;
+  int ns = 0, skipped = 0;
+  if (i < P.n) {
+    live = pos_double(G[2 * (size_t)i + 1].z);  // rho_i > 0 (0 outside the group)
+    if (live) ns = nshort[i];
+  }
+  for (int k = g; k < ns; k += TPA) {
+    const size_t slot = (size_t)k * P.n + i;
+    const unsigned j = pj[slot] & IDX_MASK;
+    const D4 e = pe[slot];
+    const D4 Gj1 = G[2 * (size_t)j], Gj2 = G[2 * (size_t)j + 1];
+    if (!pos_double(Gj2.z)) {  // a pair the reference skips (handled below)
+      skipped = 1;
+      continue;
+    }
+    const double Hji = MULTI ? pg[slot].x : e.w;  // rho_i(r^2)/r^2
+    const double sw = Hji * dot3_fma(e.x, e.y, e.z, Gj1.x, Gj1.y, Gj1.z);
+    fex = fma(sw, e.x, fex);
+    fey = fma(sw, e.y, fey);
+    fez = fma(sw, e.z, fez);
+    if (RAND) {
+      const double sx = Hji * dot3_fma(e.x, e.y, e.z, Gj1.w, Gj2.x, Gj2.y);
+      frx = fma(sx, e.x, frx);
+      fry = fma(sx, e.y, fry);
+      frz = fma(sx, e.z, frz);
+    }
+  }
+  if (TPA > 1) {
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) {
+      fex += __shfl_xor_sync(0xffffffffu, fex, o);
+      fey += __shfl_xor_sync(0xffffffffu, fey, o);
+      fez += __shfl_xor_sync(0xffffffffu, fez, o);
+      if (RAND) {
+        frx += __shfl_xor_sync(0xffffffffu, frx, o);
+        fry += __shfl_xor_sync(0xffffffffu, fry, o);
+        frz += __shfl_xor_sync(0xffffffffu, frz, o);
+      }
+      skipped |= __shfl_xor_sync(0xffffffffu, skipped, o);
+    }
+    if (i >= P.n || g != 0) return;
+  }
   if (live) {
     double cex = 0.0, cey = 0.0, cez = 0.0, crx = 0.0, cry = 0.0, crz = 0.0;
-    const int ns = nshort[i];
-    bool skipped = false;
-    for (int k = 0; k < ns; ++k) {
-      const size_t slot = (size_t)k * P.n + i;
-      const unsigned j = pj[slot] & IDX_MASK;
-      const D4 e = pe[slot];
-      const D4 Gj1 = G[2 * (size_t)j], Gj2 = G[2 * (size_t)j + 1];
-      if (!pos_double(Gj2.z)) {  // a pair the reference skips (handled below)
-        skipped = true;
-        continue;
-      }
-      const double Hji = MULTI ? pg[slot].x : e.w;  // rho_i(r^2)/r^2
-      const double sw = Hji * dot3_fma(e.x, e.y, e.z, Gj1.x, Gj1.y, Gj1.z);
-      fex = fma(sw, e.x, fex);
-      fey = fma(sw, e.y, fey);
-      fez = fma(sw, e.z, fez);
-      if (RAND) {
-        const double sx = Hji * dot3_fma(e.x, e.y, e.z, Gj1.w, Gj2.x, Gj2.y);
-        frx = fma(sx, e.x, frx);
-        fry = fma(sx, e.y, fry);
-        frz = fma(sx, e.z, frz);
-      }
-    }
     const D4 Gi1 = G[2 * (size_t)i], Gi2 = G[2 * (size_t)i + 1];
     if (skipped) {  // rare: the skipped pairs' shares of M_i come back out (a second
                     // pass keeps this work out of the main loop's instruction stream)
