@@ -150,6 +150,28 @@ DENSITY_FP64_PIPE = 0.687
 FORCES_FP64_PIPE = 0.848
 
 
+def ranks_reduce(x, op, device):
+    """x combined over the ranks of the process group ("max" for times, "sum"
+    for throughputs of independent replicas); x itself without a group or
+    with one rank."""
+    import torch
+
+    if not torch.distributed.is_available() or not torch.distributed.is_initialized():
+        return x
+    if torch.distributed.get_world_size() == 1:
+        return x
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    rop = {"max": torch.distributed.ReduceOp.MAX, "sum": torch.distributed.ReduceOp.SUM}[op]
+    torch.distributed.all_reduce(t, op=rop)
+    return float(t.item())
+
+
+def job_value(world, atoms_per_rank, steps, max_ms):
+    """Whole-job atom-steps/s: every rank steps its own replica of the
+    workload (weak scaling), timed by the slowest rank."""
+    return world * atoms_per_rank * steps / (max_ms / 1000.0)
+
+
 def run_gpu(args, rank, world):
     import torch
 
@@ -181,11 +203,7 @@ def run_gpu(args, rank, world):
         fix.step(args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = ranks_reduce(e0.elapsed_time(e1), "max", "cuda")
         clock = clocks.stop()
         fix.synchronize()
         phases = fix.phase_times()
@@ -232,11 +250,7 @@ def run_gpu(args, rank, world):
         for _ in range(e2e_steps):
             host_step()
         torch.cuda.synchronize()
-        t_e2e = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([t_e2e], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            t_e2e = float(t.item())
+        t_e2e = ranks_reduce(time.perf_counter() - t0, "max", "cuda")
         out.update(t_e2e=t_e2e, e2e_steps=e2e_steps, h2d=4 * 3 * 8 * n, d2h=3 * 3 * 8 * n + 8)
     return out
 
@@ -668,7 +682,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     res = run_gpu(args, rank, world)
     n = res["n"]
-    value = world * n * args.steps / (res["ms"] / 1000.0)
+    value = job_value(world, n, args.steps, res["ms"])
     hbm, peak_src = peaks()
 
     def roofline(phase, kernel, nbytes, dram_ratio, fp64_pipe):
@@ -703,10 +717,7 @@ def main():
                        "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"]}
     if not args.no_batched:
         line["batched"] = run_batched(args, int(os.environ.get("LOCAL_RANK", rank)))
-        if world > 1:
-            t = torch.tensor([line["batched"]["value"]], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-            line["batched"]["value"] = float(t.item())
+        line["batched"]["value"] = ranks_reduce(line["batched"]["value"], "sum", "cuda")
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = run_adjoint(args, int(os.environ.get("LOCAL_RANK", rank)), fd=not args.no_adjoint_fd)
     if rank == 0 and not args.no_c1:
