@@ -146,8 +146,8 @@ def forces_bytes(n_atoms, n_pairs):
 DENSITY_DRAM_OVER_ALGORITHMIC = (0.31433e9 + 3.50e9) / density_bytes(2048000, 86014654)
 FORCES_DRAM_OVER_ALGORITHMIC = (3.47e9 + 0.18816e9) / forces_bytes(2048000, 86014654)
 # FP64-pipe utilisation of the two sweeps (ncu, profiles/sweeps_fcc_131k.md)
-DENSITY_FP64_PIPE = 0.687
-FORCES_FP64_PIPE = 0.848
+DENSITY_FP64_PIPE = 0.676
+FORCES_FP64_PIPE = 0.874
 
 
 def ranks_reduce(x, op, device):
