@@ -61,7 +61,7 @@ def test_single_process_reduction_is_identity():
     assert bench.job_value(1, 4000, 10, 2.0) == pytest.approx(4000 * 10 / 0.002)
 
 
-def test_reference_arm_under_torchrun():
+def test_reference_arm_under_torchrun(built):
     """Two ranks: rank 0 times the reference algorithm on the host and prints
     one line; rank 1 exits 0 without work (a small lattice keeps it quick)."""
     port = _free_port()
