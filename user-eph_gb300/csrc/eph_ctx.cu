@@ -199,6 +199,25 @@ bool fused_friction(const eph_ctx *c) {
 
 template <bool FAST, bool MULTI, bool FUSE>
 void launch_density_f(eph_ctx *c, int xi_mode) {
+  // several lanes per atom in the density sweep too below 16,384 atoms, where
+  // one lane per atom leaves it latency bound (measured on GB300: 4,000 atoms
+  // 0.289 -> 0.210 ms per step; from 16,384 atoms on the extra exact-test pass
+  // and lane sums cost more than they hide: 32,000 atoms 71 -> 81 ms per 200
+  // steps, so the one-lane sweep stays there)
+  if constexpr (FAST && !FUSE) {
+    if (c->tpa > 1 && c->n < 16384) {
+#define EPH_DENSITY_TPA(T)                                                                                         \
+  k_density_tpa<MULTI, FUSE, T><<<nblocks((long)c->n * T), BLOCK, 0, c->stream>>>(                                  \
+      c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p, \
+      c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,        \
+      c->wrapflag.p, c->d_err.p, c->counters.p, c->v.p, c->Mm.p, c->G.p)
+      if (c->tpa == 2) EPH_DENSITY_TPA(2);
+      else if (c->tpa == 4) EPH_DENSITY_TPA(4);
+      else EPH_DENSITY_TPA(8);
+#undef EPH_DENSITY_TPA
+      return;
+    }
+  }
   k_density<FAST, MULTI, FUSE><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
       c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p,
       c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,

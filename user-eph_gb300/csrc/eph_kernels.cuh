@@ -150,72 +150,80 @@ __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, 
 
 // -------------------------------------------------------- density sweep
 
-// Pass 1 of the density sweep for atom i: the candidates j of the 27 bins
-// around its own whose FP32 distance passes the widened cut-off, appended
-// through cset (FAST: in the fixed bin-stencil order; EXACT: kept in
-// ascending neighbour index by insertion).  Returns their number.
+// Candidates of atom i in the bin at stencil offset (dx, dy, dz) from its
+// own: the entries whose FP32 distance passes the widened cut-off, appended
+// through cset (FAST: in bin order; EXACT: kept in ascending neighbour index
+// by insertion) while nc < cap.  Contains a warp-wide max: every lane of the
+// warp calls it the same number of times (look = false for a lane with
+// nothing to search).
+template <bool FAST, class Get, class Set>
+__device__ __forceinline__ void bin_candidates(const StepParams &P, int i, bool look, int4 Bi, float4 oi, int dx,
+                                               int dy, int dz, const int *__restrict__ bin_count,
+                                               const BinEntry *__restrict__ bins, unsigned *__restrict__ err,
+                                               int &nc, int cap, Get cget, Set cset) {
+  const int Tz = Bi.z + dz, tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
+  const int kz = Tz < 0 ? -1 : (Tz >= P.nb[2] ? 1 : 0);
+  const float bz = (float)dz * P.wf[2] - oi.z;
+  const int Ty = Bi.y + dy, ty = Ty < 0 ? Ty + P.nb[1] : (Ty >= P.nb[1] ? Ty - P.nb[1] : Ty);
+  const int ky = Ty < 0 ? -1 : (Ty >= P.nb[1] ? 1 : 0);
+  const float by = (float)dy * P.wf[1] - oi.y;
+  const int Tx = Bi.x + dx, tx = Tx < 0 ? Tx + P.nb[0] : (Tx >= P.nb[0] ? Tx - P.nb[0] : Tx);
+  const int kx = Tx < 0 ? -1 : (Tx >= P.nb[0] ? 1 : 0);
+  const float bx = (float)dx * P.wf[0] - oi.x;
+  const int flat = tx + P.nb[0] * (ty + P.nb[1] * tz);
+  int cnt = 0;
+  if (look) {
+    cnt = bin_count[flat];
+    cnt = cnt < P.bcap ? cnt : P.bcap;
+  }
+  const int cmax = __reduce_max_sync(0xffffffffu, cnt);
+  const BinEntry *be = bins + (size_t)flat * P.bcap;
+  for (int s = 0; s < cmax; ++s) {
+    if (s < cnt) {
+      const BinEntry b = be[s];
+      const unsigned j = b.idx & IDX_MASK;
+      const float ex = bx + b.ox, ey = by + b.oy, ez = bz + b.oz;
+      const float r2 = ex * ex + ey * ey + ez * ez;
+      if (j != (unsigned)i && r2 < P.rc2_band) {
+        const unsigned wc = b.idx >> IDX_BITS;
+        const int mx = kx - ((int)(wc % 3u) - 1), my = ky - ((int)((wc / 3u) % 3u) - 1),
+                  mz = kz - ((int)(wc / 9u) - 1);
+        if (mx < -1 || mx > 1 || my < -1 || my > 1 || mz < -1 || mz > 1) {
+          atomicOr(err, ERR_DRIFT);
+        } else if (nc >= cap) {
+          atomicOr(err, ERR_PAIR_OVERFLOW);
+        } else {
+          const unsigned u = j | ((unsigned)((mx + 1) + 3 * (my + 1) + 9 * (mz + 1)) << IDX_BITS);
+          int pos = nc++;
+          if (!FAST) {  // ascending neighbour index
+            while (pos > 0) {
+              const unsigned prev = cget(pos - 1);
+              if ((prev & IDX_MASK) <= j) break;
+              cset(pos, prev);
+              --pos;
+            }
+          }
+          cset(pos, u);
+        }
+      }
+    }
+  }
+}
+
+// Pass 1 of the density sweep for atom i: the candidates of the 27 bins
+// around its own (at most P.kcap).  Returns their number.
 template <bool FAST, class Get, class Set>
 __device__ __forceinline__ int collect_candidates(const StepParams &P, int i, bool active, int4 Bi, float4 oi,
                                                   const int *__restrict__ bin_count,
                                                   const BinEntry *__restrict__ bins, unsigned *__restrict__ err,
                                                   Get cget, Set cset) {
   int nc = 0;
-  for (int dz = -1; dz <= 1; ++dz) {
-    const int Tz = Bi.z + dz, tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
-    const int kz = Tz < 0 ? -1 : (Tz >= P.nb[2] ? 1 : 0);
-    const float bz = (float)dz * P.wf[2] - oi.z;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int Ty = Bi.y + dy, ty = Ty < 0 ? Ty + P.nb[1] : (Ty >= P.nb[1] ? Ty - P.nb[1] : Ty);
-      const int ky = Ty < 0 ? -1 : (Ty >= P.nb[1] ? 1 : 0);
-      const float by = (float)dy * P.wf[1] - oi.y;
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int Tx = Bi.x + dx, tx = Tx < 0 ? Tx + P.nb[0] : (Tx >= P.nb[0] ? Tx - P.nb[0] : Tx);
-        const int kx = Tx < 0 ? -1 : (Tx >= P.nb[0] ? 1 : 0);
-        const float bx = (float)dx * P.wf[0] - oi.x;
-        const int flat = tx + P.nb[0] * (ty + P.nb[1] * tz);
-        int cnt = 0;
-        if (active) {
-          cnt = bin_count[flat];
-          cnt = cnt < P.bcap ? cnt : P.bcap;
-        }
-        const int cmax = __reduce_max_sync(0xffffffffu, cnt);
-        const BinEntry *be = bins + (size_t)flat * P.bcap;
-        for (int s = 0; s < cmax; ++s) {
-          if (s < cnt) {
-            const BinEntry b = be[s];
-            const unsigned j = b.idx & IDX_MASK;
-            const float ex = bx + b.ox, ey = by + b.oy, ez = bz + b.oz;
-            const float r2 = ex * ex + ey * ey + ez * ez;
-            if (j != (unsigned)i && r2 < P.rc2_band) {
-              const unsigned wc = b.idx >> IDX_BITS;
-              const int mx = kx - ((int)(wc % 3u) - 1), my = ky - ((int)((wc / 3u) % 3u) - 1),
-                        mz = kz - ((int)(wc / 9u) - 1);
-              if (mx < -1 || mx > 1 || my < -1 || my > 1 || mz < -1 || mz > 1) {
-                atomicOr(err, ERR_DRIFT);
-              } else if (nc >= P.kcap) {
-                atomicOr(err, ERR_PAIR_OVERFLOW);
-              } else {
-                const unsigned u = j | ((unsigned)((mx + 1) + 3 * (my + 1) + 9 * (mz + 1)) << IDX_BITS);
-                int pos = nc++;
-                if (!FAST) {  // ascending neighbour index
-                  while (pos > 0) {
-                    const unsigned prev = cget(pos - 1);
-                    if ((prev & IDX_MASK) <= j) break;
-                    cset(pos, prev);
-                    --pos;
-                  }
-                }
-                cset(pos, u);
-              }
-            }
-          }
-        }
-      }
-    }
-  }
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx)
+        bin_candidates<FAST>(P, i, active, Bi, oi, dx, dy, dz, bin_count, bins, err, nc, P.kcap, cget, cset);
   return nc;
 }
-
 
 // Sort every bin's entries by atom index (one thread per bin, a handful of
 // entries each), so the candidate order below is fixed run to run.
@@ -235,6 +243,122 @@ __global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_coun
     }
     e[p] = v;
   }
+}
+
+// One in-cutoff pair (i, j) of the density sweep: rho_j(r^2) into rho_i, the
+// pair cache row at `slot`, and with FUSE_W the sums of M_i and S_i.
+template <bool FAST, bool MULTI, bool FUSE_W>
+__device__ __forceinline__ void density_pair(const StepParams &P, int ei, unsigned u, int ej, double ex, double ey,
+                                             double ez, double r2, size_t slot, unsigned *__restrict__ pj,
+                                             D4 *__restrict__ pe, double2 *__restrict__ pg,
+                                             const D4 *__restrict__ v, unsigned *__restrict__ err, double &rho,
+                                             double &mxx, double &mxy, double &mxz, double &myy, double &myz,
+                                             double &mzz, double &Sx, double &Sy, double &Sz) {
+  const double rji = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+  double rij = rji;
+  if (MULTI && ej != ei)
+    rij = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+  rho += rji;
+  pj[slot] = u;
+  if (FAST) {
+    const double inv_r2 = recip_nr(r2);
+    const double H = rji * inv_r2;
+    pe[slot] = D4{ex, ey, ez, H};
+    if (MULTI) pg[slot] = make_double2(rij * inv_r2, 0.0);
+    if (FUSE_W) {
+      const D4 vj = v[u & IDX_MASK];
+      const double hx = H * ex, hy = H * ey, hz = H * ez;
+      mxx = fma(hx, ex, mxx);
+      mxy = fma(hx, ey, mxy);
+      mxz = fma(hx, ez, mxz);
+      myy = fma(hy, ey, myy);
+      myz = fma(hy, ez, myz);
+      mzz = fma(hz, ez, mzz);
+      const double d = dot3_fma(ex, ey, ez, vj.x, vj.y, vj.z);
+      Sx = fma(d, hx, Sx);
+      Sy = fma(d, hy, Sy);
+      Sz = fma(d, hz, Sz);
+    }
+  } else {
+    pe[slot] = D4{ex, ey, ez, r2};
+    pg[slot] = make_double2(rji, rij);
+  }
+}
+
+// e = x_j (periodic image of the pair code) - x_i, as the engine's ghost
+// atoms give it: (x_j + image shift) - x_i
+__device__ __forceinline__ void density_vector(const StepParams &P, const D4 &xi, const D4 &xj, unsigned code,
+                                               double &ex, double &ey, double &ez) {
+  double cx = xj.x, cy = xj.y, cz = xj.z;
+  if (code != CODE_NOSHIFT) {
+    const int mx = (int)(code % 3u) - 1, my = (int)((code / 3u) % 3u) - 1, mz = (int)(code / 9u) - 1;
+    if (mx) cx = xj.x + (mx > 0 ? P.prd[0] : -P.prd[0]);
+    if (my) cy = xj.y + (my > 0 ? P.prd[1] : -P.prd[1]);
+    if (mz) cz = xj.z + (mz > 0 ? P.prd[2] : -P.prd[2]);
+  }
+  ex = cx - xi.x;
+  ey = cy - xi.y;
+  ez = cz - xi.z;
+}
+
+// The end of the density sweep for atom i (its pairs summed): alpha, beta,
+// the deviates, its grid cell and T_e, and the per-atom records.
+template <bool FAST, bool FUSE_W>
+__device__ __forceinline__ void density_epilogue(
+    const StepParams &P, int i, bool active, const D4 &xi, int ei, double rho, int ns, double mxx, double mxy,
+    double mxz, double myy, double myz, double mzz, double Sx, double Sy, double Sz,
+    const D4 *__restrict__ xi_given, int xi_mode, const double *__restrict__ T_e, int *__restrict__ nshort,
+    D4 *__restrict__ A, D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out,
+    int *__restrict__ cell, double *__restrict__ Te_i, unsigned *__restrict__ err,
+    unsigned long long *__restrict__ counters, const D4 *__restrict__ v, D4 *__restrict__ Mm,
+    D4 *__restrict__ G) {
+  nshort[i] = ns;
+  // per-atom quantities
+  double alpha = 0.0, beta = 0.0, xi3[3] = {0.0, 0.0, 0.0};
+  if (active) {
+    if (rho > P.rho_cutoff) {  // eph_beta.h:174-197
+      atomicAdd(&counters[CNT_RHO_CUTOFF], 1ull);
+    } else {
+      beta = spline_eval<FAST>(P.tab_beta + (size_t)ei * P.n_beta, P.inv_drho, P.n_beta, rho, err);
+      if (rho > 0) alpha = spline_eval<FAST>(P.tab_alpha + (size_t)ei * P.n_beta, P.inv_drho, P.n_beta, rho, err);
+    }
+    if (FAST && rho > 0) alpha = alpha / rho;
+    if (P.flags & 0x02) {
+      if (xi_mode == 0) {
+        gaussian3(P.seed, *P.step, (unsigned)i, xi3);
+      } else {
+        const D4 g = xi_given[i];
+        xi3[0] = g.x;
+        xi3[1] = g.y;
+        xi3[2] = g.z;
+      }
+    }
+    const long c = grid_index(P, xi.x, xi.y, xi.z);
+    cell[i] = (int)c;
+    Te_i[i] = T_e[c];
+  }
+  A[i] = D4{rho, alpha, xi3[0], xi3[1]};
+  if (FUSE_W) {
+    // w_i = a_i (M_i v_i - S_i), a_i = alpha_i/rho_i; k_friction_w's rule: w
+    // stays 0 unless rho_i > 0.  For k_forces_m: M_i, and the records
+    // G_i = {a_i w_i, a_i xi_i, rho_i} that the neighbours gather.
+    double wx = 0.0, wy = 0.0, wz = 0.0;
+    if (active && pos_double(rho)) {
+      const D4 vi = v[i];
+      wx = alpha * (fma(mxx, vi.x, fma(mxy, vi.y, mxz * vi.z)) - Sx);
+      wy = alpha * (fma(mxy, vi.x, fma(myy, vi.y, myz * vi.z)) - Sy);
+      wz = alpha * (fma(mxz, vi.x, fma(myz, vi.y, mzz * vi.z)) - Sz);
+    }
+    Bw[i] = D4{xi3[2], wx, wy, wz};
+    Mm[i] = D4{mxx, mxy, mxz, myy};
+    Mm[(size_t)P.n + i] = D4{myz, mzz, 0.0, 0.0};
+    G[2 * (size_t)i] = D4{alpha * wx, alpha * wy, alpha * wz, alpha * xi3[0]};
+    G[2 * (size_t)i + 1] = D4{alpha * xi3[1], alpha * xi3[2], active ? rho : 0.0, 0.0};
+  } else {
+    Bw[i] = D4{xi3[2], 0.0, 0.0, 0.0};
+  }
+  rho_out[i] = rho;
+  beta_out[i] = beta;
 }
 
 // calculate_environment (fix_eph.cpp:431-466) plus everything per atom the
@@ -310,102 +434,132 @@ __global__ void __launch_bounds__(128) k_density(
   for (int k = 0; k < nmax; ++k) {
     if (k < nc) {
       const unsigned u = cget(k);
-      const unsigned j = u & IDX_MASK, code = u >> IDX_BITS;
-      const D4 xj = x[j];
-      double cx = xj.x, cy = xj.y, cz = xj.z;
-      if (code != CODE_NOSHIFT) {
-        const int mx = (int)(code % 3u) - 1, my = (int)((code / 3u) % 3u) - 1, mz = (int)(code / 9u) - 1;
-        if (mx) cx = xj.x + (mx > 0 ? P.prd[0] : -P.prd[0]);
-        if (my) cy = xj.y + (my > 0 ? P.prd[1] : -P.prd[1]);
-        if (mz) cz = xj.z + (mz > 0 ? P.prd[2] : -P.prd[2]);
-      }
-      const double ex = cx - xi.x, ey = cy - xi.y, ez = cz - xi.z;
+      const D4 xj = x[u & IDX_MASK];
+      double ex, ey, ez;
+      density_vector(P, xi, xj, u >> IDX_BITS, ex, ey, ez);
       const double r2 = FAST ? dot3_fma(ex, ey, ez, ex, ey, ez) : dot3(ex, ey, ez, ex, ey, ez);
       if (below(r2, P.rc2)) {  // r2 >= 0
-        const int ej = (int)xj.w;
-        const double rji =
-            spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
-        double rij = rji;
-        if (MULTI && ej != ei)
-          rij = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
-        rho += rji;
-        const size_t slot = (size_t)ns * P.n + i;
-        pj[slot] = u;
-        if (FAST) {
-          const double inv_r2 = recip_nr(r2);
-          const double H = rji * inv_r2;
-          pe[slot] = D4{ex, ey, ez, H};
-          if (MULTI) pg[slot] = make_double2(rij * inv_r2, 0.0);
-          if (FUSE_W) {
-            const D4 vj = v[j];
-            const double hx = H * ex, hy = H * ey, hz = H * ez;
-            mxx = fma(hx, ex, mxx);
-            mxy = fma(hx, ey, mxy);
-            mxz = fma(hx, ez, mxz);
-            myy = fma(hy, ey, myy);
-            myz = fma(hy, ez, myz);
-            mzz = fma(hz, ez, mzz);
-            const double d = dot3_fma(ex, ey, ez, vj.x, vj.y, vj.z);
-            Sx = fma(d, hx, Sx);
-            Sy = fma(d, hy, Sy);
-            Sz = fma(d, hz, Sz);
-          }
-        } else {
-          pe[slot] = D4{ex, ey, ez, r2};
-          pg[slot] = make_double2(rji, rij);
-        }
+        density_pair<FAST, MULTI, FUSE_W>(P, ei, u, (int)xj.w, ex, ey, ez, r2, (size_t)ns * P.n + i, pj, pe, pg,
+                                          v, err, rho, mxx, mxy, mxz, myy, myz, mzz, Sx, Sy, Sz);
         ++ns;
       }
     }
   }
   if (!valid) return;
-  nshort[i] = ns;
-  // per-atom quantities
-  double alpha = 0.0, beta = 0.0, xi3[3] = {0.0, 0.0, 0.0};
-  if (active) {
-    if (rho > P.rho_cutoff) {  // eph_beta.h:174-197
-      atomicAdd(&counters[CNT_RHO_CUTOFF], 1ull);
-    } else {
-      beta = spline_eval<FAST>(P.tab_beta + (size_t)ei * P.n_beta, P.inv_drho, P.n_beta, rho, err);
-      if (rho > 0) alpha = spline_eval<FAST>(P.tab_alpha + (size_t)ei * P.n_beta, P.inv_drho, P.n_beta, rho, err);
+  density_epilogue<FAST, FUSE_W>(P, i, active, xi, ei, rho, ns, mxx, mxy, mxz, myy, myz, mzz, Sx, Sy, Sz, xi_given,
+                                 xi_mode, T_e, nshort, A, Bw, rho_out, beta_out, cell, Te_i, err, counters, v, Mm, G);
+}
+
+// The FAST density sweep with TPA lanes per atom (TPA = 2, 4, 8) for small
+// systems, where one lane per atom leaves the SMs a few warps each and the
+// sweep waits on its loads.  Lane g of an atom searches bins g, g + TPA, ...
+// of the 27 (its candidates in its own shared-memory column, at most
+// CAND_SMEM), tests them exactly, and after a prefix sum over the atom's
+// lanes writes its in-cutoff pairs to rows [offset_g, offset_g + count_g)
+// of the pair cache; rho (and with FUSE_W, M_i and S_i) are summed over the
+// lanes by a butterfly and lane 0 finishes the atom.  Sums in a fixed order
+// (the same every run), within rounding of the one-lane sweep.
+template <bool MULTI, bool FUSE_W, int TPA>
+__global__ void __launch_bounds__(128) k_density_tpa(
+    StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
+    const BinEntry *__restrict__ bins, const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
+    const D4 *__restrict__ xi_given, int xi_mode, const double *__restrict__ T_e, unsigned *__restrict__ pj,
+    D4 *__restrict__ pe, double2 *__restrict__ pg, int *__restrict__ nshort, D4 *__restrict__ A,
+    D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell,
+    double *__restrict__ Te_i, int *__restrict__ wrapflag, unsigned *__restrict__ err,
+    unsigned long long *__restrict__ counters, const D4 *__restrict__ v, D4 *__restrict__ Mm,
+    D4 *__restrict__ G) {
+  static_assert(CAND_SMEM <= 64, "candidate masks are 64 bits");
+  __shared__ unsigned s_cand[CAND_SMEM * 128];
+  const long gt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(gt / TPA), g = (int)(gt % TPA);
+  const int t = threadIdx.x, nt = blockDim.x;
+  if (gt == 0) *wrapflag = 0;  // the binning kernel has read it
+  const bool valid = i < P.n;
+  const bool active = valid && (mask[i] & P.groupbit) != 0;
+  auto cget = [&](int k) -> unsigned { return s_cand[k * nt + t]; };
+  auto cset = [&](int k, unsigned u) { s_cand[k * nt + t] = u; };
+  D4 xi = D4{0.0, 0.0, 0.0, 0.0};
+  if (valid) xi = x[i];
+  const int ei = (int)xi.w;
+  // pass 1: this lane's bins (the same number of rounds on every lane)
+  int nc = 0;
+  {
+    int4 Bi = make_int4(0, 0, 0, 0);
+    float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) {
+      Bi = atom_bin[i];
+      oi = atom_off[i];
     }
-    if (FAST && rho > 0) alpha = alpha / rho;
-    if (P.flags & 0x02) {
-      if (xi_mode == 0) {
-        gaussian3(P.seed, *P.step, (unsigned)i, xi3);
-      } else {
-        const D4 g = xi_given[i];
-        xi3[0] = g.x;
-        xi3[1] = g.y;
-        xi3[2] = g.z;
-      }
+    for (int m = 0; m < (27 + TPA - 1) / TPA; ++m) {
+      const int b = g + m * TPA;  // (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)
+      const bool look = active && b < 27;
+      const int bb = b < 27 ? b : 13;
+      bin_candidates<true>(P, i, look, Bi, oi, bb % 3 - 1, (bb / 3) % 3 - 1, bb / 9 - 1, bin_count, bins, err, nc,
+                           CAND_SMEM, cget, cset);
     }
-    const long c = grid_index(P, xi.x, xi.y, xi.z);
-    cell[i] = (int)c;
-    Te_i[i] = T_e[c];
   }
-  A[i] = D4{rho, alpha, xi3[0], xi3[1]};
-  if (FUSE_W) {
-    // w_i = a_i (M_i v_i - S_i), a_i = alpha_i/rho_i; k_friction_w's rule: w
-    // stays 0 unless rho_i > 0.  For k_forces_m: M_i, and the records
-    // G_i = {a_i w_i, a_i xi_i, rho_i} that the neighbours gather.
-    double wx = 0.0, wy = 0.0, wz = 0.0;
-    if (active && pos_double(rho)) {
-      const D4 vi = v[i];
-      wx = alpha * (fma(mxx, vi.x, fma(mxy, vi.y, mxz * vi.z)) - Sx);
-      wy = alpha * (fma(mxy, vi.x, fma(myy, vi.y, myz * vi.z)) - Sy);
-      wz = alpha * (fma(mxz, vi.x, fma(myz, vi.y, mzz * vi.z)) - Sz);
+  __syncwarp();
+  // pass 2a: the exact test of this lane's candidates
+  unsigned long long keep = 0ull;
+  const int nmax = __reduce_max_sync(0xffffffffu, nc);
+  for (int k = 0; k < nmax; ++k) {
+    if (k < nc) {
+      const unsigned u = cget(k);
+      double ex, ey, ez;
+      density_vector(P, xi, x[u & IDX_MASK], u >> IDX_BITS, ex, ey, ez);
+      if (below(dot3_fma(ex, ey, ez, ex, ey, ez), P.rc2)) keep |= 1ull << k;
     }
-    Bw[i] = D4{xi3[2], wx, wy, wz};
-    Mm[i] = D4{mxx, mxy, mxz, myy};
-    Mm[(size_t)P.n + i] = D4{myz, mzz, 0.0, 0.0};
-    G[2 * (size_t)i] = D4{alpha * wx, alpha * wy, alpha * wz, alpha * xi3[0]};
-    G[2 * (size_t)i + 1] = D4{alpha * xi3[1], alpha * xi3[2], active ? rho : 0.0, 0.0};
-  } else {
-    Bw[i] = D4{xi3[2], 0.0, 0.0, 0.0};
   }
-  rho_out[i] = rho;
-  beta_out[i] = beta;
+  // rows of this lane's pairs: an exclusive prefix sum over the atom's lanes
+  const int count = __popcll(keep);
+  int incl = count;
+#pragma unroll
+  for (int d = 1; d < TPA; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (g >= d) incl += y;
+  }
+  const int ns = __shfl_sync(0xffffffffu, incl, (int)(threadIdx.x & 31) | (TPA - 1));
+  const int off = incl - count;
+  if (ns > P.kcap && g == 0 && valid) atomicOr(err, ERR_PAIR_OVERFLOW);
+  // pass 2b: the kept pairs
+  double rho = 0.0, Sx = 0.0, Sy = 0.0, Sz = 0.0;
+  double mxx = 0.0, mxy = 0.0, mxz = 0.0, myy = 0.0, myz = 0.0, mzz = 0.0;
+  unsigned long long rest = keep;
+  const int n2 = __reduce_max_sync(0xffffffffu, count);
+  for (int m = 0; m < n2; ++m) {
+    if (m < count) {
+      const int k = __ffsll((long long)rest) - 1;
+      rest &= rest - 1ull;
+      const unsigned u = cget(k);
+      const D4 xj = x[u & IDX_MASK];
+      double ex, ey, ez;
+      density_vector(P, xi, xj, u >> IDX_BITS, ex, ey, ez);
+      const double r2 = dot3_fma(ex, ey, ez, ex, ey, ez);
+      if (off + m < P.kcap)
+        density_pair<true, MULTI, FUSE_W>(P, ei, u, (int)xj.w, ex, ey, ez, r2, (size_t)(off + m) * P.n + i, pj, pe,
+                                          pg, v, err, rho, mxx, mxy, mxz, myy, myz, mzz, Sx, Sy, Sz);
+    }
+  }
+#pragma unroll
+  for (int o = TPA / 2; o > 0; o >>= 1) {
+    rho += __shfl_xor_sync(0xffffffffu, rho, o);
+    if (FUSE_W) {
+      mxx += __shfl_xor_sync(0xffffffffu, mxx, o);
+      mxy += __shfl_xor_sync(0xffffffffu, mxy, o);
+      mxz += __shfl_xor_sync(0xffffffffu, mxz, o);
+      myy += __shfl_xor_sync(0xffffffffu, myy, o);
+      myz += __shfl_xor_sync(0xffffffffu, myz, o);
+      mzz += __shfl_xor_sync(0xffffffffu, mzz, o);
+      Sx += __shfl_xor_sync(0xffffffffu, Sx, o);
+      Sy += __shfl_xor_sync(0xffffffffu, Sy, o);
+      Sz += __shfl_xor_sync(0xffffffffu, Sz, o);
+    }
+  }
+  if (!valid || g != 0) return;
+  density_epilogue<true, FUSE_W>(P, i, active, xi, ei, rho, ns < P.kcap ? ns : P.kcap, mxx, mxy, mxz, myy, myz, mzz,
+                                 Sx, Sy, Sz, xi_given, xi_mode, T_e, nshort, A, Bw, rho_out, beta_out, cell, Te_i,
+                                 err, counters, v, Mm, G);
 }
 
 // -------------------------------------------------------- friction sweep 1
