@@ -333,7 +333,11 @@ int launch_bin(eph_ctx *c) {
   k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
                                      c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 1);
   ps.launched();
-  k_bin_sort<<<nblocks(c->nbins), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p, c->bins.p);
+  if (c->bcap <= 64)
+    k_bin_sort_warp<<<nblocks((long)c->nbins * 32), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p,
+                                                                            c->bins.p);
+  else
+    k_bin_sort<<<nblocks(c->nbins), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p, c->bins.p);
   CUDA_TRY(c, cudaGetLastError());
   return EPH_OK;
 }

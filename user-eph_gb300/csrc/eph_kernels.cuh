@@ -225,6 +225,33 @@ __device__ __forceinline__ int collect_candidates(const StepParams &P, int i, bo
   return nc;
 }
 
+// The same sort with one warp per bin, for bins of at most 64 entries: lane l
+// holds entries l and l + 32, each entry's place is the number of entries
+// with a smaller atom index (indices are distinct), found by broadcasting
+// every entry's key across the warp; all loads happen before any store.
+__global__ void k_bin_sort_warp(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins) {
+  const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nbins) return;  // whole warps leave together
+  int cnt = bin_count[w];
+  cnt = cnt < bcap ? cnt : bcap;
+  BinEntry *e = bins + (size_t)w * bcap;
+  const bool h0 = lane < cnt, h1 = lane + 32 < cnt;
+  BinEntry a{}, b{};
+  if (h0) a = e[lane];
+  if (h1) b = e[lane + 32];
+  const unsigned ka = h0 ? (a.idx & IDX_MASK) : 0xffffffffu, kb = h1 ? (b.idx & IDX_MASK) : 0xffffffffu;
+  int ra = 0, rb = 0;
+  for (int s = 0; s < 32; ++s) {
+    const unsigned k0 = __shfl_sync(0xffffffffu, ka, s), k1 = __shfl_sync(0xffffffffu, kb, s);
+    ra += (k0 < ka) + (k1 < ka);
+    rb += (k0 < kb) + (k1 < kb);
+  }
+  __syncwarp();
+  if (h0) e[ra] = a;
+  if (h1) e[rb] = b;
+}
+
 // Sort every bin's entries by atom index (one thread per bin, a handful of
 // entries each), so the candidate order below is fixed run to run.
 __global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins) {
