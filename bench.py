@@ -362,6 +362,21 @@ def run_adjoint(args, dev, fd=True):
         e1.record(stream)
         torch.cuda.synchronize()
         plain_ms = e0.elapsed_time(e1)
+        # the same gradient with the whole trajectory recorded as one segment:
+        # no recomputation (the recorded steps take ~4 GB at this size)
+        fix1 = ephgb.FixEPH(words, atoms, dt=ADJ_DT, mode=ephgb.MODE_FAST, device=dev)
+        adj1 = Adjoint(fix1, checkpoint_every=nsteps)
+        adj1.set_knots(0, r0, b0)
+        for _ in range(3):
+            E1, _ = adj1.forward(nsteps)
+            adj1.backward(2.0 * (E1 - target), None)
+        t1 = adj1.timing()
+        g1 = adj1.gradients(0)
+        one_seg = {"backward_ms": t1["backward_ms"], "forward_ms": t1["forward_ms"],
+                   "adjoint_over_forward": t1["backward_ms"] / t1["forward_ms"],
+                   "gradient_identical_to_checkpointed": all(
+                       np.array_equal(np.asarray(g[k]), np.asarray(g1[k])) for k in g)}
+        del adj1, fix1
         res = {"workload": "fcc Ni 20^3 cells (32,000 atoms), ions 300 K, T_e 2,000 K, FDM 16^3, %d steps of 1 fs, "
                            "flags 7; 64 beta knots (beta = 0.02 + 2 rho^2), 16 rho(r) knots, C_e, kappa_e; "
                            "checkpoints every 20 steps" % nsteps,
@@ -371,6 +386,7 @@ def run_adjoint(args, dev, fd=True):
                "forward_plus_adjoint_over_plain_forward": (t["forward_ms"] + t["backward_ms"]) / plain_ms,
                "forward_launches": t["forward_launches"], "backward_launches": t["backward_launches"],
                "rho_cutoff_crossings": rho_cut_events,
+               "one_segment": one_seg,
                "timing": "CUDA events on the fix's stream (graph replays); backward includes the recomputation "
                          "from checkpoints"}
         if not fd:
