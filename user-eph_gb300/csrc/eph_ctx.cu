@@ -425,14 +425,30 @@ int launch_end_of_step(eph_ctx *c) {
     double *src = c->T0.p, *dst = c->T1.p;
     for (unsigned s = 0; s < c->nsub; ++s) {
       if (c->fdm_rec) dst = c->fdm_rec + (size_t)s * (size_t)g.ntotal;
+      // each substep a programmatic dependent of the one before (the kernel
+      // waits for it before touching memory; its launch overlaps that tail)
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(nblocks(g.ntotal, 64));
+      cfg.blockDim = dim3(64);
+      cfg.stream = c->stream;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      at[0].val.programmaticStreamSerializationAllowed = s > 0 ? 1 : 0;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      const double *csrc = src;
+      const int first = s == 0;
       if (c->mode == EPH_MODE_FAST)
-        k_fdm_substep<true><<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(
-            g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt, src, dst, c->kappa.p, c->rhoC.p, c->S.p, c->gflag.p,
-            c->dT.p, c->acc.p, s == 0, c->counters.p, c->td, ih2, c->irhoC.p);
+        CUDA_TRY(c, cudaLaunchKernelEx(&cfg, k_fdm_substep<true>, (long)g.nx, (long)g.ny, (long)g.nz, g.dx, g.dy, g.dz,
+                                       c->inner_dt, csrc, dst, (const double *)c->kappa.p, (const double *)c->rhoC.p,
+                                       (const double *)c->S.p, (const signed char *)c->gflag.p, c->dT.p, c->acc.p,
+                                       first, c->counters.p, c->td, ih2, (const double *)c->irhoC.p));
       else
-        k_fdm_substep<false><<<nblocks(g.ntotal, 64), 64, 0, c->stream>>>(
-            g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, c->inner_dt, src, dst, c->kappa.p, c->rhoC.p, c->S.p, c->gflag.p,
-            c->dT.p, c->acc.p, s == 0, c->counters.p, c->td, ih2, c->irhoC.p);
+        CUDA_TRY(c, cudaLaunchKernelEx(&cfg, k_fdm_substep<false>, (long)g.nx, (long)g.ny, (long)g.nz, g.dx, g.dy,
+                                       g.dz, c->inner_dt, csrc, dst, (const double *)c->kappa.p,
+                                       (const double *)c->rhoC.p, (const double *)c->S.p,
+                                       (const signed char *)c->gflag.p, c->dT.p, c->acc.p, first, c->counters.p,
+                                       c->td, ih2, (const double *)c->irhoC.p));
       if (c->fdm_rec) src = dst;
       else std::swap(src, dst);
     }

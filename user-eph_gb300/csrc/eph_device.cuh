@@ -84,6 +84,11 @@ struct StepParams {
 // keep these tests off the FP64 pipe (IEEE order of non-negative doubles is
 // the order of their bits).
 __device__ __forceinline__ bool pos_double(double v) { return __double_as_longlong(v) > 0; }
+
+// Wait until the grids this one depends on programmatically have completed
+// and their memory is visible (griddepcontrol.wait; returns at once for a
+// kernel launched without a programmatic dependency).
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ bool below(double v, double c) { return __double_as_longlong(v) < __double_as_longlong(c); }
 
 // (size_t)y for a non-negative double y, by integer work on its bits (the

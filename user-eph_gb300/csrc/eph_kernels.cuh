@@ -1156,7 +1156,11 @@ __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, d
                               unsigned long long *__restrict__ counters, TdynTables td, double3 ih2,
                               const double *__restrict__ irhoC) {
   // FAST: ih2 = 1/h^2 per axis and irhoC = 1/(rho_e C_e) per cell come
-  // precomputed (the same correctly rounded quotients as 1.0 / x here)
+  // precomputed (the same correctly rounded quotients as 1.0 / x here).
+  // Launched as a programmatic dependent of the kernel before it (its launch
+  // overlaps that kernel's tail): wait for that kernel's results before
+  // touching memory.
+  griddep_wait();
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long ntotal = nx * ny * nz;
   if (r >= ntotal) return;
