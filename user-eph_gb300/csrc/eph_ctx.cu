@@ -186,15 +186,10 @@ int launch_final(eph_ctx *c) {
 }
 
 // FAST mode folds stage 1 (the friction pre-vector) and M_i into the density
-// sweep, and stages 2 and 3 run as k_forces_m (any number of lanes per atom).
-// Below 16,384 atoms with several lanes per atom the separate stage-1 sweep
-// stays: there the one-lane density sweep is the latency bottleneck and
-// stage 1 is better split over the lanes (measured on GB300: 4,000 atoms
-// 0.290 ms per step separate, 0.304 ms folded; 32,000 atoms and up faster
-// folded).
+// sweep (one lane per atom, or below 16,384 atoms the lanes of
+// k_density_tpa), and stages 2 and 3 run as k_forces_m with the same lanes.
 bool fused_friction(const eph_ctx *c) {
-  return c->mode == EPH_MODE_FAST && c->args.model == 4 && (c->P.flags & FLAG_FRICTION) && c->fuse_w &&
-         (c->tpa == 1 || c->n >= 16384);
+  return c->mode == EPH_MODE_FAST && c->args.model == 4 && (c->P.flags & FLAG_FRICTION) && c->fuse_w;
 }
 
 template <bool FAST, bool MULTI, bool FUSE>
@@ -204,7 +199,7 @@ void launch_density_f(eph_ctx *c, int xi_mode) {
   // 0.289 -> 0.210 ms per step; from 16,384 atoms on the extra exact-test pass
   // and lane sums cost more than they hide: 32,000 atoms 71 -> 81 ms per 200
   // steps, so the one-lane sweep stays there)
-  if constexpr (FAST && !FUSE) {
+  if constexpr (FAST) {
     if (c->tpa > 1 && c->n < 16384) {
 #define EPH_DENSITY_TPA(T)                                                                                         \
   k_density_tpa<MULTI, FUSE, T><<<nblocks((long)c->n * T), BLOCK, 0, c->stream>>>(                                  \
@@ -267,30 +262,10 @@ void launch_forces_t(eph_ctx *c) {
 // from ~30,000 atoms on the lanes make no difference)
 int auto_tpa(long n) { return n <= 65536 ? 4 : 1; }
 
+// stage 1 as its own sweep: EXACT mode (FAST mode folds it into the density sweep)
 void launch_friction_w(eph_ctx *c) {
-  const int nb = nblocks(c->n);
-  if (c->mode != EPH_MODE_FAST) {
-    k_friction_w<false><<<nb, BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
-                                                     c->nshort.p, c->A.p, c->Bw.p);
-    return;
-  }
-  switch (c->tpa) {
-    case 2:
-      k_friction_w_tpa<2><<<nblocks((long)c->n * 2), BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p,
-                                                                            c->pe.p, c->nshort.p, c->A.p, c->Bw.p);
-      break;
-    case 4:
-      k_friction_w_tpa<4><<<nblocks((long)c->n * 4), BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p,
-                                                                            c->pe.p, c->nshort.p, c->A.p, c->Bw.p);
-      break;
-    case 8:
-      k_friction_w_tpa<8><<<nblocks((long)c->n * 8), BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p,
-                                                                            c->pe.p, c->nshort.p, c->A.p, c->Bw.p);
-      break;
-    default:
-      k_friction_w<true><<<nb, BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
-                                                      c->nshort.p, c->A.p, c->Bw.p);
-  }
+  k_friction_w<<<nblocks(c->n), BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
+                                                       c->nshort.p, c->A.p, c->Bw.p);
 }
 
 template <bool FAST, bool FRIC, bool RAND>

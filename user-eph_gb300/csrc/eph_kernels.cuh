@@ -591,9 +591,9 @@ __global__ void __launch_bounds__(128) k_density_tpa(
 
 // -------------------------------------------------------- friction sweep 1
 
-// force_prl stage 1 (fix_eph.cpp:699-741):
+// force_prl stage 1 (fix_eph.cpp:699-741) in the reference's expression order
+// (EXACT mode; FAST mode folds it into the density sweep):
 // w_i = sum_j p_ij [(e.v_i) - (e.v_j)] e,  p_ij = alpha_i rho_j(r^2) / (rho_i r^2)
-template <bool FAST>
 __global__ void __launch_bounds__(128) k_friction_w(StepParams P, const int *__restrict__ mask,
                                                      const D4 *__restrict__ v, const unsigned *__restrict__ pj,
                                                      const D4 *__restrict__ pe, const double2 *__restrict__ pg,
@@ -611,23 +611,14 @@ __global__ void __launch_bounds__(128) k_friction_w(StepParams P, const int *__r
     const unsigned j = pj[slot] & IDX_MASK;
     const D4 e = pe[slot];
     const D4 vj = v[j];
-    if (FAST) {
-      const double c = Ai.y * e.w;  // alpha_i/rho_i * rho_j(r^2)/r^2
-      const double d = dot3_fma(e.x, e.y, e.z, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
-      const double s = c * d;
-      wx = fma(s, e.x, wx);
-      wy = fma(s, e.y, wy);
-      wz = fma(s, e.z, wz);
-    } else {
-      const double rji = pg[slot].x;
-      const double prescaler = Ai.y * rji / (Ai.x * e.w);
-      const double var1 = prescaler * dot3(e.x, e.y, e.z, vi.x, vi.y, vi.z);
-      const double var2 = prescaler * dot3(e.x, e.y, e.z, vj.x, vj.y, vj.z);
-      const double dvar = var1 - var2;
-      wx += dvar * e.x;
-      wy += dvar * e.y;
-      wz += dvar * e.z;
-    }
+    const double rji = pg[slot].x;
+    const double prescaler = Ai.y * rji / (Ai.x * e.w);
+    const double var1 = prescaler * dot3(e.x, e.y, e.z, vi.x, vi.y, vi.z);
+    const double var2 = prescaler * dot3(e.x, e.y, e.z, vj.x, vj.y, vj.z);
+    const double dvar = var1 - var2;
+    wx += dvar * e.x;
+    wy += dvar * e.y;
+    wz += dvar * e.z;
   }
   const double xiz = Bw[i].x;
   Bw[i] = D4{xiz, wx, wy, wz};
@@ -869,46 +860,6 @@ __global__ void __launch_bounds__(128) k_forces_m(StepParams P, const unsigned *
 // the SMs with a few warps each and the one-lane sweeps wait on their loads;
 // TPA times more warps hide that.  The order of the sums depends on TPA
 // (results within rounding of the one-lane sweeps, the same every run).
-template <int TPA>
-__global__ void __launch_bounds__(128) k_friction_w_tpa(StepParams P, const int *__restrict__ mask,
-                                                         const D4 *__restrict__ v, const unsigned *__restrict__ pj,
-                                                         const D4 *__restrict__ pe, const int *__restrict__ nshort,
-                                                         const D4 *__restrict__ A, D4 *__restrict__ Bw) {
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = gt / TPA, g = gt % TPA;
-  bool act = false;
-  D4 Ai{0.0, 0.0, 0.0, 0.0};
-  if (i < P.n) {
-    Ai = A[i];
-    act = (mask[i] & P.groupbit) && pos_double(Ai.x);
-  }
-  double wx = 0.0, wy = 0.0, wz = 0.0;
-  if (act) {
-    const D4 vi = v[i];
-    const int ns = nshort[i];
-    for (int k = g; k < ns; k += TPA) {
-      const size_t slot = (size_t)k * P.n + i;
-      const unsigned j = pj[slot] & IDX_MASK;
-      const D4 e = pe[slot];
-      const D4 vj = v[j];
-      const double s = Ai.y * e.w * dot3_fma(e.x, e.y, e.z, vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
-      wx = fma(s, e.x, wx);
-      wy = fma(s, e.y, wy);
-      wz = fma(s, e.z, wz);
-    }
-  }
-#pragma unroll
-  for (int o = TPA / 2; o > 0; o >>= 1) {
-    wx += __shfl_xor_sync(0xffffffffu, wx, o);
-    wy += __shfl_xor_sync(0xffffffffu, wy, o);
-    wz += __shfl_xor_sync(0xffffffffu, wz, o);
-  }
-  if (act && g == 0) {
-    const double xiz = Bw[i].x;
-    Bw[i] = D4{xiz, wx, wy, wz};
-  }
-}
-
 template <bool MULTI, bool FRIC, bool RAND, int TPA>
 __global__ void __launch_bounds__(128) k_forces_tpa(StepParams P, const int *__restrict__ mask,
                                                      const unsigned *__restrict__ pj, const D4 *__restrict__ pe,
