@@ -653,7 +653,7 @@ def main():
     ap.add_argument("--only-fit", action="store_true", help="run the batched adjoint fitting leg alone")
     ap.add_argument("--fit-replicas", type=int, default=16)
     ap.add_argument("--fit-steps", type=int, default=100)
-    ap.add_argument("--fit-iters", type=int, default=30)
+    ap.add_argument("--fit-iters", type=int, default=60)
     ap.add_argument("--cells", type=int, default=CELLS, help="fcc cells per edge (profiling cases)")
     ap.add_argument("--grid", type=int, default=GRID[0], help="FDM cells per edge (profiling cases)")
     args = ap.parse_args()
