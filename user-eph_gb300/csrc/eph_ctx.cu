@@ -258,9 +258,10 @@ void launch_forces_t(eph_ctx *c) {
 
 // lanes per atom of the FAST pair sweeps for n atoms: more lanes where the
 // one-lane sweeps leave the SMs with too few warps to hide their loads
-// (measured on GB300: 4,000 atoms 0.467 -> 0.420 ms per step with 4 lanes;
-// from ~30,000 atoms on the lanes make no difference)
-int auto_tpa(long n) { return n <= 65536 ? 4 : 1; }
+// (measured on GB300, µs per step with 2 / 4 / 8 lanes: 2,048 atoms
+// 207 / 171 / 148; 4,000 atoms 220 / 185 / 177; 8,788 atoms 226 / 213 / 235;
+// 16,384 atoms 282 / 280 / 284; above ~65,000 atoms one lane)
+int auto_tpa(long n) { return n <= 6144 ? 8 : (n <= 65536 ? 4 : 1); }
 
 // stage 1 as its own sweep: EXACT mode (FAST mode folds it into the density sweep)
 void launch_friction_w(eph_ctx *c) {
