@@ -67,6 +67,8 @@ struct eph_ctx {
   bool tpa_auto = true;
   // FAST mode, one lane per atom: stage 1 folded into the density sweep
   bool fuse_w = true;
+  // small grids run all their substeps as one thread-block cluster launch
+  bool fdm_cluster = false;
 
   int n = 0;
   DevBuf<D4> x, v, f, xhold, f_eph, f_rng, xi, fext, A, Bw;

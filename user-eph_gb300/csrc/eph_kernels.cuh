@@ -1093,38 +1093,23 @@ __global__ void k_fdm_bounds(long ncells, const double *__restrict__ C, const do
   }
 }
 
-// One substep of EPH_FDM::solve (eph_fdm.h:315-396) with the reference's
-// expression order: the variable-kappa 7-point stencil with periodic wrap and
-// ZERO_DERIVATIVE walls, then T += (ddT + dT + S)/(rho_e C_e) dt' on DYNAMIC
-// cells and the clamp at T = 0.  Reads T_in, writes T_out.  The first
-// substep turns the fixed-point deposits into dT and clears them.
-template <bool FAST>
-__global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, double dz, double inner_dt,
-                              const double *__restrict__ T, double *__restrict__ Tout,
-                              const double *__restrict__ kappa, const double *__restrict__ rhoC,
-                              const double *__restrict__ S, const signed char *__restrict__ flag,
-                              double *__restrict__ dT, U128 *__restrict__ acc, int first,
-                              unsigned long long *__restrict__ counters, TdynTables td, double3 ih2,
-                              const double *__restrict__ irhoC) {
-  // FAST: ih2 = 1/h^2 per axis and irhoC = 1/(rho_e C_e) per cell come
-  // precomputed (the same correctly rounded quotients as 1.0 / x here).
-  // Launched as a programmatic dependent of the kernel before it (its launch
-  // overlaps that kernel's tail): wait for that kernel's results before
-  // touching memory.
-  griddep_wait();
-  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long ntotal = nx * ny * nz;
-  if (r >= ntotal) return;
-  double dTr;
-  if (first) {
-    U128 a = acc[r];
-    dTr = from_fixed(a);
-    dT[r] = dTr;
-    acc[r] = U128{0ull, 0ull};
-  } else {
-    dTr = dT[r];
-  }
+// T of cell r after one substep of EPH_FDM::solve (eph_fdm.h:315-396) with
+// the reference's expression order: the variable-kappa 7-point stencil with
+// periodic wrap and ZERO_DERIVATIVE walls, then T += (ddT + dT + S)/(rho_e C_e)
+// dt' on DYNAMIC cells and the clamp at T = 0.  FAST: ih2 = 1/h^2 per axis and
+// irhoC = 1/(rho_e C_e) per cell come precomputed (the same correctly rounded
+// quotients as 1.0 / x here).  CG: read the temperatures through L2 only
+// (other blocks wrote them in the substep before).
+template <bool FAST, bool CG>
+__device__ __forceinline__ double fdm_cell(long r, long nx, long ny, long nz, double dx, double dy, double dz,
+                                           double inner_dt, const double *__restrict__ T,
+                                           const double *__restrict__ kappa, const double *__restrict__ rhoC,
+                                           const double *__restrict__ S, const signed char *__restrict__ flag,
+                                           double dTr, unsigned long long *__restrict__ counters,
+                                           const TdynTables &td, double3 ih2, const double *__restrict__ irhoC) {
+  auto ldT = [&](long k) -> double { return CG ? __ldcg(T + k) : T[k]; };
   const long i = r % nx, j = (r / nx) % ny, k = r / (nx * ny);
+  const double Tr = ldT(r);
   double ddT = 0.0;
   if (flag[r] != 2) {
     long p, q;
@@ -1140,17 +1125,18 @@ __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, d
       q = qr[a];
       if (flag[q] == 2) q = r;
       else if (flag[p] == 2) p = r;
+      const double Tq = ldT(q), Tp = ldT(p);
       if (FAST) {  // reciprocals instead of the reference's divisions (within 1e-15 of them)
-        const double ih2 = ih2s[a];
-        ddT = fma((kappa[q] - kappa[p]) * (T[q] - T[p]), 0.25 * ih2, ddT);
-        ddT = fma(kappa[r] * ih2, T[q] + T[p] - 2.0 * T[r], ddT);
+        const double ih2v = ih2s[a];
+        ddT = fma((kappa[q] - kappa[p]) * (Tq - Tp), 0.25 * ih2v, ddT);
+        ddT = fma(kappa[r] * ih2v, Tq + Tp - 2.0 * Tr, ddT);
       } else {
-        ddT += (kappa[q] - kappa[p]) * (T[q] - T[p]) / h[a] / h[a] / 4.0;
-        ddT += kappa[r] * ((T[q] + T[p] - 2.0 * T[r]) / h[a] / h[a]);
+        ddT += (kappa[q] - kappa[p]) * (Tq - Tp) / h[a] / h[a] / 4.0;
+        ddT += kappa[r] * ((Tq + Tp - 2.0 * Tr) / h[a] / h[a]);
       }
     }
   }
-  double t = T[r];
+  double t = Tr;
   if (FAST && flag[r] == 1 && !(td.tdyn && td.tdyn[r] == 1)) {
     t = fma((ddT + dTr + S[r]) * inner_dt, irhoC[r], t);
   } else if (flag[r] == 1) {
@@ -1166,7 +1152,80 @@ __global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, d
     t = 0.0;
     atomicAdd(&counters[CNT_T_CLAMP], 1ull);
   }
-  Tout[r] = t;
+  return t;
+}
+
+// One substep over the grid, one thread per cell: reads T, writes Tout.  The
+// first substep turns the fixed-point deposits into dT and clears them.
+// Launched as a programmatic dependent of the kernel before it (its launch
+// overlaps that kernel's tail): waits for that kernel's results before
+// touching memory.
+template <bool FAST>
+__global__ void k_fdm_substep(long nx, long ny, long nz, double dx, double dy, double dz, double inner_dt,
+                              const double *__restrict__ T, double *__restrict__ Tout,
+                              const double *__restrict__ kappa, const double *__restrict__ rhoC,
+                              const double *__restrict__ S, const signed char *__restrict__ flag,
+                              double *__restrict__ dT, U128 *__restrict__ acc, int first,
+                              unsigned long long *__restrict__ counters, TdynTables td, double3 ih2,
+                              const double *__restrict__ irhoC) {
+  griddep_wait();
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long ntotal = nx * ny * nz;
+  if (r >= ntotal) return;
+  double dTr;
+  if (first) {
+    U128 a = acc[r];
+    dTr = from_fixed(a);
+    dT[r] = dTr;
+    acc[r] = U128{0ull, 0ull};
+  } else {
+    dTr = dT[r];
+  }
+  Tout[r] = fdm_cell<FAST, false>(r, nx, ny, nz, dx, dy, dz, inner_dt, T, kappa, rhoC, S, flag, dTr, counters, td,
+                                  ih2, irhoC);
+}
+
+// All substeps of a small grid in one launch of one thread-block cluster of
+// FDM_CLUSTER blocks (one per SM), block b holding the cells
+// [b * blockDim, (b + 1) * blockDim) (one cell per thread).  Substeps are
+// separated by a device-scope fence and the cluster's hardware barrier,
+// which every thread of every block reaches the same number of times (the
+// loop bound is a launch argument).  Substep s reads src, writes dst as the
+// per-substep launches do (rec: substep s writes rec + s * ncells);
+// temperatures are read through L2.  Results are those of nsub launches of
+// k_fdm_substep.
+constexpr int FDM_CLUSTER = 8;
+template <bool FAST>
+__global__ void __launch_bounds__(1024, 1)
+    k_fdm_cluster(long nx, long ny, long nz, double dx, double dy, double dz, double inner_dt, unsigned nsub,
+                  double *__restrict__ T0, double *__restrict__ T1, double *__restrict__ rec,
+                  const double *__restrict__ kappa, const double *__restrict__ rhoC, const double *__restrict__ S,
+                  const signed char *__restrict__ flag, double *__restrict__ dT, U128 *__restrict__ acc,
+                  unsigned long long *__restrict__ counters, TdynTables td, double3 ih2,
+                  const double *__restrict__ irhoC) {
+  const long ntotal = nx * ny * nz;
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool mine = r < ntotal;
+  double dTr = 0.0;
+  if (mine) {
+    U128 a = acc[r];
+    dTr = from_fixed(a);
+    dT[r] = dTr;
+    acc[r] = U128{0ull, 0ull};
+  }
+  const double *src = T0;
+  double *dst = T1;
+  for (unsigned s = 0; s < nsub; ++s) {
+    if (rec) dst = rec + (size_t)s * (size_t)ntotal;
+    if (mine)
+      dst[r] = fdm_cell<FAST, true>(r, nx, ny, nz, dx, dy, dz, inner_dt, src, kappa, rhoC, S, flag, dTr, counters,
+                                    td, ih2, irhoC);
+    __threadfence();
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    double *next = rec ? nullptr : const_cast<double *>(src);
+    src = dst;
+    if (!rec) dst = next;
+  }
 }
 
 // Exact sum of the grid temperatures (EPH_FDM::get_T_total, eph_fdm.h:189-196).
