@@ -148,6 +148,12 @@ FORCES_DRAM_OVER_ALGORITHMIC = (3.47e9 + 0.18816e9) / forces_bytes(2048000, 8601
 # FP64-pipe utilisation of the two sweeps (ncu, profiles/sweeps_fcc_131k.md)
 DENSITY_FP64_PIPE = 0.676
 FORCES_FP64_PIPE = 0.874
+# FP64 thread instructions per in-cutoff pair (DADD + DMUL + DFMA, predicated
+# on; ncu on the 131,072-atom case, per-atom work included) and the GB300's
+# FP64 issue rate: 2 thread instructions per SM per clock at 2.07 GHz
+DENSITY_FP64_PER_PAIR = 31.34
+FORCES_FP64_PER_PAIR = 15.14
+FP64_PEAK = 2 * 152 * 2.07e9
 
 
 def ranks_reduce(x, op, device):
@@ -701,13 +707,16 @@ def main():
     value = job_value(world, n, args.steps, res["ms"])
     hbm, peak_src = peaks()
 
-    def roofline(phase, kernel, nbytes, dram_ratio, fp64_pipe):
+    def roofline(phase, kernel, nbytes, dram_ratio, fp64_pipe, fp64_per_pair):
         ms_p, nl_p = res["phases"][phase]
         t_launch = ms_p / max(nl_p, 1) / 1000.0
         achieved = nbytes / t_launch / 1e9
+        fp64 = fp64_per_pair * res["n_pairs"] / t_launch
         return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_source": peak_src, "traffic": dram_ratio * nbytes,
                 "algorithmic_bytes": nbytes, "launch_ms": t_launch * 1000.0, "fp64_pipe_frac_ncu": fp64_pipe,
+                "fp64": {"achieved": fp64, "peak": FP64_PEAK, "unit": "FP64 thread-instructions/s",
+                         "frac": fp64 / FP64_PEAK, "per_pair": fp64_per_pair},
                 "note": "bound by FP64 issue, not HBM: GB300 issues ~0.6e12 FP64 thread-instructions/s "
                         "(2 per SM per clock); ncu puts this kernel's FP64 pipe at %.0f%%" % (100 * fp64_pipe)}
     line = {
@@ -720,9 +729,9 @@ def main():
                    "mode": "fast", "xi": "device Philox4x32-10"},
         "gpu_launches": res["launches"],
         "roofline": roofline("density", "k_density", density_bytes(n, res["n_pairs"]),
-                             DENSITY_DRAM_OVER_ALGORITHMIC, DENSITY_FP64_PIPE),
+                             DENSITY_DRAM_OVER_ALGORITHMIC, DENSITY_FP64_PIPE, DENSITY_FP64_PER_PAIR),
         "roofline_forces": roofline("forces", "k_forces_m", forces_bytes(n, res["n_pairs"]),
-                                    FORCES_DRAM_OVER_ALGORITHMIC, FORCES_FP64_PIPE),
+                                    FORCES_DRAM_OVER_ALGORITHMIC, FORCES_FP64_PIPE, FORCES_FP64_PER_PAIR),
         "phases_ms": {k: round(v[0], 3) for k, v in res["phases"].items()},
         "clocks": res["clocks"],
         "pairs_per_atom": res["n_pairs"] / n,
