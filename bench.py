@@ -725,7 +725,7 @@ def main():
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "atoms_per_gpu": n, "grid": list(GRID), "dt_ps": DT,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 52 // 2 ** 20),
+                   "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 36 // 2 ** 20),
                    "mode": "fast", "xi": "device Philox4x32-10"},
         "gpu_launches": res["launches"],
         "roofline": roofline("density", "k_density", density_bytes(n, res["n_pairs"]),

@@ -24,6 +24,14 @@ using namespace ephgb;
 namespace ephgb {
 namespace ctxi {
 
+// pg rows (rho(r^2) per pair) exist for EXACT mode and for several elements;
+// FAST mode with one element reads neither (16 B per pair saved)
+cudaError_t alloc_pg(eph_ctx *c) {
+  if (c->mode == EPH_MODE_EXACT || c->multi) return c->pg.alloc((size_t)c->kcap * (size_t)c->n);
+  c->pg.free();
+  return cudaSuccess;
+}
+
 int fail(eph_ctx *c, int code, const std::string &msg) {
   if (c) c->err = msg;
   return code;
@@ -753,7 +761,7 @@ int eph_set_capacity(eph_ctx *c, int bin_capacity, int pair_capacity) {
     CUDA_TRY(c, c->bins.alloc((size_t)c->nbins * c->bcap));
     CUDA_TRY(c, c->pj.alloc((size_t)c->kcap * c->n));
     CUDA_TRY(c, c->pe.alloc((size_t)c->kcap * c->n));
-    CUDA_TRY(c, c->pg.alloc((size_t)c->kcap * c->n));
+    CUDA_TRY(c, alloc_pg(c));
   }
   return EPH_OK;
 }
@@ -889,7 +897,7 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
     CUDA_TRY(c, c->bins.alloc((size_t)c->nbins * c->bcap));
     CUDA_TRY(c, c->pj.alloc((size_t)c->kcap * N));
     CUDA_TRY(c, c->pe.alloc((size_t)c->kcap * N));
-    CUDA_TRY(c, c->pg.alloc((size_t)c->kcap * N));
+    CUDA_TRY(c, alloc_pg(c));
   }
   if ((r0 = eam_resize(c))) return r0;
   if (!c->tmap.p) CUDA_TRY(c, c->tmap.alloc(65));

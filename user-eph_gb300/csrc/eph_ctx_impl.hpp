@@ -141,6 +141,7 @@ namespace ephgb {
 namespace ctxi {
 
 int fail(eph_ctx *c, int code, const std::string &msg);
+cudaError_t alloc_pg(eph_ctx *c);
 int check_device(eph_ctx *c);
 int require_atoms(eph_ctx *c);
 int upload_tables(eph_ctx *c);

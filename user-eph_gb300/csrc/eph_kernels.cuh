@@ -700,7 +700,8 @@ __global__ void __launch_bounds__(128) k_forces(StepParams P, const int *__restr
       const D4 Aj = A[j];
       if (!pos_double(Aj.x)) continue;
       const D4 e = pe[slot];
-      const double2 g = pg[slot];
+      // FAST mode with one element has no pg rows (the buffer is not allocated)
+      const double2 g = (FAST && !MULTI) ? make_double2(0.0, 0.0) : pg[slot];
       const D4 Bj = Bw[j];
       if (FAST) {
         const double a = Ai.y * e.w;                  // alpha_i/rho_i * rho_j(r^2)/r^2
