@@ -190,6 +190,8 @@ def run_gpu(args, rank, world):
         words, atoms = make_system(wd)
         n = atoms.n
         fix = ephgb.FixEPH(words, atoms, dt=DT, mode=ephgb.MODE_FAST, device=dev)
+        if args.list_skin is not None:
+            fix.set_list_skin(args.list_skin)
         stream = torch.cuda.current_stream()
         fix.set_stream(stream.cuda_stream)
         # ---------------------------------------------- device-resident value
@@ -197,6 +199,7 @@ def run_gpu(args, rank, world):
         fix.synchronize()
         if world > 1:
             torch.distributed.barrier()
+        builds0 = fix.counter("build")
         fix.set_profiling(True)
         clocks = ClockSampler(dev)
         clocks.start()
@@ -217,7 +220,7 @@ def run_gpu(args, rank, world):
         fix.set_profiling(False)
         n_pairs = fix.pair_count()
         out.update(ms=ms, phases=phases, launches=launches, n_pairs=n_pairs, clocks=clock, n=n,
-                   rebuilds=fix.counter("wrap"))
+                   rebuilds=fix.counter("wrap"), list_builds=fix.counter("build") - builds0, list_skin=fix.list_skin())
         if args.no_e2e:
             return out
         # ------------------------------------------------ end to end (host)
@@ -662,6 +665,8 @@ def main():
     ap.add_argument("--fit-iters", type=int, default=60)
     ap.add_argument("--cells", type=int, default=CELLS, help="fcc cells per edge (profiling cases)")
     ap.add_argument("--grid", type=int, default=GRID[0], help="FDM cells per edge (profiling cases)")
+    ap.add_argument("--list-skin", type=float, default=None,
+                    help="skin of the kept candidate lists in A (0: bin search every step; default: the library's)")
     args = ap.parse_args()
     if args.cells != CELLS or args.grid != GRID[0]:
         CELLS, GRID = args.cells, (args.grid,) * 3
@@ -736,6 +741,8 @@ def main():
         "clocks": res["clocks"],
         "pairs_per_atom": res["n_pairs"] / n,
         "wraps": res["rebuilds"],
+        "list_skin_A": res["list_skin"][0] if res["list_skin"][1] else 0.0,
+        "list_builds": res["list_builds"],  # in the timed steps
     }
     if "t_e2e" in res:
         line["e2e"] = {"value": world * n * res["e2e_steps"] / res["t_e2e"], "unit": METRIC,

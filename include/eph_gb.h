@@ -182,6 +182,21 @@ int eph_get_threads_per_atom(eph_ctx *ctx, int *tpa);
  * fastest; *chosen gets it (may be NULL). */
 int eph_autotune(eph_ctx *ctx, int *chosen);
 
+/* Skin s of the kept candidate lists (Angstrom; default 0.3, used up to 2^20
+ * atoms, where it pays; a skin set here applies at any size, 0 turns the
+ * lists off).  The reference takes its pairs from the engine's Verlet list
+ * (fix_eph.cpp:273-275: a full list with cutoff r_cutoff, padded by the
+ * engine's skin and rebuilt when an atom moved half of it); here the list is
+ * the context's own.  In FAST mode (model 4, the one-lane density sweep) the
+ * candidates within r_cutoff + s are found by a bin search on build steps
+ * only; in between, up to 32 atoms that moved more than s/2 (and the atoms
+ * near them) search afresh every step, and more of them make the step a
+ * build step (counter 2 counts the builds).  Pairs and results are those of
+ * a search every step, up to the order of the sums.  *active reports whether
+ * the context uses it (either pointer may be NULL). */
+int eph_set_list_skin(eph_ctx *ctx, double skin);
+int eph_get_list_skin(eph_ctx *ctx, double *skin, int *active);
+
 /* Timing of the step's phases with CUDA events on the context's stream
  * (no reference counterpart; the reference relies on gprof, lib/Makefile:25-28).
  * Phases: */

@@ -1,0 +1,164 @@
+"""Kept candidate lists (FAST mode, model 4, the one-lane density sweep): the
+candidates within r_cutoff + s are searched on build steps only; atoms that
+moved more than s/2 since the build, and the atoms near them, search afresh
+every step, and more than 32 moved atoms make a build step.  The pairs, and
+so the results, must be those of a search every step (up to the order of
+the sums): checked against the oracle and against the same context with
+reuse switched off, with a fast primary knock-on atom (moved atoms, wraps
+across the box faces) and with hot atoms (builds forced by many moved
+atoms); runs and graph replays stay bit-identical."""
+import numpy as np
+import pytest
+
+import ephgb
+from ephgb import workloads as W
+from helpers import n_in_group, rel_err, scenario, xi_rows
+from oracle.bindings import OracleFix
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+ATOM_KEYS = ("rho", "w", "f_eph", "f_rng", "f", "x", "v", "array")
+
+
+def _fix(words, at, dt, skin=None):
+    fix = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_FAST)
+    fix.set_threads_per_atom(1)
+    if skin is not None:
+        fix.set_list_skin(skin)
+    return fix
+
+
+def _against_oracle(words, at, dt, steps, seed=5):
+    gpu = _fix(words, at, dt)
+    assert gpu.list_skin() == (0.3, True)
+    ref = OracleFix(words, at, dt)
+    ng = n_in_group(at)
+    for s in range(steps):
+        stream = W.gaussian_stream(ng, seed, s)
+        gpu.step(1, xi=xi_rows(at, stream))
+        ref.step(stream)
+        for k in ATOM_KEYS:
+            assert rel_err(gpu.get(k), ref.get(k)) <= TOL, (s, k, rel_err(gpu.get(k), ref.get(k)))
+        assert rel_err(gpu.get("T"), ref.get("T")) <= TOL, s
+    return gpu
+
+
+def test_pka_against_oracle(built, beta_file):
+    """A 2 keV knock-on atom (0.2 A per step) in 6^3 cells for 40 steps: it
+    is a moved atom from the second step on and crosses box faces."""
+    words, at, dt = scenario("pka", beta_file)
+    gpu = _against_oracle(words, at, dt, 40)
+    builds = gpu.counter("build")
+    assert 1 <= builds < 40, builds
+
+
+def test_hot_atoms_force_builds(built, beta_file):
+    """Velocities of a few thousand kelvin: more than 32 atoms pass s/2
+    within a few steps, so builds recur."""
+    at = W.fcc_lattice(5, seed=31)
+    at.v *= 4.0
+    words = W.fix_args(beta_file, grid=(5, 5, 5))
+    gpu = _against_oracle(words, at, 0.001, 30)
+    builds = gpu.counter("build")
+    assert 3 <= builds < 30, builds
+
+
+def test_group_and_two_elements(built, beta_file, beta_file_2el):
+    for name in ("group", "two_elements"):
+        words, at, dt = scenario(name, beta_file, beta_file_2el)
+        at.v *= 2.0
+        _against_oracle(words, at, dt, 20)
+
+
+@pytest.fixture(scope="module")
+def cascade(tmp_path_factory):
+    import os
+
+    wd = str(tmp_path_factory.mktemp("list"))
+    bf = W.write_beta_file(os.path.join(wd, "synth.beta"))
+    at = W.fcc_lattice(16, seed=41)
+    W.add_pka(at, 10000.0, seed=42)
+    words = W.fix_args(bf, seed=43, grid=(8, 8, 8))
+    return words, at
+
+
+def test_same_as_search_every_step(built, cascade):
+    """16,384 atoms, a 10 keV knock-on atom, 60 steps with the device RNG:
+    kept lists against a bin search every step."""
+    words, at = cascade
+    a = _fix(words, at, 0.0005)
+    b = _fix(words, at, 0.0005, skin=0.0)
+    assert a.list_skin()[1] and not b.list_skin()[1]
+    for _ in range(6):
+        a.step(10)
+        b.step(10)
+        for k in ("rho", "w", "f_eph", "f_rng", "x", "v", "T"):
+            assert rel_err(a.get(k), b.get(k)) <= TOL, (k, rel_err(a.get(k), b.get(k)))
+    assert a.pair_count() == b.pair_count()
+    assert 1 <= a.counter("build") < 60
+    assert a.counter("wrap") == b.counter("wrap")
+
+
+def test_run_to_run_and_graph(built, cascade):
+    """Direct steps and graph replays give the same bits (the build decisions
+    live on the device)."""
+    import torch
+
+    words, at = cascade
+    a = _fix(words, at, 0.0005)
+    g = _fix(words, at, 0.0005)
+    stream = torch.cuda.Stream()
+    g.set_stream(stream.cuda_stream)
+    g.set_graph(True)
+    a.step(25)
+    g.step(25)
+    g.synchronize()
+    for k in ("x", "v", "f", "f_eph", "f_rng", "rho", "T"):
+        assert np.array_equal(a.get(k), g.get(k)), k
+    assert a.counter("build") == g.counter("build") < 25
+
+
+def test_hooks_with_host_positions(built, cascade):
+    """The hooks driven as an engine does, positions, velocities and forces
+    copied in and out every step (no wraps: the engine does those): kept
+    lists against a bin search every step."""
+    words, at = cascade
+    out = []
+    for skin in (None, 0.0):
+        h = _fix(words, at, 0.0005, skin=skin)
+        x, v = at.x.copy(), at.v.copy()
+        f = np.zeros_like(x)
+        for s in range(25):
+            h.put("x", x)
+            h.put("v", v)
+            h.put("f", f)
+            h.set_timestep(s + 1)
+            h.initial_integrate()
+            h.put("f", np.zeros_like(x))
+            h.post_force()
+            h.final_integrate()
+            h.end_of_step()
+            x, v, f = h.get("x"), h.get("v"), h.get("f")
+        out.append(({k: h.get(k) for k in ("x", "v", "f", "f_eph", "f_rng", "rho", "T")}, h.counter("build")))
+    (a, builds), (b, _) = out
+    for k in a:
+        assert rel_err(a[k], b[k]) <= TOL, (k, rel_err(a[k], b[k]))
+    assert 1 <= builds < 25
+
+
+def test_when_reuse_is_off(built, beta_file):
+    words, at, dt = scenario("c1_small", beta_file)
+    assert not ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_EXACT).list_skin()[1]
+    fix = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_FAST)
+    fix.set_threads_per_atom(4)
+    assert not fix.list_skin()[1]
+    fix.set_threads_per_atom(1)
+    assert fix.list_skin()[1]
+    fix.set_list_skin(3.0)  # 17.6 A box: fewer than three bins of r_cutoff + 3 A
+    assert fix.list_skin() == (3.0, False)
+    fix.step(2)
+    fix.set_list_skin(0.4)
+    assert fix.list_skin() == (0.4, True)
+    fix.step(2)
+    with pytest.raises(ephgb.EphError):
+        fix.set_list_skin(-1.0)

@@ -1187,6 +1187,11 @@ int eph_adjoint_create(eph_ctx *c, int checkpoint_every, eph_adjoint **out) {
   if (c->eam) return ctxi::fail(c, EPH_ERR_UNSUPPORTED_MODEL, "the adjoint does not differentiate the EAM pair force");
   if (c->beta.n_elements * c->beta.n_beta > 65536)
     return ctxi::fail(c, EPH_ERR_CAPACITY, "alpha tables too large for the adjoint's accumulators");
+  // recomputed segments must repeat the recorded steps bit for bit: every
+  // step searches the bins (a kept candidate list would carry state across
+  // checkpoints)
+  c->list_block = true;
+  if (int rl = ctxi::configure_list(c)) return rl;
   eph_adjoint *a = new (std::nothrow) eph_adjoint();
   if (!a) return EPH_ERR_ARG;
   *out = a;

@@ -221,6 +221,16 @@ void launch_density_f(eph_ctx *c, int xi_mode) {
       return;
     }
   }
+  if constexpr (FAST && FUSE) {
+    if (c->reuse) {
+      k_density_list<MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+          c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode,
+          c->T0.p, c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p,
+          c->Te_i.p, c->wrapflag.p, c->d_err.p, c->counters.p, c->v.p, c->Mm.p, c->G.p, c->cl.p, c->cl_n.p,
+          c->state.p, c->rb.p, c->flist.p);
+      return;
+    }
+  }
   k_density<FAST, MULTI, FUSE><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
       c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p,
       c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,
@@ -271,6 +281,104 @@ void launch_forces_t(eph_ctx *c) {
 // 16,384 atoms 282 / 280 / 284; above ~65,000 atoms one lane)
 int auto_tpa(long n) { return n <= 6144 ? 8 : (n <= 65536 ? 4 : 1); }
 
+// Bins of edge >= r (1 + 5e-5), at least three per axis; 0 or an error
+int set_bin_geometry(eph_ctx *c, double r) {
+  const double edge = r * (1.0 + 5e-5);
+  int nb[3];
+  for (int k = 0; k < 3; ++k) {
+    nb[k] = (int)(c->prd[k] / edge);
+    if (nb[k] < 3) return fail(c, EPH_ERR_ARG, "box edge shorter than three bin edges: too small for minimum-image bins");
+  }
+  for (int k = 0; k < 3; ++k) {
+    c->P.nb[k] = nb[k];
+    c->P.w[k] = c->prd[k] / nb[k];
+    c->P.inv_w[k] = 1.0 / c->P.w[k];
+    c->P.wf[k] = (float)c->P.w[k];
+  }
+  c->nbins = nb[0] * nb[1] * nb[2];
+  return EPH_OK;
+}
+
+// a bin's capacity from the number density: ~density * w^3 atoms
+int auto_bcap(const eph_ctx *c) {
+  const double dens = c->n / (c->prd[0] * c->prd[1] * c->prd[2]);
+  const double per_bin = dens * c->P.w[0] * c->P.w[1] * c->P.w[2];
+  return ((int)std::ceil(2.0 * per_bin + 16.0) + 7) / 8 * 8;
+}
+
+// Kept candidate lists: FAST mode, model 4 with friction, the one-lane
+// density sweep (one lane per atom, or 16,384 atoms and more), no pair force
+// of the engine (it needs bins every step) and no adjoint.  By default up to
+// 2^20 atoms: the lists save the bin search, which the density sweep's FP64
+// pass hides less well in small systems (measured on GB300 with a 0.3 A skin,
+// step time: 131,072 atoms -9 %, 500,000 atoms -2 %, 2,048,000 atoms +0.2 %,
+// where both sweeps already run at the FP64 issue limit); a skin set through
+// eph_set_list_skin applies at any size.
+bool want_list(const eph_ctx *c) {
+  if (c->mode != EPH_MODE_FAST || c->lskin <= 0.0 || c->list_block || c->eam || c->n <= 0 ||
+      !(c->tpa == 1 || c->n >= 16384) || !fused_friction(c) || !(c->lskin_user || c->n <= (1 << 20)))
+    return false;
+  for (int k = 0; k < 3; ++k)
+    if ((int)(c->prd[k] / ((c->beta.r_cutoff + c->lskin) * (1.0 + 5e-5))) < 3) return false;
+  return true;
+}
+
+void drop_list(eph_ctx *c) {
+  c->reuse = false;
+  c->lcap = 0;
+  c->cl.free();
+  c->cl_n.free();
+  c->state.free();
+  c->rb.free();
+  c->flist.free();
+  c->xref.free();
+}
+
+int configure_list(eph_ctx *c) {
+  const bool want = want_list(c);
+  if (!want && !c->reuse) return EPH_OK;
+  const double rc = c->beta.r_cutoff;
+  const int nbins_was = c->nbins, bcap_was = c->bcap;
+  int r = set_bin_geometry(c, want ? rc + c->lskin : rc);
+  if (r) return r;
+  if (!c->bcap_user) c->bcap = auto_bcap(c);
+  c->P.bcap = c->bcap;
+  if (c->nbins != nbins_was || c->bcap != bcap_was || !c->bins.p) {
+    CUDA_TRY(c, c->bins.alloc((size_t)c->nbins * c->bcap));
+    CUDA_TRY(c, c->bin_count.alloc((size_t)c->nbins));
+    CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
+  }
+  c->buf_gen += 1;
+  drop_graph(c);
+  if (!want) {
+    drop_list(c);
+    return EPH_OK;
+  }
+  const size_t N = (size_t)c->n;
+  const double rl = rc + c->lskin, rm = rc + 0.5 * c->lskin;
+  const double dens = c->n / (c->prd[0] * c->prd[1] * c->prd[2]);
+  const int lcap = std::min(256, ((int)std::ceil(2.0 * dens * 4.18879020478639 * rl * rl * rl + 24.0) + 7) / 8 * 8);
+  if (lcap != c->lcap || c->cl.n != (size_t)lcap * N) CUDA_TRY(c, c->cl.alloc((size_t)lcap * N));
+  c->lcap = lcap;
+  for (DevBuf<int> *b : {&c->cl_n, &c->state})
+    if (b->n != N) CUDA_TRY(c, b->alloc(N));
+  if (c->xref.n != N) CUDA_TRY(c, c->xref.alloc(N));
+  if (!c->rb.p) CUDA_TRY(c, c->rb.alloc(4));
+  if (!c->flist.p) CUDA_TRY(c, c->flist.alloc(LIST_FMAX));
+  CUDA_TRY(c, cudaMemsetAsync(c->rb.p, 0, 4 * sizeof(int), c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->rb.p, 0x01, 1, c->stream));  // rb[0] = 1: the next step builds
+  c->P.lcap = lcap;
+  c->P.rl2_band = (float)(rl * rl * (1.0 + 1e-4));
+  c->P.rmark2_band = (float)(rm * rm * (1.0 + 1e-4));
+  c->P.lslow2 = 0.25 * c->lskin * c->lskin;
+  for (int k = 0; k < 3; ++k) {
+    c->P.half_prd[k] = 0.5 * c->prd[k];
+    c->P.half_prdf[k] = (float)c->P.half_prd[k];
+  }
+  c->reuse = true;
+  return EPH_OK;
+}
+
 // stage 1 as its own sweep: EXACT mode (FAST mode folds it into the density sweep)
 void launch_friction_w(eph_ctx *c) {
   k_friction_w<<<nblocks(c->n), BLOCK, 0, c->stream>>>(c->P, c->mask.p, c->v.p, c->pj.p, c->pe.p, c->pg.p,
@@ -312,6 +420,30 @@ int launch_post_force(eph_ctx *c, int xi_mode) {
 int launch_bin(eph_ctx *c) {
   const int nb = nblocks(c->n);
   PhaseScope ps(c, EPH_PHASE_BIN);
+  if (c->reuse) {
+    // the engine's wrap and the displacements since the list build; a build
+    // step (decided on the device) bins and sorts as below, any other step
+    // flags the atoms near moved ones and leaves the bins as they are
+    int *rb = c->rb.p;
+    CUDA_TRY(c, cudaMemsetAsync(rb + 1, 0, sizeof(int), c->stream));
+    k_list_check<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->xref.p, c->state.p, rb,
+                                              c->flist.p, c->counters.p);
+    k_list_decide<<<1, 32, 0, c->stream>>>(rb, c->flist.p, c->counters.p);
+    k_list_mark<<<LIST_FMAX, BLOCK, 0, c->stream>>>(c->P, c->x.p, rb, c->flist.p, c->bin_count.p, c->bins.p,
+                                                    c->state.p);
+    k_zero_if<<<nblocks(c->nbins), BLOCK, 0, c->stream>>>(c->bin_count.p, c->nbins, rb + 2);
+    k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
+                                       c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 0, rb + 2,
+                                       c->xref.p);
+    if (c->bcap <= 64 && c->nbins < 32768)
+      k_bin_sort_warp<<<nblocks((long)c->nbins * 32), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p,
+                                                                              c->bins.p, rb + 2);
+    else
+      k_bin_sort<<<nblocks(c->nbins), BLOCK, 0, c->stream>>>(c->nbins, c->bcap, c->bin_count.p, c->bins.p, rb + 2);
+    ps.launched(6);
+    CUDA_TRY(c, cudaGetLastError());
+    return EPH_OK;
+  }
   ps.launched();
   CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
   k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
@@ -722,15 +854,7 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
   P.step = c->step_ctr.p;
   set_time_params(c);
   // bins: edge >= rc (1 + 5e-5), at least 3 per axis
-  for (int k = 0; k < 3; ++k) {
-    const int nb = (int)(c->prd[k] / (c->beta.r_cutoff * (1.0 + 5e-5)));
-    if (nb < 3) return fail(c, EPH_ERR_ARG, "box edge shorter than three r_cutoff: too small for minimum-image bins");
-    P.nb[k] = nb;
-    P.w[k] = c->prd[k] / nb;
-    P.inv_w[k] = 1.0 / P.w[k];
-    P.wf[k] = (float)P.w[k];
-  }
-  c->nbins = P.nb[0] * P.nb[1] * P.nb[2];
+  if ((r = set_bin_geometry(c, c->beta.r_cutoff))) return r;
   CUDA_TRY(c, cudaDeviceSynchronize());  // the set-up copies and memsets above ran on the default stream
   return EPH_OK;
 }
@@ -753,7 +877,7 @@ int eph_set_capacity(eph_ctx *c, int bin_capacity, int pair_capacity) {
   drop_graph(c);
   if (pair_capacity > KMAX) return fail(c, EPH_ERR_ARG, "pair capacity above the compiled maximum");
   c->buf_gen += 1;
-  if (bin_capacity > 0) c->bcap = bin_capacity;
+  if (bin_capacity > 0) c->bcap = bin_capacity, c->bcap_user = true;
   if (pair_capacity > 0) c->kcap = pair_capacity;
   if (c->n > 0) {
     c->P.bcap = c->bcap;
@@ -774,6 +898,34 @@ int eph_set_threads_per_atom(eph_ctx *c, int tpa) {
   c->buf_gen += 1;  // graphs captured elsewhere hold the old launch shape
   c->tpa_auto = tpa == 0;
   c->tpa = tpa == 0 ? auto_tpa(c->n) : tpa;
+  return c->n > 0 ? configure_list(c) : EPH_OK;
+}
+
+int eph_set_list_skin(eph_ctx *c, double skin) {
+  if (!c || !(skin >= 0.0)) return EPH_ERR_ARG;
+  drop_graph(c);
+  c->lskin = skin;
+  c->lskin_user = true;
+  if (c->n <= 0) return EPH_OK;
+  const bool was = c->reuse;
+  if (was) drop_list(c);  // a new radius: new bins and lists
+  int r = configure_list(c);
+  if (r) return r;
+  if (was && !c->reuse) {  // back to the cutoff's bins
+    if ((r = set_bin_geometry(c, c->beta.r_cutoff))) return r;
+    if (!c->bcap_user) c->bcap = auto_bcap(c);
+    c->P.bcap = c->bcap;
+    CUDA_TRY(c, c->bins.alloc((size_t)c->nbins * c->bcap));
+    CUDA_TRY(c, c->bin_count.alloc((size_t)c->nbins));
+    c->buf_gen += 1;
+  }
+  return EPH_OK;
+}
+
+int eph_get_list_skin(eph_ctx *c, double *skin, int *active) {
+  if (!c) return EPH_ERR_ARG;
+  if (skin) *skin = c->lskin;
+  if (active) *active = c->reuse ? 1 : 0;
   return EPH_OK;
 }
 
@@ -918,6 +1070,8 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
   CUDA_TRY(c, cudaMemcpyAsync(c->xhold.p, c->x.p, sizeof(D4) * N, cudaMemcpyDeviceToDevice, c->stream));
   // the engine wraps positions at set-up (Verlet::setup)
   CUDA_TRY(c, cudaMemsetAsync(c->wrapflag.p, 0xff, sizeof(int), c->stream));
+  // list reuse as the settings allow (may change the bins); the next step builds
+  if ((r = configure_list(c))) return r;
   CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
   k_bin<<<nblocks(n), BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
                                              c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 0);

@@ -87,6 +87,18 @@ struct eph_ctx {
   DevBuf<D4> pe;
   DevBuf<double2> pg;
   int nbins = 0, bcap = 0, kcap = 0;
+  bool bcap_user = false;  // bin capacity set by eph_set_capacity
+  // candidate-list reuse (FAST mode, one lane per atom, model 4 with
+  // friction): the list skin s (0: search the bins every step), whether it is
+  // on, and whether an adjoint keeps it off (its recomputed segments must
+  // repeat the recorded ones bit for bit)
+  double lskin = 0.3;
+  bool lskin_user = false;  // set by eph_set_list_skin: applies at any size
+  bool reuse = false, list_block = false;
+  int lcap = 0;
+  DevBuf<unsigned> cl;  // [lcap][n] candidates
+  DevBuf<int> cl_n, state, rb, flist;
+  DevBuf<D4> xref;  // positions at the last build
 
   DevBuf<D4> tab_rho_r_sq, tab_beta, tab_alpha;
 
@@ -155,6 +167,10 @@ int launch_final(eph_ctx *c);
 int launch_end_of_step(eph_ctx *c);
 // post_force in two parts: spatial binning (and the wrap), then the sweeps
 int launch_bin(eph_ctx *c);
+// candidate-list reuse on or off as the context's settings allow (bins,
+// list buffers), and a build requested for the next step; drop_list turns it off
+int configure_list(eph_ctx *c);
+void drop_list(eph_ctx *c);
 int launch_pair_sweeps(eph_ctx *c, int xi_mode);
 // the engine's pair force for this step into f (plus the external force)
 int launch_eam(eph_ctx *c);

@@ -27,6 +27,7 @@ constexpr int CAND_SMEM = 48;  // candidate rows of one atom kept in shared memo
 constexpr unsigned IDX_BITS = 27;
 constexpr unsigned IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr unsigned CODE_NOSHIFT = 13;  // (0,0,0) image of the 3x3x3 code
+constexpr int LIST_FMAX = 32;          // moved atoms handled between two list builds (one warp)
 
 enum : unsigned {
   ERR_BIN_OVERFLOW = 1u,
@@ -52,6 +53,15 @@ struct StepParams {
   double inv_w[3], w[3];
   float wf[3];
   int bcap, kcap;
+  // candidate-list reuse (FAST mode, one lane per atom): the candidates within
+  // r_list = r_cutoff + s stay complete for every pair of atoms that moved
+  // less than s/2 since the list was built (bins then have edge >= r_list)
+  float rl2_band;     // r_list^2 (1 + 1e-4): candidates kept in the list
+  float rmark2_band;  // (r_cutoff + s/2)^2 (1 + 1e-4): atoms this close to a moved atom search afresh
+  double lslow2;      // (s/2)^2: squared displacement from which an atom counts as moved
+  double half_prd[3];
+  float half_prdf[3];
+  int lcap;           // rows of the candidate list
   // splines: tables of element e start at e * n_knots
   const D4 *tab_rho_r_sq;
   const D4 *tab_beta;

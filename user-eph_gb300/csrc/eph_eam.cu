@@ -330,6 +330,7 @@ int eph_set_pair_eam(eph_ctx *c, const char *path, int ntypes, const char *const
     d->map[t] = m;
   }
   ctxi::eam_free(c);
+  ctxi::drop_list(c);  // the pair force needs this step's bins every step
   c->eam = d;
   int r;
   CUDA_TRY(c, cudaSetDevice(c->device));

@@ -85,36 +85,46 @@ __global__ void k_final_integrate(StepParams P, D4 *__restrict__ v, const D4 *__
 
 // ------------------------------------------------------------------ binning
 
-// Wrap positions into [lo, hi) when the engine rebuilds (LAMMPS Domain::pbc
-// for an orthogonal box), then drop every atom into its spatial bin.  A bin
-// edge is at least the cutoff, so all pairs inside the cutoff are found in
-// the 27 bins around an atom.  Bins keep unwrapped coordinates: an atom that
-// drifted up to one bin outside the box carries a wrap code and the offset
-// from its own (unwrapped) bin corner.
+// LAMMPS Domain::pbc for an orthogonal box: a position into [lo, hi)
+__device__ __forceinline__ void wrap_into_box(const StepParams &P, D4 &xi) {
+  double *c[3] = {&xi.x, &xi.y, &xi.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double q = *c[k];
+    if (q < P.lo[k]) q += P.prd[k];
+    if (q >= P.hi[k]) {
+      q -= P.prd[k];
+      q = q > P.lo[k] ? q : P.lo[k];
+    }
+    *c[k] = q;
+  }
+}
+
+// Wrap positions into [lo, hi) when the engine rebuilds, then drop every
+// atom into its spatial bin.  A bin edge is at least the cutoff (with list
+// reuse: the list radius), so all pairs inside it are found in the 27 bins
+// around an atom.  Bins keep unwrapped coordinates: an atom that drifted up
+// to one bin outside the box carries a wrap code and the offset from its own
+// (unwrapped) bin corner.
+// With a gate (candidate-list reuse): nothing unless *gate (a build step),
+// no wrap (k_list_check did it), and the positions are kept in xref.
 __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, const int *__restrict__ wrapflag,
                       int *__restrict__ bin_count, BinEntry *__restrict__ bins, int4 *__restrict__ atom_bin,
                       float4 *__restrict__ atom_off, unsigned *__restrict__ err,
-                      unsigned long long *__restrict__ counters, int bump_step) {
+                      unsigned long long *__restrict__ counters, int bump_step, const int *__restrict__ gate = nullptr,
+                      D4 *__restrict__ xref = nullptr) {
+  if (gate && !*gate) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0 && bump_step) *P.step += 1ull;  // read by the density sweep that follows
   if (i >= P.n) return;
   D4 xi = x[i];
-  if (*wrapflag) {
-    double *c[3] = {&xi.x, &xi.y, &xi.z};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      double q = *c[k];
-      if (q < P.lo[k]) q += P.prd[k];
-      if (q >= P.hi[k]) {
-        q -= P.prd[k];
-        q = q > P.lo[k] ? q : P.lo[k];
-      }
-      *c[k] = q;
-    }
+  if (!gate && *wrapflag) {
+    wrap_into_box(P, xi);
     x[i] = xi;
     xhold[i] = xi;
     if (i == 0) atomicAdd(&counters[CNT_WRAP], 1ull);
   }
+  if (xref) xref[i] = xi;
   const double p[3] = {xi.x, xi.y, xi.z};
   int B[3], t[3], wc[3];
   float o[3];
@@ -155,12 +165,15 @@ __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, 
 // through cset (FAST: in bin order; EXACT: kept in ascending neighbour index
 // by insertion) while nc < cap.  Contains a warp-wide max: every lane of the
 // warp calls it the same number of times (look = false for a lane with
-// nothing to search).
-template <bool FAST, class Get, class Set>
+// nothing to search).  r2band is the FP32 threshold (the cutoff's, or the
+// candidate list's); with SKIP, entries of atoms flagged as moved (skip[j] &
+// 2) are left out.
+template <bool FAST, bool SKIP = false, class Get, class Set>
 __device__ __forceinline__ void bin_candidates(const StepParams &P, int i, bool look, int4 Bi, float4 oi, int dx,
                                                int dy, int dz, const int *__restrict__ bin_count,
                                                const BinEntry *__restrict__ bins, unsigned *__restrict__ err,
-                                               int &nc, int cap, Get cget, Set cset) {
+                                               int &nc, int cap, Get cget, Set cset, float r2band,
+                                               const int *__restrict__ skip = nullptr, float r2lo = -1.f) {
   const int Tz = Bi.z + dz, tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
   const int kz = Tz < 0 ? -1 : (Tz >= P.nb[2] ? 1 : 0);
   const float bz = (float)dz * P.wf[2] - oi.z;
@@ -184,7 +197,7 @@ __device__ __forceinline__ void bin_candidates(const StepParams &P, int i, bool 
       const unsigned j = b.idx & IDX_MASK;
       const float ex = bx + b.ox, ey = by + b.oy, ez = bz + b.oz;
       const float r2 = ex * ex + ey * ey + ez * ez;
-      if (j != (unsigned)i && r2 < P.rc2_band) {
+      if (j != (unsigned)i && r2 < r2band && r2 >= r2lo && !(SKIP && (skip[j] & 2))) {
         const unsigned wc = b.idx >> IDX_BITS;
         const int mx = kx - ((int)(wc % 3u) - 1), my = ky - ((int)((wc / 3u) % 3u) - 1),
                   mz = kz - ((int)(wc / 9u) - 1);
@@ -211,17 +224,21 @@ __device__ __forceinline__ void bin_candidates(const StepParams &P, int i, bool 
 }
 
 // Pass 1 of the density sweep for atom i: the candidates of the 27 bins
-// around its own (at most P.kcap).  Returns their number.
-template <bool FAST, class Get, class Set>
+// around its own within the FP32 thresholds r2lo <= r^2 < r2band, appended
+// after the first nc0 (at most cap in all).  Returns their number.
+template <bool FAST, bool SKIP = false, class Get, class Set>
 __device__ __forceinline__ int collect_candidates(const StepParams &P, int i, bool active, int4 Bi, float4 oi,
                                                   const int *__restrict__ bin_count,
                                                   const BinEntry *__restrict__ bins, unsigned *__restrict__ err,
-                                                  Get cget, Set cset) {
-  int nc = 0;
+                                                  Get cget, Set cset, float r2band, int cap,
+                                                  const int *__restrict__ skip = nullptr, float r2lo = -1.f,
+                                                  int nc0 = 0) {
+  int nc = nc0;
   for (int dz = -1; dz <= 1; ++dz)
     for (int dy = -1; dy <= 1; ++dy)
       for (int dx = -1; dx <= 1; ++dx)
-        bin_candidates<FAST>(P, i, active, Bi, oi, dx, dy, dz, bin_count, bins, err, nc, P.kcap, cget, cset);
+        bin_candidates<FAST, SKIP>(P, i, active, Bi, oi, dx, dy, dz, bin_count, bins, err, nc, cap, cget, cset,
+                                   r2band, skip, r2lo);
   return nc;
 }
 
@@ -229,7 +246,9 @@ __device__ __forceinline__ int collect_candidates(const StepParams &P, int i, bo
 // holds entries l and l + 32, each entry's place is the number of entries
 // with a smaller atom index (indices are distinct), found by broadcasting
 // every entry's key across the warp; all loads happen before any store.
-__global__ void k_bin_sort_warp(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins) {
+__global__ void k_bin_sort_warp(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins,
+                                const int *__restrict__ gate = nullptr) {
+  if (gate && !*gate) return;
   const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (w >= nbins) return;  // whole warps leave together
@@ -254,7 +273,9 @@ __global__ void k_bin_sort_warp(int nbins, int bcap, const int *__restrict__ bin
 
 // Sort every bin's entries by atom index (one thread per bin, a handful of
 // entries each), so the candidate order below is fixed run to run.
-__global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins) {
+__global__ void k_bin_sort(int nbins, int bcap, const int *__restrict__ bin_count, BinEntry *__restrict__ bins,
+                           const int *__restrict__ gate = nullptr) {
+  if (gate && !*gate) return;
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbins) return;
   int cnt = bin_count[b];
@@ -450,7 +471,7 @@ __global__ void __launch_bounds__(128) k_density(
       Bi = atom_bin[i];
       oi = atom_off[i];
     }
-    nc = collect_candidates<FAST>(P, i, active, Bi, oi, bin_count, bins, err, cget, cset);
+    nc = collect_candidates<FAST>(P, i, active, Bi, oi, bin_count, bins, err, cget, cset, P.rc2_band, P.kcap);
   }
   __syncwarp();
   // pass 2: exact FP64 test, density and pair cache, in lockstep
@@ -523,7 +544,7 @@ __global__ void __launch_bounds__(128) k_density_tpa(
       const bool look = active && b < 27;
       const int bb = b < 27 ? b : 13;
       bin_candidates<true>(P, i, look, Bi, oi, bb % 3 - 1, (bb / 3) % 3 - 1, bb / 9 - 1, bin_count, bins, err, nc,
-                           CAND_SMEM, cget, cset);
+                           CAND_SMEM, cget, cset, P.rc2_band);
     }
   }
   __syncwarp();
@@ -587,6 +608,305 @@ __global__ void __launch_bounds__(128) k_density_tpa(
   density_epilogue<true, FUSE_W>(P, i, active, xi, ei, rho, ns < P.kcap ? ns : P.kcap, mxx, mxy, mxz, myy, myz, mzz,
                                  Sx, Sy, Sz, xi_given, xi_mode, T_e, nshort, A, Bw, rho_out, beta_out, cell, Te_i,
                                  err, counters, v, Mm, G);
+}
+
+// ------------------------------------------------ candidate-list reuse
+
+// FAST mode, one lane per atom.  The candidates of atom i within r_list =
+// r_cutoff + s (s the list skin) are kept from a build step on: while atoms
+// i and j both moved less than s/2 since the build, |x_i - x_j| < r_cutoff
+// implies that j is in i's list.  Atoms that moved farther ("moved", at most
+// LIST_FMAX of them) are handled every step instead: they and every atom
+// within r_cutoff + s/2 of one of them (from the bins of the build) search
+// the bins afresh, leave moved atoms' bin entries out and take the moved
+// atoms as extra candidates.  More moved atoms, or a request from the host,
+// make the step a build step.  Decisions live on the device (rb[0] build
+// requested, rb[1] moved atoms this step, rb[2] this step builds), so a
+// captured step replays them.  Lists hold atom indices; the periodic image of
+// a pair is the minimum image of the current positions, decided in FP32 (the
+// box is at least three list radii wide, so it is the image within the
+// cutoff), and e = (x_j +- L) - x_i rounds as the engine's ghost atoms give
+// it.
+
+__device__ __forceinline__ double min_image(double d, double L, double h) {
+  return d > h ? d - L : (d < -h ? d + L : d);
+}
+
+// v truncated to float by integer work on its bits (the conversion
+// instruction would run on the FP64 pipe): exponent rebased, top 23 mantissa
+// bits; |v| < 2^-126 gives 0.  Good to 2^-23 relative, for the image test.
+__device__ __forceinline__ float float_bits(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned hi = (unsigned)(b >> 32);
+  int e = (int)((hi >> 20) & 0x7ffu);
+  if (e < 897) return 0.f;
+  e = e > 1150 ? 1150 : e;
+  return __uint_as_float((hi & 0x80000000u) | ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) |
+                         ((unsigned)b >> 29));
+}
+
+// The 3x3x3 image code of x_j seen from x_i: the image of x_j within half a
+// box of x_i on every axis, decided in FP32 (the box is at least three list
+// radii wide, so a pair within the list radius is far from the threshold).
+// The pair vector then comes from density_vector, the rounding of the bin
+// search path.
+__device__ __forceinline__ unsigned image_code(const StepParams &P, float xi, float yi, float zi, const D4 &xj) {
+  const float dx = float_bits(xj.x) - xi, dy = float_bits(xj.y) - yi, dz = float_bits(xj.z) - zi;
+  const int mx = dx > P.half_prdf[0] ? -1 : (dx < -P.half_prdf[0] ? 1 : 0);
+  const int my = dy > P.half_prdf[1] ? -1 : (dy < -P.half_prdf[1] ? 1 : 0);
+  const int mz = dz > P.half_prdf[2] ? -1 : (dz < -P.half_prdf[2] ? 1 : 0);
+  return (unsigned)((mx + 1) + 3 * (my + 1) + 9 * (mz + 1));
+}
+
+// The bin and FP32 offset of a position wrapped into the box (an atom whose
+// bins entry is stale: it moved since the build)
+__device__ __forceinline__ void current_bin(const StepParams &P, const D4 &xi, int4 &B, float4 &o) {
+  const double p[3] = {xi.x, xi.y, xi.z};
+  int b[3];
+  float of[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double q = p[k] - P.lo[k];
+    q -= floor(q / P.prd[k]) * P.prd[k];
+    if (q >= P.prd[k]) q -= P.prd[k];
+    if (q < 0.0) q = 0.0;
+    int bb = (int)floor(q * P.inv_w[k]);
+    bb = bb < 0 ? 0 : (bb >= P.nb[k] ? P.nb[k] - 1 : bb);
+    b[k] = bb;
+    of[k] = (float)(q - (double)bb * P.w[k]);
+  }
+  B = make_int4(b[0], b[1], b[2], b[0] + P.nb[0] * (b[1] + P.nb[1] * b[2]));
+  o = make_float4(of[0], of[1], of[2], 0.f);
+}
+
+// First kernel of a step with list reuse: the engine's wrap (as k_bin does
+// it), then each atom's displacement since the list build; moved atoms get
+// state 2 and join the list of moved atoms (state 0 otherwise).
+__global__ void k_list_check(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold,
+                             const int *__restrict__ wrapflag, const D4 *__restrict__ xref, int *__restrict__ state,
+                             int *__restrict__ rb, int *__restrict__ flist, unsigned long long *__restrict__ counters) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *P.step += 1ull;  // read by the density sweep that follows
+  bool moved = false;
+  if (i < P.n) {
+    D4 xi = x[i];
+    if (*wrapflag) {
+      wrap_into_box(P, xi);
+      x[i] = xi;
+      xhold[i] = xi;
+      if (i == 0) atomicAdd(&counters[CNT_WRAP], 1ull);
+    }
+    const D4 r = xref[i];
+    const double dx = min_image(xi.x - r.x, P.prd[0], P.half_prd[0]);
+    const double dy = min_image(xi.y - r.y, P.prd[1], P.half_prd[1]);
+    const double dz = min_image(xi.z - r.z, P.prd[2], P.half_prd[2]);
+    moved = dx * dx + dy * dy + dz * dz >= P.lslow2;
+    state[i] = moved ? 2 : 0;
+  }
+  // one atomic per warp (after a long run without a build most atoms move)
+  const unsigned mv = __ballot_sync(0xffffffffu, moved);
+  if (mv) {
+    const int lane = threadIdx.x & 31, lead = __ffs(mv) - 1;
+    int base = 0;
+    if (lane == lead) base = atomicAdd(&rb[1], __popc(mv));
+    base = __shfl_sync(0xffffffffu, base, lead);
+    const int k = base + __popc(mv & ((1u << lane) - 1u));
+    if (moved && k < LIST_FMAX) flist[k] = i;
+  }
+}
+
+// One warp: build or not, and the moved atoms in index order (they were
+// appended in any order; the order of the extra candidates must not change
+// from run to run).
+__global__ void k_list_decide(int *__restrict__ rb, int *__restrict__ flist,
+                              unsigned long long *__restrict__ counters) {
+  const int lane = threadIdx.x;
+  const int cnt = rb[1];
+  const bool build = rb[0] != 0 || cnt > LIST_FMAX;
+  if (!build && cnt > 1) {
+    const int v = lane < cnt ? flist[lane] : 0x7fffffff;
+    int rank = 0;
+    for (int s = 0; s < 32; ++s) rank += __shfl_sync(0xffffffffu, v, s) < v;
+    __syncwarp();
+    if (lane < cnt) flist[rank] = v;
+  }
+  if (lane == 0) {
+    rb[2] = build ? 1 : 0;
+    rb[0] = 0;
+    if (build) atomicAdd(&counters[CNT_BUILD], 1ull);
+  }
+}
+
+__global__ void k_zero_if(int *__restrict__ p, int n, const int *__restrict__ gate) {
+  if (!*gate) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0;
+}
+
+// Block b: moved atom flist[b] flags (state |= 1) every atom whose position
+// at the build lies within r_cutoff + s/2 of its current position — the
+// only unmoved atoms it can now be within r_cutoff of.
+__global__ void k_list_mark(StepParams P, const D4 *__restrict__ x, const int *__restrict__ rb,
+                            const int *__restrict__ flist, const int *__restrict__ bin_count,
+                            const BinEntry *__restrict__ bins, int *__restrict__ state) {
+  if (rb[2] || (int)blockIdx.x >= rb[1]) return;
+  const int f = flist[blockIdx.x];
+  int4 B;
+  float4 o;
+  current_bin(P, x[f], B, o);
+  const int per = 27 * P.bcap;
+  for (int q = threadIdx.x; q < per; q += blockDim.x) {
+    const int slot = q % P.bcap, b = q / P.bcap;
+    const int dx = b % 3 - 1, dy = (b / 3) % 3 - 1, dz = b / 9 - 1;
+    const int Tx = B.x + dx, Ty = B.y + dy, Tz = B.z + dz;
+    const int tx = Tx < 0 ? Tx + P.nb[0] : (Tx >= P.nb[0] ? Tx - P.nb[0] : Tx);
+    const int ty = Ty < 0 ? Ty + P.nb[1] : (Ty >= P.nb[1] ? Ty - P.nb[1] : Ty);
+    const int tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
+    const int flat = tx + P.nb[0] * (ty + P.nb[1] * tz);
+    const int cnt = min(bin_count[flat], P.bcap);
+    if (slot >= cnt) continue;
+    const BinEntry e = bins[(size_t)flat * P.bcap + slot];
+    const float ex = ((float)dx * P.wf[0] - o.x) + e.ox;
+    const float ey = ((float)dy * P.wf[1] - o.y) + e.oy;
+    const float ez = ((float)dz * P.wf[2] - o.z) + e.oz;
+    if (ex * ex + ey * ey + ez * ez < P.rmark2_band) atomicOr(&state[e.idx & IDX_MASK], 1);
+  }
+}
+
+// k_density (FAST, stage 1 and M_i folded in) over the kept candidate lists:
+// on a build step pass 1 searches the bins within r_list for every atom and
+// writes the lists (rows k * n + i of cl, counts in cl_n); otherwise an atom
+// reads its list, except the atoms flagged by k_list_check / k_list_mark,
+// which search the bins of the build afresh (their candidates in shared
+// memory, spilling into their pj rows as in k_density) and add the moved
+// atoms.  Pass 2 and the epilogue are k_density's.
+template <bool MULTI>
+__global__ void __launch_bounds__(128) k_density_list(
+    StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
+    const BinEntry *__restrict__ bins, const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
+    const D4 *__restrict__ xi_given, int xi_mode, const double *__restrict__ T_e, unsigned *__restrict__ pj,
+    D4 *__restrict__ pe, double2 *__restrict__ pg, int *__restrict__ nshort, D4 *__restrict__ A,
+    D4 *__restrict__ Bw, double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell,
+    double *__restrict__ Te_i, int *__restrict__ wrapflag, unsigned *__restrict__ err,
+    unsigned long long *__restrict__ counters, const D4 *__restrict__ v, D4 *__restrict__ Mm, D4 *__restrict__ G,
+    unsigned *__restrict__ cl, int *__restrict__ cl_n, const int *__restrict__ state, const int *__restrict__ rb,
+    const int *__restrict__ flist) {
+  __shared__ unsigned s_cand[CAND_SMEM * 128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
+  if (i == 0) *wrapflag = 0;  // k_list_check has read it
+  const bool valid = i < P.n;
+  const bool active = valid && (mask[i] & P.groupbit) != 0;
+  const size_t n = (size_t)P.n;
+  auto sget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : pj[(size_t)k * n + i]; };
+  auto sset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM)
+      s_cand[k * nt + t] = u;
+    else
+      pj[(size_t)k * n + i] = u;
+  };
+  // build steps: the list rows, their first CAND_SMEM also in shared memory
+  auto lset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM) s_cand[k * nt + t] = u;
+    cl[(size_t)k * n + i] = u;
+  };
+  auto lget = [&](int k) -> unsigned { return cl[(size_t)k * n + i]; };
+  D4 xi = D4{0.0, 0.0, 0.0, 0.0};
+  if (valid) xi = x[i];
+  const int ei = (int)xi.w;
+  const bool build = rb[2] != 0;
+  int nc = 0;
+  bool fresh = false;
+  if (build) {
+    int4 Bi = make_int4(0, 0, 0, 0);
+    float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) {
+      Bi = atom_bin[i];
+      oi = atom_off[i];
+    }
+    // the candidates inside the cut-off first, the shell out to r_list after
+    // them: the shell's pairs mostly fail the exact test, and at the end of
+    // the lists whole warps skip them
+    nc = collect_candidates<true>(P, i, active, Bi, oi, bin_count, bins, err, lget, lset, P.rc2_band, P.lcap);
+    nc = collect_candidates<true>(P, i, active, Bi, oi, bin_count, bins, err, lget, lset, P.rl2_band, P.lcap,
+                                  nullptr, P.rc2_band, nc);
+    if (valid) cl_n[i] = nc;
+  } else {
+    const int st = active ? state[i] : 0;
+    fresh = st != 0;
+    if (__any_sync(0xffffffffu, fresh)) {
+      int4 Bi = make_int4(0, 0, 0, 0);
+      float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (fresh) {
+        if (st & 2) {
+          current_bin(P, xi, Bi, oi);
+        } else {
+          Bi = atom_bin[i];
+          oi = atom_off[i];
+        }
+      }
+      nc = collect_candidates<true, true>(P, i, fresh, Bi, oi, bin_count, bins, err, sget, sset, P.rl2_band, P.kcap,
+                                          state);
+      // the moved atoms near enough (a widened test; pass 2 decides)
+      const int nf = rb[1];  // <= LIST_FMAX on a step without a build
+      for (int q = 0; q < nf; ++q) {
+        const int f = flist[q];
+        if (fresh && f != i) {
+          const D4 xf = x[f];
+          const double dx = min_image(xf.x - xi.x, P.prd[0], P.half_prd[0]);
+          const double dy = min_image(xf.y - xi.y, P.prd[1], P.half_prd[1]);
+          const double dz = min_image(xf.z - xi.z, P.prd[2], P.half_prd[2]);
+          if (dx * dx + dy * dy + dz * dz < P.rc2 * (1.0 + 1e-4)) {
+            if (nc < P.kcap)
+              sset(nc++, (unsigned)f | (CODE_NOSHIFT << IDX_BITS));
+            else
+              atomicOr(err, ERR_PAIR_OVERFLOW);
+          }
+        }
+      }
+    }
+    if (active && !fresh) {
+      // the list's head into shared memory: independent loads up front
+      // instead of one DRAM round trip in front of every pair
+      nc = cl_n[i];
+      const int nh = nc < CAND_SMEM ? nc : CAND_SMEM;
+#pragma unroll 8
+      for (int k = 0; k < nh; ++k) s_cand[k * nt + t] = __ldcs(cl + (size_t)k * n + i);  // read once a step
+    }
+  }
+  __syncwarp();
+  // candidate k: shared memory, then the list rows (or, for an atom that
+  // searched afresh, its pj rows)
+  const unsigned *__restrict__ tail = fresh ? pj : cl;
+  double rho = 0.0, Sx = 0.0, Sy = 0.0, Sz = 0.0;
+  double mxx = 0.0, mxy = 0.0, mxz = 0.0, myy = 0.0, myz = 0.0, mzz = 0.0;
+  int ns = 0;
+  // pass 2: the image of each candidate from FP32 copies of the positions
+  // (integer and FP32 work), then k_density's FP64 work per pair
+  const float xif = float_bits(xi.x), yif = float_bits(xi.y), zif = float_bits(xi.z);
+  const int nmax = __reduce_max_sync(0xffffffffu, nc);
+  for (int k = 0; k < nmax; ++k) {
+    if (k < nc) {
+      const unsigned j = (k < CAND_SMEM ? s_cand[k * nt + t] : __ldcs(tail + (size_t)k * n + i)) & IDX_MASK;
+      const D4 xj = x[j];
+      const unsigned code = image_code(P, xif, yif, zif, xj);
+      double ex, ey, ez;
+      density_vector(P, xi, xj, code, ex, ey, ez);
+      const double r2 = dot3_fma(ex, ey, ez, ex, ey, ez);
+      if (below(r2, P.rc2)) {
+        if (ns < P.kcap)
+          density_pair<true, MULTI, true>(P, ei, j | (code << IDX_BITS), (int)xj.w, ex, ey, ez, r2,
+                                          (size_t)ns * n + i, pj, pe, pg, v, err, rho, mxx, mxy, mxz, myy, myz, mzz,
+                                          Sx, Sy, Sz);
+        else
+          atomicOr(err, ERR_PAIR_OVERFLOW);
+        ++ns;
+      }
+    }
+  }
+  if (!valid) return;
+  density_epilogue<true, true>(P, i, active, xi, ei, rho, ns < P.kcap ? ns : P.kcap, mxx, mxy, mxz, myy, myz, mzz, Sx, Sy, Sz, xi_given,
+                               xi_mode, T_e, nshort, A, Bw, rho_out, beta_out, cell, Te_i, err, counters, v, Mm, G);
 }
 
 // -------------------------------------------------------- friction sweep 1

@@ -77,6 +77,8 @@ SIGNATURES = {
     "eph_pair_energy": (C.c_int, [C.c_void_p, _dp]),
     "eph_set_threads_per_atom": (C.c_int, [C.c_void_p, C.c_int]),
     "eph_get_threads_per_atom": (C.c_int, [C.c_void_p, _ip]),
+    "eph_set_list_skin": (C.c_int, [C.c_void_p, C.c_double]),
+    "eph_get_list_skin": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), _ip]),
     "eph_autotune": (C.c_int, [C.c_void_p, _ip]),
     "eph_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.POINTER(C.c_char_p)),
                                    C.POINTER(eph_md), C.POINTER(C.c_void_p)]),
@@ -434,6 +436,16 @@ class FixEPH:
         out = C.c_int()
         self._check(self.L.eph_get_threads_per_atom(self.h, C.byref(out)))
         return out.value
+
+    def set_list_skin(self, skin):
+        """Skin of the kept candidate lists (0 searches the bins every step)."""
+        self._check(self.L.eph_set_list_skin(self.h, float(skin)))
+
+    def list_skin(self):
+        """(skin, whether the context keeps candidate lists)"""
+        s, a = C.c_double(), C.c_int()
+        self._check(self.L.eph_get_list_skin(self.h, C.byref(s), C.byref(a)))
+        return s.value, bool(a.value)
 
     def autotune(self):
         out = C.c_int()
