@@ -182,9 +182,9 @@ int eph_get_threads_per_atom(eph_ctx *ctx, int *tpa);
  * fastest; *chosen gets it (may be NULL). */
 int eph_autotune(eph_ctx *ctx, int *chosen);
 
-/* Skin s of the kept candidate lists (Angstrom; default 0.3, used up to 2^20
- * atoms, where it pays; a skin set here applies at any size, 0 turns the
- * lists off).  The reference takes its pairs from the engine's Verlet list
+/* Skin s of the kept candidate lists (Angstrom; default 0.3, used from 2^15
+ * to 2^20 atoms, where it pays; a skin set here applies at any size, 0 turns
+ * the lists off).  The reference takes its pairs from the engine's Verlet list
  * (fix_eph.cpp:273-275: a full list with cutoff r_cutoff, padded by the
  * engine's skin and rebuilt when an atom moved half of it); here the list is
  * the context's own.  In FAST mode (model 4, the one-lane density sweep) the

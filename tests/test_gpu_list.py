@@ -20,11 +20,11 @@ TOL = 1e-12
 ATOM_KEYS = ("rho", "w", "f_eph", "f_rng", "f", "x", "v", "array")
 
 
-def _fix(words, at, dt, skin=None):
+def _fix(words, at, dt, skin=0.3, tpa=1):
+    """A FAST context with the list skin set (so it applies at any size)"""
     fix = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_FAST)
-    fix.set_threads_per_atom(1)
-    if skin is not None:
-        fix.set_list_skin(skin)
+    fix.set_threads_per_atom(tpa)
+    fix.set_list_skin(skin)
     return fix
 
 
@@ -99,6 +99,19 @@ def test_same_as_search_every_step(built, cascade):
     assert a.counter("wrap") == b.counter("wrap")
 
 
+def test_with_lanes_in_the_force_sweep(built, cascade):
+    """From 16,384 atoms on the one-lane density sweep feeds force sweeps
+    with several lanes per atom: lists with 4 lanes against the bin search."""
+    words, at = cascade
+    a = _fix(words, at, 0.0005, tpa=4)
+    b = _fix(words, at, 0.0005, skin=0.0, tpa=4)
+    assert a.list_skin()[1] and a.threads_per_atom() == 4
+    a.step(30)
+    b.step(30)
+    for k in ("rho", "w", "f_eph", "f_rng", "x", "v", "T"):
+        assert rel_err(a.get(k), b.get(k)) <= TOL, (k, rel_err(a.get(k), b.get(k)))
+
+
 def test_run_to_run_and_graph(built, cascade):
     """Direct steps and graph replays give the same bits (the build decisions
     live on the device)."""
@@ -124,7 +137,7 @@ def test_hooks_with_host_positions(built, cascade):
     lists against a bin search every step."""
     words, at = cascade
     out = []
-    for skin in (None, 0.0):
+    for skin in (0.3, 0.0):
         h = _fix(words, at, 0.0005, skin=skin)
         x, v = at.x.copy(), at.v.copy()
         f = np.zeros_like(x)
@@ -150,7 +163,11 @@ def test_when_reuse_is_off(built, beta_file):
     words, at, dt = scenario("c1_small", beta_file)
     assert not ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_EXACT).list_skin()[1]
     fix = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_FAST)
-    fix.set_threads_per_atom(4)
+    fix.set_threads_per_atom(1)
+    assert fix.list_skin() == (0.3, False)  # 500 atoms: below the default size range
+    fix.set_list_skin(0.3)
+    assert fix.list_skin() == (0.3, True)
+    fix.set_threads_per_atom(4)  # below 16,384 atoms the density sweep has the lanes
     assert not fix.list_skin()[1]
     fix.set_threads_per_atom(1)
     assert fix.list_skin()[1]

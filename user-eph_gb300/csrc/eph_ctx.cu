@@ -308,15 +308,18 @@ int auto_bcap(const eph_ctx *c) {
 
 // Kept candidate lists: FAST mode, model 4 with friction, the one-lane
 // density sweep (one lane per atom, or 16,384 atoms and more), no pair force
-// of the engine (it needs bins every step) and no adjoint.  By default up to
-// 2^20 atoms: the lists save the bin search, which the density sweep's FP64
-// pass hides less well in small systems (measured on GB300 with a 0.3 A skin,
-// step time: 131,072 atoms -9 %, 500,000 atoms -2 %, 2,048,000 atoms +0.2 %,
-// where both sweeps already run at the FP64 issue limit); a skin set through
-// eph_set_list_skin applies at any size.
+// of the engine (it needs bins every step) and no adjoint.  By default from
+// 2^15 to 2^20 atoms: the lists save the bin search, which the density
+// sweep's FP64 pass hides less well in small systems, and cost four small
+// launches a step plus the atoms near moved ones (measured on GB300 with a
+// 0.3 A skin, step time: 16,384 atoms +18 %, 62,500 atoms -8 %, 131,072 atoms
+// -9 %, 256,000 atoms -5 %, 500,000 atoms -2 %, 1,000,188 atoms -1 %,
+// 2,048,000 atoms +0.2 %, where both sweeps already run at the FP64 issue
+// limit); a skin set through eph_set_list_skin applies at any size.
 bool want_list(const eph_ctx *c) {
+  const bool size_ok = c->lskin_user || (c->n >= (1 << 15) && c->n <= (1 << 20));
   if (c->mode != EPH_MODE_FAST || c->lskin <= 0.0 || c->list_block || c->eam || c->n <= 0 ||
-      !(c->tpa == 1 || c->n >= 16384) || !fused_friction(c) || !(c->lskin_user || c->n <= (1 << 20)))
+      !(c->tpa == 1 || c->n >= 16384) || !fused_friction(c) || !size_ok)
     return false;
   for (int k = 0; k < 3; ++k)
     if ((int)(c->prd[k] / ((c->beta.r_cutoff + c->lskin) * (1.0 + 5e-5))) < 3) return false;

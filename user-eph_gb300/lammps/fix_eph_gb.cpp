@@ -112,6 +112,9 @@ int FixEPHGB::modify_param(int narg, char **arg) {
     return 2;
   } else if (strcmp(arg[0], "device") == 0) {
     device = atoi(arg[1]);
+  } else if (strcmp(arg[0], "list_skin") == 0) {
+    check(eph_set_list_skin(ctx, atof(arg[1])), "list skin");
+    return 2;
   } else {
     return 0;
   }

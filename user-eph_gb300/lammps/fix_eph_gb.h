@@ -14,7 +14,8 @@
  *
  * fix_modify options: `mode exact|fast` (EPH_MODE_*), `xi host|device`
  * (deviates from the engine's RanMars stream on the host, or the device
- * Philox generator), `device N`.
+ * Philox generator), `device N`, `list_skin S` (skin of the kept candidate
+ * lists in distance units, 0: search the bins every step).
  * One MPI rank per GPU holding every atom of the box (the device builds its
  * own periodic minimum-image neighbour pairs, so no ghost communication).
  */
