@@ -123,19 +123,19 @@ def density_bytes(n_atoms, n_pairs):
     FAST, one element, stage 1 folded in): per atom read x_i, v_i (64 B), mask
     (4), bin and offset (32), T_e at the atom (8); written pair count (4), A_i,
     Bw_i (64), M_i (64), G_i (64), rho, beta, T_e at the atom (24), cell (4);
-    per in-cutoff pair the cached index (4) and e_ij with rho_j(r^2)/r^2 (32)
-    written.  The neighbours' positions and velocities and the bins are L2
-    hits and not counted."""
-    return 332 * n_atoms + 36 * n_pairs
+    per in-cutoff pair the cached index (4), e_ij with the x of H e (32) and
+    the y, z of H e (16) written, H = rho_j(r^2)/r^2.  The neighbours'
+    positions and velocities and the bins are L2 hits and not counted."""
+    return 332 * n_atoms + 52 * n_pairs
 
 
 def forces_bytes(n_atoms, n_pairs):
     """Algorithmic HBM bytes of one launch of the force sweep (k_forces_m,
     FAST, one element): per atom G_i and M_i (128 B), pair count (4), T_e at
     the atom (8), f read and written (64), f_EPH and f_RNG written (64); per
-    in-cutoff pair the cached index (4) and e_ij with rho_j(r^2)/r^2 (32).
-    The neighbours' records G_j are L2 hits and not counted."""
-    return 268 * n_atoms + 36 * n_pairs
+    in-cutoff pair the cached index (4), e_ij and H e (48).  The neighbours'
+    records G_j are L2 hits and not counted."""
+    return 268 * n_atoms + 52 * n_pairs
 
 
 # DRAM bytes of one launch (dram__bytes_read.sum + dram__bytes_write.sum,
@@ -143,16 +143,16 @@ def forces_bytes(n_atoms, n_pairs):
 # pairs per atom, profiles/launch_list_cascade_2048k.md) over the algorithmic
 # bytes of that launch; the bench's traffic figure is this ratio times the
 # algorithmic bytes at its own pair count.
-DENSITY_DRAM_OVER_ALGORITHMIC = (0.31433e9 + 3.50e9) / density_bytes(2048000, 86014654)
-FORCES_DRAM_OVER_ALGORITHMIC = (3.47e9 + 0.18816e9) / forces_bytes(2048000, 86014654)
+DENSITY_DRAM_OVER_ALGORITHMIC = (0.333024e9 + 4.871331e9) / density_bytes(2048000, 86014654)
+FORCES_DRAM_OVER_ALGORITHMIC = (4.877350e9 + 0.189359e9) / forces_bytes(2048000, 86014654)
 # FP64-pipe utilisation of the two sweeps (ncu, profiles/sweeps_fcc_131k.md)
-DENSITY_FP64_PIPE = 0.676
-FORCES_FP64_PIPE = 0.874
+DENSITY_FP64_PIPE = 0.675
+FORCES_FP64_PIPE = 0.841
 # FP64 thread instructions per in-cutoff pair (DADD + DMUL + DFMA, predicated
 # on; ncu on the 131,072-atom case, per-atom work included) and the GB300's
 # FP64 issue rate: 2 thread instructions per SM per clock at 2.07 GHz
-DENSITY_FP64_PER_PAIR = 31.34
-FORCES_FP64_PER_PAIR = 15.14
+DENSITY_FP64_PER_PAIR = 31.18
+FORCES_FP64_PER_PAIR = 13.14
 FP64_PEAK = 2 * 152 * 2.07e9
 
 
@@ -730,7 +730,7 @@ def main():
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "atoms_per_gpu": n, "grid": list(GRID), "dt_ps": DT,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 36 // 2 ** 20),
+                   "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 52 // 2 ** 20),
                    "mode": "fast", "xi": "device Philox4x32-10"},
         "gpu_launches": res["launches"],
         "roofline": roofline("density", "k_density", density_bytes(n, res["n_pairs"]),

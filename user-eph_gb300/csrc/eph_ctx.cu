@@ -24,10 +24,15 @@ using namespace ephgb;
 namespace ephgb {
 namespace ctxi {
 
-// pg rows (rho(r^2) per pair) exist for EXACT mode and for several elements;
-// FAST mode with one element reads neither (16 B per pair saved)
+bool fused_friction(const eph_ctx *c);
+
+// pg rows per pair: {rho_j(r^2), rho_i(r^2)} in EXACT mode, {rho_i(r^2)/r^2, 0}
+// in FAST mode with several elements, the y and z of H e with one element
+// when stage 1 is folded into the density sweep (the force sweep then needs
+// no H per pair); none otherwise
 cudaError_t alloc_pg(eph_ctx *c) {
-  if (c->mode == EPH_MODE_EXACT || c->multi) return c->pg.alloc((size_t)c->kcap * (size_t)c->n);
+  if (c->mode == EPH_MODE_EXACT || c->multi || fused_friction(c))
+    return c->pg.alloc((size_t)c->kcap * (size_t)c->n);
   c->pg.free();
   return cudaSuccess;
 }

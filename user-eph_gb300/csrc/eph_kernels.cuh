@@ -311,11 +311,18 @@ __device__ __forceinline__ void density_pair(const StepParams &P, int ei, unsign
   if (FAST) {
     const double inv_r2 = recip_nr(r2);
     const double H = rji * inv_r2;
-    pe[slot] = D4{ex, ey, ez, H};
-    if (MULTI) pg[slot] = make_double2(rij * inv_r2, 0.0);
+    const double hx = H * ex, hy = H * ey, hz = H * ez;
+    if (FUSE_W && !MULTI) {
+      // one element: H_ij = H_ji, and the force sweep takes the pair's
+      // H e from here instead of multiplying by H per pair
+      pe[slot] = D4{ex, ey, ez, hx};
+      pg[slot] = make_double2(hy, hz);
+    } else {
+      pe[slot] = D4{ex, ey, ez, H};
+      if (MULTI) pg[slot] = make_double2(rij * inv_r2, 0.0);
+    }
     if (FUSE_W) {
       const D4 vj = v[u & IDX_MASK];
-      const double hx = H * ex, hy = H * ey, hz = H * ez;
       mxx = fma(hx, ex, mxx);
       mxy = fma(hx, ey, mxy);
       mxz = fma(hx, ez, mxz);
@@ -1110,16 +1117,30 @@ __global__ void __launch_bounds__(128) k_forces_m(StepParams P, const unsigned *
       skipped = 1;
       continue;
     }
-    const double Hji = MULTI ? pg[slot].x : e.w;  // rho_i(r^2)/r^2
-    const double sw = Hji * dot3_fma(e.x, e.y, e.z, Gj1.x, Gj1.y, Gj1.z);
-    fex = fma(sw, e.x, fex);
-    fey = fma(sw, e.y, fey);
-    fez = fma(sw, e.z, fez);
-    if (RAND) {
-      const double sx = Hji * dot3_fma(e.x, e.y, e.z, Gj1.w, Gj2.x, Gj2.y);
-      frx = fma(sx, e.x, frx);
-      fry = fma(sx, e.y, fry);
-      frz = fma(sx, e.z, frz);
+    if (MULTI) {
+      const double Hji = pg[slot].x;  // rho_i(r^2)/r^2
+      const double sw = Hji * dot3_fma(e.x, e.y, e.z, Gj1.x, Gj1.y, Gj1.z);
+      fex = fma(sw, e.x, fex);
+      fey = fma(sw, e.y, fey);
+      fez = fma(sw, e.z, fez);
+      if (RAND) {
+        const double sx = Hji * dot3_fma(e.x, e.y, e.z, Gj1.w, Gj2.x, Gj2.y);
+        frx = fma(sx, e.x, frx);
+        fry = fma(sx, e.y, fry);
+        frz = fma(sx, e.z, frz);
+      }
+    } else {  // the pair's H e: {e.w, pg.x, pg.y}
+      const double2 h = pg[slot];
+      const double sw = dot3_fma(e.x, e.y, e.z, Gj1.x, Gj1.y, Gj1.z);
+      fex = fma(sw, e.w, fex);
+      fey = fma(sw, h.x, fey);
+      fez = fma(sw, h.y, fez);
+      if (RAND) {
+        const double sx = dot3_fma(e.x, e.y, e.z, Gj1.w, Gj2.x, Gj2.y);
+        frx = fma(sx, e.w, frx);
+        fry = fma(sx, h.x, fry);
+        frz = fma(sx, h.y, frz);
+      }
     }
   }
   if (TPA > 1) {
@@ -1147,15 +1168,24 @@ __global__ void __launch_bounds__(128) k_forces_m(StepParams P, const unsigned *
         const unsigned j = pj[slot] & IDX_MASK;
         if (pos_double(G[2 * (size_t)j + 1].z)) continue;
         const D4 e = pe[slot];
-        const double sw = e.w * dot3_fma(e.x, e.y, e.z, Gi1.x, Gi1.y, Gi1.z);
-        cex = fma(sw, e.x, cex);
-        cey = fma(sw, e.y, cey);
-        cez = fma(sw, e.z, cez);
+        // H_ij e: {H e.x, e.y, e.z} with several elements, {e.w, pg} with one
+        double hx = e.x, hy = e.y, hz = e.z, H = e.w;
+        if (!MULTI) {
+          const double2 h = pg[slot];
+          hx = e.w;
+          hy = h.x;
+          hz = h.y;
+          H = 1.0;
+        }
+        const double sw = H * dot3_fma(e.x, e.y, e.z, Gi1.x, Gi1.y, Gi1.z);
+        cex = fma(sw, hx, cex);
+        cey = fma(sw, hy, cey);
+        cez = fma(sw, hz, cez);
         if (RAND) {
-          const double sx = e.w * dot3_fma(e.x, e.y, e.z, Gi1.w, Gi2.x, Gi2.y);
-          crx = fma(sx, e.x, crx);
-          cry = fma(sx, e.y, cry);
-          crz = fma(sx, e.z, crz);
+          const double sx = H * dot3_fma(e.x, e.y, e.z, Gi1.w, Gi2.x, Gi2.y);
+          crx = fma(sx, hx, crx);
+          cry = fma(sx, hy, cry);
+          crz = fma(sx, hz, crz);
         }
       }
     }
