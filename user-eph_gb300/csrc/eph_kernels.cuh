@@ -302,10 +302,12 @@ __device__ __forceinline__ void density_pair(const StepParams &P, int ei, unsign
                                              const D4 *__restrict__ v, unsigned *__restrict__ err, double &rho,
                                              double &mxx, double &mxy, double &mxz, double &myy, double &myz,
                                              double &mzz, double &Sx, double &Sy, double &Sz) {
-  const double rji = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+  const double rji = FAST ? spline_eval_f32i(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq_f, P.n_rho, r2, err)
+                         : spline_eval<false>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
   double rij = rji;
   if (MULTI && ej != ei)
-    rij = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+    rij = FAST ? spline_eval_f32i(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq_f, P.n_rho, r2, err)
+               : spline_eval<false>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
   rho += rji;
   pj[slot] = u;
   if (FAST) {
@@ -639,19 +641,6 @@ __device__ __forceinline__ double min_image(double d, double L, double h) {
   return d > h ? d - L : (d < -h ? d + L : d);
 }
 
-// v truncated to float by integer work on its bits (the conversion
-// instruction would run on the FP64 pipe): exponent rebased, top 23 mantissa
-// bits; |v| < 2^-126 gives 0.  Good to 2^-23 relative, for the image test.
-__device__ __forceinline__ float float_bits(double v) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned hi = (unsigned)(b >> 32);
-  int e = (int)((hi >> 20) & 0x7ffu);
-  if (e < 897) return 0.f;
-  e = e > 1150 ? 1150 : e;
-  return __uint_as_float((hi & 0x80000000u) | ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) |
-                         ((unsigned)b >> 29));
-}
-
 // The 3x3x3 image code of x_j seen from x_i: the image of x_j within half a
 // box of x_i on every axis, decided in FP32 (the box is at least three list
 // radii wide, so a pair within the list radius is far from the threshold).
@@ -787,8 +776,10 @@ __global__ void k_list_mark(StepParams P, const D4 *__restrict__ x, const int *_
 // which search the bins of the build afresh (their candidates in shared
 // memory, spilling into their pj rows as in k_density) and add the moved
 // atoms.  Pass 2 and the epilogue are k_density's.
+// (128 threads a block; 64 registers as k_density has: with
+// __launch_bounds__(128) ptxas settled on 56 and spilled)
 template <bool MULTI>
-__global__ void __launch_bounds__(128) k_density_list(
+__global__ void __maxnreg__(64) k_density_list(
     StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
     const BinEntry *__restrict__ bins, const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
     const D4 *__restrict__ xi_given, int xi_mode, const double *__restrict__ T_e, unsigned *__restrict__ pj,
