@@ -143,15 +143,15 @@ def forces_bytes(n_atoms, n_pairs):
 # pairs per atom, profiles/launch_list_cascade_2048k.md) over the algorithmic
 # bytes of that launch; the bench's traffic figure is this ratio times the
 # algorithmic bytes at its own pair count.
-DENSITY_DRAM_OVER_ALGORITHMIC = (0.333751e9 + 4.871318e9) / density_bytes(2048000, 86014654)
-FORCES_DRAM_OVER_ALGORITHMIC = (4.876678e9 + 0.189090e9) / forces_bytes(2048000, 86014654)
+DENSITY_DRAM_OVER_ALGORITHMIC = (0.333330e9 + 4.870853e9) / density_bytes(2048000, 86014654)
+FORCES_DRAM_OVER_ALGORITHMIC = (4.876371e9 + 0.189099e9) / forces_bytes(2048000, 86014654)
 # FP64-pipe utilisation of the two sweeps (ncu, profiles/sweeps_fcc_131k.md)
-DENSITY_FP64_PIPE = 0.673
+DENSITY_FP64_PIPE = 0.670
 FORCES_FP64_PIPE = 0.841
 # FP64 thread instructions per in-cutoff pair (DADD + DMUL + DFMA, predicated
 # on; ncu on the 131,072-atom case, per-atom work included) and the GB300's
 # FP64 issue rate: 2 thread instructions per SM per clock at 2.07 GHz
-DENSITY_FP64_PER_PAIR = 30.18
+DENSITY_FP64_PER_PAIR = 29.23
 FORCES_FP64_PER_PAIR = 13.14
 FP64_PEAK = 2 * 152 * 2.07e9
 

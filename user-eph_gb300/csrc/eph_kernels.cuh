@@ -308,7 +308,9 @@ __device__ __forceinline__ void density_pair(const StepParams &P, int ei, unsign
   if (MULTI && ej != ei)
     rij = FAST ? spline_eval_f32i(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq_f, P.n_rho, r2, err)
                : spline_eval<false>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
-  rho += rji;
+  // with M_i summed (FAST, FUSE_W) rho_i is its trace, sum_j H_ij r^2
+  // (density_epilogue): one FP64 add per pair less
+  if (!(FAST && FUSE_W)) rho += rji;
   pj[slot] = u;
   if (FAST) {
     const double inv_r2 = recip_nr(r2);
@@ -370,6 +372,9 @@ __device__ __forceinline__ void density_epilogue(
     unsigned long long *__restrict__ counters, const D4 *__restrict__ v, D4 *__restrict__ Mm,
     D4 *__restrict__ G) {
   nshort[i] = ns;
+  // FAST with M_i: rho_i = trace M_i = sum_j rho_j(r^2) / r^2 * r^2, within
+  // the reciprocal's error (~6e-14) of the sum of rho_j(r^2)
+  if (FAST && FUSE_W) rho = mxx + myy + mzz;
   // per-atom quantities
   double alpha = 0.0, beta = 0.0, xi3[3] = {0.0, 0.0, 0.0};
   if (active) {
@@ -600,7 +605,7 @@ __global__ void __launch_bounds__(128) k_density_tpa(
   }
 #pragma unroll
   for (int o = TPA / 2; o > 0; o >>= 1) {
-    rho += __shfl_xor_sync(0xffffffffu, rho, o);
+    if (!FUSE_W) rho += __shfl_xor_sync(0xffffffffu, rho, o);  // with M_i: its trace
     if (FUSE_W) {
       mxx += __shfl_xor_sync(0xffffffffu, mxx, o);
       mxy += __shfl_xor_sync(0xffffffffu, mxy, o);
