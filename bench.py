@@ -151,7 +151,7 @@ FORCES_FP64_PIPE = 0.841
 # FP64 thread instructions per in-cutoff pair (DADD + DMUL + DFMA, predicated
 # on; ncu on the 131,072-atom case, per-atom work included) and the GB300's
 # FP64 issue rate: 2 thread instructions per SM per clock at 2.07 GHz
-DENSITY_FP64_PER_PAIR = 29.23
+DENSITY_FP64_PER_PAIR = 30.23  # 29.23 counted with an FP32 spline index, + the exact index's DMUL
 FORCES_FP64_PER_PAIR = 13.14
 FP64_PEAK = 2 * 152 * 2.07e9
 

@@ -840,7 +840,6 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
   P.tab_beta = c->tab_beta.p;
   P.tab_alpha = c->tab_alpha.p;
   P.inv_dr_sq = c->beta.rho_r_sq[0].inv_dx;
-  P.inv_dr_sq_f = (float)P.inv_dr_sq;
   P.inv_drho = c->beta.beta[0].inv_dx;
   P.n_rho = (int)c->beta.n_rho;
   P.n_beta = (int)c->beta.n_beta;

@@ -67,7 +67,6 @@ struct StepParams {
   const D4 *tab_beta;
   const D4 *tab_alpha;
   double inv_dr_sq, inv_drho;
-  float inv_dr_sq_f;  // (float) inv_dr_sq, for the FP32 spline index of the pair loop
   int n_rho, n_beta;
   double rho_cutoff;
   // integrator and forces
@@ -116,7 +115,7 @@ __device__ __forceinline__ unsigned long long trunc_index(double y) {
 // v truncated to float by integer work on its bits (the conversion
 // instruction would run on the FP64 pipe): exponent rebased, top 23 mantissa
 // bits; |v| < 2^-126 gives 0.  Good to 2^-23 relative (truncated): for image
-// tests and spline indices, not for arithmetic.
+// tests, not for arithmetic.
 __device__ __forceinline__ float float_bits(double v) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
   const unsigned hi = (unsigned)(b >> 32);
@@ -125,23 +124,6 @@ __device__ __forceinline__ float float_bits(double v) {
   e = e > 1150 ? 1150 : e;
   return __uint_as_float((hi & 0x80000000u) | ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) |
                          ((unsigned)b >> 29));
-}
-
-// FAST-mode spline of the pair loop: the index floor(x / dx) from FP32
-// copies (x truncated by its bits, the FP32 product), which keeps the
-// multiplication off the FP64 pipe.  Near a knot the index may land one
-// interval off; the spline is C2 there, so the neighbouring cubic evaluated
-// next to its knot differs from the right one at rounding level.
-__device__ __forceinline__ double spline_eval_f32i(const D4 *__restrict__ tab, float inv_dx, int n, double x,
-                                                   unsigned *err) {
-  const float q = float_bits(x) * inv_dx;
-  unsigned idx = q < 4.0e9f ? (unsigned)q : 0xffffffffu;
-  if (idx >= (unsigned)n) {
-    atomicOr(err, ERR_SPLINE_RANGE);
-    idx = (unsigned)(n - 1);
-  }
-  const D4 c = tab[idx];
-  return fma(x, fma(x, fma(x, c.w, c.z), c.y), c.x);
 }
 
 template <bool FAST>

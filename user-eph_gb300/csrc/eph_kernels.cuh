@@ -302,12 +302,10 @@ __device__ __forceinline__ void density_pair(const StepParams &P, int ei, unsign
                                              const D4 *__restrict__ v, unsigned *__restrict__ err, double &rho,
                                              double &mxx, double &mxy, double &mxz, double &myy, double &myz,
                                              double &mzz, double &Sx, double &Sy, double &Sz) {
-  const double rji = FAST ? spline_eval_f32i(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq_f, P.n_rho, r2, err)
-                         : spline_eval<false>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+  const double rji = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ej * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
   double rij = rji;
   if (MULTI && ej != ei)
-    rij = FAST ? spline_eval_f32i(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq_f, P.n_rho, r2, err)
-               : spline_eval<false>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
+    rij = spline_eval<FAST>(P.tab_rho_r_sq + (size_t)ei * P.n_rho, P.inv_dr_sq, P.n_rho, r2, err);
   // with M_i summed (FAST, FUSE_W) rho_i is its trace, sum_j H_ij r^2
   // (density_epilogue): one FP64 add per pair less
   if (!(FAST && FUSE_W)) rho += rji;
