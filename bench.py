@@ -140,12 +140,12 @@ def forces_bytes(n_atoms, n_pairs):
 
 # DRAM bytes of one launch (dram__bytes_read.sum + dram__bytes_write.sum,
 # one-pass ncu capture of the bench workload itself, 2,048,000 atoms at 42.0
-# pairs per atom, profiles/launch_list_cascade_2048k.md) over the algorithmic
+# pairs per atom) over the algorithmic
 # bytes of that launch; the bench's traffic figure is this ratio times the
 # algorithmic bytes at its own pair count.
 DENSITY_DRAM_OVER_ALGORITHMIC = (0.333330e9 + 4.870853e9) / density_bytes(2048000, 86014654)
 FORCES_DRAM_OVER_ALGORITHMIC = (4.876371e9 + 0.189099e9) / forces_bytes(2048000, 86014654)
-# FP64-pipe utilisation of the two sweeps (ncu, profiles/sweeps_fcc_131k.md)
+# FP64-pipe utilisation of the two sweeps (ncu, 131,072-atom fcc case)
 DENSITY_FP64_PIPE = 0.670
 FORCES_FP64_PIPE = 0.841
 # FP64 thread instructions per in-cutoff pair (DADD + DMUL + DFMA, predicated

@@ -249,10 +249,17 @@ int eph_batch_launch_count(eph_batch *batch, long *per_step);
  * loading this library holds until exit; larger grids return
  * EPH_ERR_CAPACITY.  The first call on a device looks up that array's device
  * address, so make it before any stream capture.  All calls share the
- * scratch: calls that overlap on the GPU race.  Work is ordered on `stream`
- * (a cudaStream_t, 0 for the default stream) and finished on return; the
- * number of substeps taken goes to *nsub_out (may be NULL). */
+ * scratch: calls that overlap on the GPU race.  lo and hi are HOST arrays of
+ * 3 doubles (the grid box); every other array is a device pointer.  Work is
+ * ordered on `stream` (a cudaStream_t, 0 for the default stream); the call
+ * synchronises that stream twice (it reads the stability bounds back to pick
+ * the substep count) and has finished on return.  The number of substeps
+ * taken goes to *nsub_out (may be NULL).  EPH_ERR_ARG, before any launch:
+ * C_e or rho_e of cell 0 or of a non-CONSTANT cell <= 0, or more than
+ * EPH_NOALLOC_MAX_SUBSTEPS substeps (given or required by the stability
+ * rule). */
 #define EPH_NOALLOC_MAX_CELLS 262144 /* 64^3 */
+#define EPH_NOALLOC_MAX_SUBSTEPS 1000000
 int eph_fdm_solve_noalloc(long nx, long ny, long nz, const double *lo, const double *hi, double dt, long steps,
                           double *T, const double *dT, const double *S, const double *rho_e, const double *C_e,
                           const double *kappa, const signed char *flag, void *stream, unsigned *nsub_out);

@@ -183,6 +183,17 @@ def ref_available():
     return os.path.exists(REF_SO)
 
 
+def reference_tree():
+    """The reference tree _ref/libephref.so was compiled from (recorded by the
+    Makefile in _ref/tree.txt), or EPH_REFERENCE_TREE; None when neither names
+    an existing directory."""
+    tree = os.environ.get("EPH_REFERENCE_TREE")
+    rec = os.path.join(HERE, "_ref", "tree.txt")
+    if not tree and os.path.exists(rec):
+        tree = open(rec).read().strip()
+    return tree if tree and os.path.isdir(tree) else None
+
+
 def ref_lib():
     global _ref
     if _ref is None:
@@ -372,6 +383,7 @@ class GbFix:
             lib.gbh_step.argtypes = [C.c_void_p, _dp, C.c_long, C.c_char_p, C.c_int]
             lib.gbh_get.argtypes = [C.c_void_p, C.c_char_p, _dp]
             lib.gbh_post_run.argtypes = [C.c_void_p]
+            lib.gbh_modify.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int]
             GbFix._lib = lib
         lib = GbFix._lib
         self.lib = lib
@@ -398,6 +410,13 @@ class GbFix:
         err = C.create_string_buffer(512)
         if self.lib.gbh_step(self.h, _d(a), 0 if a is None else a.size, err, 512):
             raise RuntimeError(err.value.decode())
+
+    def modify(self, key, value):
+        """fix_modify ID key value"""
+        err = C.create_string_buffer(512)
+        rc = self.lib.gbh_modify(self.h, key.encode(), str(value).encode(), err, 512)
+        if rc:
+            raise RuntimeError(f"fix_modify {key} {value}: {err.value.decode()} ({rc})")
 
     def get(self, what):
         k = {"x": 3, "v": 3, "f": 3, "array": 8}.get(what)

@@ -110,6 +110,19 @@ int gbh_get(void *h, const char *what, double *out) {
   return 0;
 }
 
+/* fix_modify ID key value (e.g. "peratom" "3", "list_skin" "0.3") */
+int gbh_modify(void *h, const char *key, const char *value, char *errbuf, int errlen) {
+  GbSim *s = static_cast<GbSim *>(h);
+  std::string k(key), v(value);
+  char *a[2] = {&k[0], &v[0]};
+  try {
+    return s->fix->modify_param(2, a) == 2 ? 0 : 1;
+  } catch (std::exception &e) {
+    copy_err(e.what(), errbuf, errlen);
+    return 2;
+  }
+}
+
 int gbh_post_run(void *h) {
   static_cast<GbSim *>(h)->fix->post_run();
   return 0;

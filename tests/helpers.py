@@ -29,6 +29,46 @@ def rel_err(a, b):
     return float(np.abs(a - b).max() / scale)
 
 
+def atom_err(a, b, floor=None):
+    """Per-atom relative error: max over atoms i of |a_i - b_i| / (|b_i| + s),
+    with |.| the largest component of atom i's row (a 3-vector, or a scalar
+    for 1-D arrays).  Every atom is measured against its own magnitude —
+    unlike a norm-wise error, which a single fast atom's large value
+    dominates — plus a floor s for values that nearly vanish by cancellation
+    (their own digits are rounding noise in any arithmetic, the reference's
+    included).  s defaults to the larger of the median of |b_i| (a typical
+    atom) and 1e-3 max_i |b_i|; the second only matters where most atoms
+    carry nothing, as in a lattice at rest hit by one knock-on atom, whose
+    other nonzero values are sums cancelling by the lattice's symmetry.
+    Rows equal in both count as 0 (also where b_i = 0)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if a.ndim == 1:
+        a, b = a[:, None], b[:, None]
+    d = np.abs(a - b).max(axis=1)
+    m = np.abs(b).max(axis=1)
+    s = max(float(np.median(m)), 1e-3 * float(m.max(initial=0.0))) if floor is None else float(floor)
+    den = m + s
+    e = np.zeros_like(d)
+    nz = d != 0
+    e[nz] = d[nz] / np.where(den[nz] > 0, den[nz], np.inf)
+    e[nz & (den == 0)] = np.inf
+    return float(e.max()) if e.size else 0.0
+
+
+# column groups of the fix's per-atom array (fix_eph.cpp:406-415): rho_i,
+# beta(rho_i), f_EPH, f_RNG
+ARRAY_GROUPS = ((0, 1), (1, 2), (2, 5), (5, 8))
+
+
+def key_err(key, a, b):
+    """The per-atom error of a named per-atom output (atom_err per row; the
+    per-atom array per column group); the grid T per cell."""
+    if key == "array":
+        return max(atom_err(np.asarray(a)[:, lo:hi], np.asarray(b)[:, lo:hi]) for lo, hi in ARRAY_GROUPS)
+    return atom_err(a, b)
+
+
 def scenario(name, beta_file, beta_file_2el=None):
     """(words, atoms, dt, flags) of a named test scenario."""
     if name == "c1_small":  # the C1 setting on 5^3 cells

@@ -4,24 +4,43 @@ the oracle builds, including hosts without the reference tree."""
 import numpy as np
 import pytest
 
-from golden_io import FIXTURES, GOLDEN, load_fix
+from golden_io import FIXTURES, GOLDEN, REF_FIXTURES, fixture_steps, fixture_xi, load_fix
 from oracle.bindings import OracleFix
 
 LAST_ONLY = ("f_eph", "f_rng", "w", "array")
 
 
-@pytest.mark.parametrize("name", FIXTURES)
+@pytest.mark.parametrize("name", FIXTURES + REF_FIXTURES)
 def test_oracle_matches_golden(built, tmp_path, name):
+    """Every recorded step bit for bit.  The REF_FIXTURES run the reference's
+    own input files: Tests/MD_Run (the deck's fix line `eph 1111 7 4 1.0 3.5e-6
+    0.1248 0.0 7 8 9 NULL 0 T_out Ni.beta Ni Ni` with its Ni.beta: T_e = 0, a
+    7x8x9 grid, two types on one element), Tests/EPH_Beta_zero (rho_cutoff 5,
+    crossed by a knock-on atom: beta = alpha = 0 above it), the four-element
+    NiCoCrFe beta file, and Examples/Example_4 (its atoms, grid file T.in and
+    beta file)."""
     words, at, dt, rec = load_fix(name, str(tmp_path))
     o = OracleFix(words, at, dt)
-    nsteps = rec["x"].shape[0]
+    nsteps, recorded = fixture_steps(rec)
     for s in range(nsteps):
-        xi = rec["xi"][s]
-        o.step(xi if xi.size else None)
+        xi = fixture_xi(rec, words, at, s)
+        o.step(xi if xi is not None and xi.size else None)
+        if s not in recorded:
+            continue
+        r = recorded.index(s)
         for k in ("x", "v", "f", "rho", "vector", "T"):
-            assert np.array_equal(o.get(k), rec[k][s]), (name, s, k)
+            assert np.array_equal(o.get(k), rec[k][r]), (name, s, k)
     for k in LAST_ONLY:
         assert np.array_equal(o.get(k), rec[k]), (name, k)
+
+
+def test_beta_zero_fixture_crosses_rho_cutoff(tmp_path):
+    """The Tests/EPH_Beta_zero fixture exercises the rho > rho_cutoff branch
+    (eph_beta.h:174-197): some recorded step has an atom above rho_cutoff = 5,
+    whose beta column in the per-atom array is 0."""
+    words, at, dt, rec = load_fix("beta_zero", str(tmp_path))
+    assert (rec["rho"] > 5.0).any()
+    assert (rec["rho"] < 5.0).all(axis=1)[-1]  # and the pair has left the region again
 
 
 def test_fdm_test1_golden(built):

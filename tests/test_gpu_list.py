@@ -12,7 +12,7 @@ import pytest
 
 import ephgb
 from ephgb import workloads as W
-from helpers import n_in_group, rel_err, scenario, xi_rows
+from helpers import atom_err, key_err, n_in_group, scenario, xi_rows
 from oracle.bindings import OracleFix
 
 pytestmark = pytest.mark.gpu
@@ -38,8 +38,8 @@ def _against_oracle(words, at, dt, steps, seed=5):
         gpu.step(1, xi=xi_rows(at, stream))
         ref.step(stream)
         for k in ATOM_KEYS:
-            assert rel_err(gpu.get(k), ref.get(k)) <= TOL, (s, k, rel_err(gpu.get(k), ref.get(k)))
-        assert rel_err(gpu.get("T"), ref.get("T")) <= TOL, s
+            assert key_err(k, gpu.get(k), ref.get(k)) <= TOL, (s, k, key_err(k, gpu.get(k), ref.get(k)))
+        assert atom_err(gpu.get("T"), ref.get("T")) <= TOL, s
     return gpu
 
 
@@ -93,7 +93,7 @@ def test_same_as_search_every_step(built, cascade):
         a.step(10)
         b.step(10)
         for k in ("rho", "w", "f_eph", "f_rng", "x", "v", "T"):
-            assert rel_err(a.get(k), b.get(k)) <= TOL, (k, rel_err(a.get(k), b.get(k)))
+            assert key_err(k, a.get(k), b.get(k)) <= TOL, (k, key_err(k, a.get(k), b.get(k)))
     assert a.pair_count() == b.pair_count()
     assert 1 <= a.counter("build") < 60
     assert a.counter("wrap") == b.counter("wrap")
@@ -109,7 +109,7 @@ def test_with_lanes_in_the_force_sweep(built, cascade):
     a.step(30)
     b.step(30)
     for k in ("rho", "w", "f_eph", "f_rng", "x", "v", "T"):
-        assert rel_err(a.get(k), b.get(k)) <= TOL, (k, rel_err(a.get(k), b.get(k)))
+        assert key_err(k, a.get(k), b.get(k)) <= TOL, (k, key_err(k, a.get(k), b.get(k)))
 
 
 def test_run_to_run_and_graph(built, cascade):
@@ -155,7 +155,7 @@ def test_hooks_with_host_positions(built, cascade):
         out.append(({k: h.get(k) for k in ("x", "v", "f", "f_eph", "f_rng", "rho", "T")}, h.counter("build")))
     (a, builds), (b, _) = out
     for k in a:
-        assert rel_err(a[k], b[k]) <= TOL, (k, rel_err(a[k], b[k]))
+        assert key_err(k, a[k], b[k]) <= TOL, (k, key_err(k, a[k], b[k]))
     assert 1 <= builds < 25
 
 

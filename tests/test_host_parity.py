@@ -9,7 +9,7 @@ import pytest
 
 import ephgb
 from ephgb import workloads as W
-from golden_io import GOLDEN
+from golden_io import GOLDEN, write_ref_input
 from oracle.bindings import RefBeta, RefGrid, oracle_lib, ref_available
 
 needs_ref = pytest.mark.skipif(not ref_available(), reason="reference build (oracle/_ref) absent")
@@ -37,18 +37,22 @@ def test_spline_tables_match_reference(built, beta_file_2el, which):
 
 
 @needs_ref
-def test_real_reference_beta_file(built):
-    """The reference's own Ni beta file (1001 rho knots, 50001 beta knots),
-    read where the reference tree is present."""
-    path = "/root/reference/Tests/MD_Run/Ni.beta"
-    if not os.path.exists(path):
-        pytest.skip("reference beta file absent")
+@pytest.mark.parametrize("name", ["MD_Run_Ni.beta", "Beta_zero_Ni.beta", "NiCoCrFe_PRB2019.beta"])
+def test_real_reference_beta_file(built, tmp_path, name):
+    """The reference's own beta files (Tests/MD_Run/Ni.beta: 1001 rho knots,
+    50001 beta knots; Tests/EPH_Beta_zero/Ni.beta; the four-element
+    NiCoCrFe file), kept under tests/golden/ref_inputs: host tables of every
+    element bit-identical to the reference's EPH_Beta."""
+    path = write_ref_input(name, str(tmp_path))
     b = ephgb.BetaFile(path)
     r = RefBeta(path)
-    for which, name in enumerate(("rho_r", "rho_r_sq", "beta", "alpha")):
-        assert np.array_equal(b.table(name, 0), r.table(which, 0)), name
-    xs = np.linspace(0, 0.999 * r.r_cutoff ** 2, 101)
-    assert np.array_equal(b.eval("rho_r_sq", 0, xs), r.eval(1, 0, xs))
+    nel = 4 if name.startswith("NiCoCrFe") else 1
+    for e in range(nel):
+        for which, tab in enumerate(("rho_r", "rho_r_sq", "beta", "alpha")):
+            assert np.array_equal(b.table(tab, e), r.table(which, e)), (tab, e)
+        xs = np.linspace(0, 0.999 * r.r_cutoff ** 2, 101)
+        assert np.array_equal(b.eval("rho_r_sq", e, xs), r.eval(1, e, xs))
+    assert b.rho_cutoff == r.rho_cutoff and b.r_cutoff == r.r_cutoff
 
 
 def test_spline_tables_match_oracle(built, beta_file):

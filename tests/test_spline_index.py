@@ -10,15 +10,14 @@ cubics differ by ~1e-8: beyond the 1e-12 parity bar for any atom such a
 pair touches (atoms do come that close in cascades).  So the FP32 index,
 measured 3 % faster in the density sweep, is not used.  Host tables only,
 no GPU."""
-import os
 
 import numpy as np
 import pytest
 
 import ephgb
 from ephgb import workloads as W
+from golden_io import write_ref_input
 
-REF_BETA = os.path.join(os.sep, "root", "reference", "Tests", "MD_Run", "Ni.beta")
 SLIP = 2.5e-7  # relative distance from a knot within which an FP32 index can slip
 
 
@@ -46,9 +45,9 @@ def test_synthetic_beta_file(tmp_path):
     assert gap.max() < 1e-14
 
 
-@pytest.mark.skipif(not os.path.exists(REF_BETA), reason="reference tree not present")
-def test_reference_ni_beta_needs_the_exact_index():
-    r, gap = neighbour_gaps(REF_BETA)
+def test_reference_ni_beta_needs_the_exact_index(tmp_path):
+    """Tests/MD_Run/Ni.beta, kept under tests/golden/ref_inputs."""
+    r, gap = neighbour_gaps(write_ref_input("MD_Run_Ni.beta", str(tmp_path)))
     assert gap[r >= 1.5].max() < 1e-14  # lattice distances: harmless
     # a lattice atom's density is ~0.05 (12 neighbours at 2.49 A, ~0.004 each):
     # near r = 0.16 A a slipped index would move it by far more than 1e-12

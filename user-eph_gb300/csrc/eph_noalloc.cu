@@ -15,6 +15,7 @@
 // or serialise them.  Nothing in the array has to start at zero: the
 // reduction slots and the ping-pong grid are fully written before they are
 // read.
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 
@@ -31,8 +32,10 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_fdm_scratch[EPH_NOALLOC_MAX_CELLS + 8];
 
 // Device address of g_fdm_scratch per device, filled on the first call on
-// that device (host code cannot use the symbol itself as an address).
-double *g_scratch_addr[kMaxDevices] = {nullptr};
+// that device (host code cannot use the symbol itself as an address).  Two
+// host threads making their first call on one device at once both look the
+// address up and store the same value.
+std::atomic<double *> g_scratch_addr[kMaxDevices];
 
 __global__ void k_noalloc_bounds(long ntotal, const double *__restrict__ C, const double *__restrict__ rho,
                                  const double *__restrict__ kappa, const signed char *__restrict__ flag,
@@ -118,13 +121,14 @@ extern "C" int eph_fdm_solve_noalloc(long nx, long ny, long nz, const double *lo
   if (ntotal > EPH_NOALLOC_MAX_CELLS) return EPH_ERR_CAPACITY;  // larger than the static scratch
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return EPH_ERR_CUDA;
-  if (!g_scratch_addr[dev]) {
+  double *scratch = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
     // set-up, once per device, with that device current
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_fdm_scratch) != cudaSuccess || !p) return EPH_ERR_CUDA;
-    g_scratch_addr[dev] = static_cast<double *>(p);
+    scratch = static_cast<double *>(p);
+    g_scratch_addr[dev].store(scratch, std::memory_order_release);
   }
-  double *scratch = g_scratch_addr[dev];
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // grid spacing as eph_fdm.h:127-146 computes it
   const double dx = (hi[0] - lo[0]) / (double)(size_t)nx;
@@ -136,13 +140,21 @@ extern "C" int eph_fdm_solve_noalloc(long nx, long ny, long nz, const double *lo
   if (cudaMemcpyAsync(b, scratch + EPH_NOALLOC_MAX_CELLS, sizeof b, cudaMemcpyDeviceToHost, st) != cudaSuccess)
     return EPH_ERR_CUDA;
   if (cudaStreamSynchronize(st) != cudaSuccess) return EPH_ERR_CUDA;
+  // the reference only asserts positive bounds; here a zero or negative C_e
+  // or rho_e (cell 0 enters the minimum whatever its flag) is an argument
+  // error, and so is a substep count above EPH_NOALLOC_MAX_SUBSTEPS, before
+  // anything is launched
+  if (!(b[0] > 0.0) || !(b[1] > 0.0) || !(b[2] >= 0.0)) return EPH_ERR_ARG;
+  if (steps > EPH_NOALLOC_MAX_SUBSTEPS) return EPH_ERR_ARG;
   double inner_dt = dt / (double)(size_t)steps;
   const double dtdxdydz = inner_dt * (1.0 / dx / dx + 1.0 / dy / dy + 1.0 / dz / dz);
   const double r = dtdxdydz / b[0] / b[1] * b[2];
   unsigned nsub = (unsigned)steps;
   if (r > 0.4) {
     inner_dt = 0.4 * inner_dt / r;
-    const unsigned s = (unsigned)(dt / inner_dt);
+    const double want = dt / inner_dt;
+    if (!(want < (double)EPH_NOALLOC_MAX_SUBSTEPS + 1.0)) return EPH_ERR_ARG;
+    const unsigned s = (unsigned)want;
     nsub = s > 1u ? s : 1u;
     inner_dt = dt / nsub;
   }

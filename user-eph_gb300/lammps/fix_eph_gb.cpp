@@ -6,9 +6,14 @@
  *   initial_integrate  x, v, f in   -> device integrate -> x, v out
  *   post_force         f in         -> bins, density, force_prl -> f out
  *   final_integrate    f in         -> device integrate -> v out
- *   end_of_step        (device)     -> deposition, FDM, T output; per-atom array out
- * After the engine re-neighbours (atoms may have moved between ranks or been
- * re-sorted) the whole atom set is uploaded again.
+ *   end_of_step        (device)     -> deposition, FDM, T output; per-atom array
+ *                                      out on steps that are multiples of
+ *                                      peratom_freq (`fix_modify ID peratom N`,
+ *                                      default 1: every step, as the reference)
+ * post_force needs no x or v: between initial_integrate (which copied them
+ * back) and post_force the engine changes them only when it re-neighbours
+ * (wraps, re-sorts or migrates atoms), and after that the whole atom set is
+ * uploaded again.
  */
 #include "fix_eph_gb.h"
 
@@ -89,6 +94,8 @@ void FixEPHGB::create_context() {
   md.device = device;
   md.mode = mode;
   check(eph_create((int)words.size(), words.data(), &md, &ctx), "create");
+  // a list skin set by fix_modify outlives contexts made by later fix_modify words
+  if (list_skin >= 0.0) check(eph_set_list_skin(ctx, list_skin), "list skin");
   nlocal_dev = -1;
 }
 
@@ -113,7 +120,16 @@ int FixEPHGB::modify_param(int narg, char **arg) {
   } else if (strcmp(arg[0], "device") == 0) {
     device = atoi(arg[1]);
   } else if (strcmp(arg[0], "list_skin") == 0) {
-    check(eph_set_list_skin(ctx, atof(arg[1])), "list skin");
+    list_skin = atof(arg[1]);
+    check(eph_set_list_skin(ctx, list_skin), "list skin");
+    return 2;
+  } else if (strcmp(arg[0], "peratom") == 0) {
+    // computes, dumps and variables read the per-atom array only on steps
+    // that are multiples of peratom_freq (the engine checks), so it is
+    // copied back only then
+    const int every = atoi(arg[1]);
+    if (every < 1) error->all(FLERR, "fix_modify eph/gb peratom: N must be >= 1");
+    peratom_freq = every;
     return 2;
   } else {
     return 0;
@@ -146,11 +162,14 @@ void FixEPHGB::initial_integrate(int) {
 }
 
 void FixEPHGB::post_force(int) {
-  // the engine re-neighboured this step: atoms may be re-sorted or wrapped
-  if (neighbor->ago == 0 || nlocal_dev != atom->nlocal) upload_atoms();
-  check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "put x");
-  check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST_ASYNC), "put v");
-  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
+  // the engine re-neighboured this step: atoms may be re-sorted or wrapped,
+  // so all of them go up again (x, v, type, mask and f); otherwise the device
+  // holds this step's x and v since initial_integrate and only the force the
+  // engine computed since then goes up
+  if (neighbor->ago == 0 || nlocal_dev != atom->nlocal)
+    upload_atoms();
+  else
+    check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
   int source = EPH_XI_DEVICE_RNG;
   if (xi_on_host && (eph_flag & 0x02)) {
     // the engine's own Gaussian stream, three per in-group atom in atom
@@ -178,7 +197,8 @@ void FixEPHGB::end_of_step() {
   check(eph_set_timestep(ctx, (long)update->ntimestep), "set timestep");
   if (eph_flag & 0x08) check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "put v");
   check(eph_end_of_step(ctx), "end_of_step");
-  check(eph_get(ctx, EPH_FIELD_PERATOM, &array[0][0], EPH_HOST), "get per-atom array");
+  if (update->ntimestep % peratom_freq == 0)
+    check(eph_get(ctx, EPH_FIELD_PERATOM, &array[0][0], EPH_HOST), "get per-atom array");
 }
 
 void FixEPHGB::reset_dt() {

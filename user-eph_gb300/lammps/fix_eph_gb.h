@@ -15,7 +15,10 @@
  * fix_modify options: `mode exact|fast` (EPH_MODE_*), `xi host|device`
  * (deviates from the engine's RanMars stream on the host, or the device
  * Philox generator), `device N`, `list_skin S` (skin of the kept candidate
- * lists in distance units, 0: search the bins every step).
+ * lists in distance units, 0: search the bins every step), `peratom N` (copy
+ * the per-atom array back only on steps that are multiples of N and declare
+ * peratom_freq = N, so that the engine lets computes, dumps and variables
+ * read it only then; default 1, every step, as the reference).
  * One MPI rank per GPU holding every atom of the box (the device builds its
  * own periodic minimum-image neighbour pairs, so no ghost communication).
  */
@@ -63,6 +66,7 @@ class FixEPHGB : public Fix {
   int xi_on_host = 0;
   int device = 0;
   int nlocal_dev = -1;            // atom count the device holds
+  double list_skin = -1.0;        // fix_modify list_skin (negative: the library's default)
   bigint last_upload_step = -1;   // step of the last full atom upload
   class RanMars *random = nullptr;
   std::vector<double> xi;  // deviates drawn on the host (xi host)
