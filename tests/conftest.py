@@ -23,17 +23,18 @@ def built():
 
 @pytest.fixture(scope="session")
 def beta_file(tmp_path_factory):
-    from ephgb import workloads as W
+    """The synthetic beta file (ephgb.workloads.write_beta_file), the bytes
+    the golden fixtures were made from, so every host tests the same knots."""
+    from golden_io import write_synthetic_beta
 
-    return W.write_beta_file(str(tmp_path_factory.mktemp("beta") / "synth.beta"))
+    return write_synthetic_beta("synth.beta", str(tmp_path_factory.mktemp("beta")))
 
 
 @pytest.fixture(scope="session")
 def beta_file_2el(tmp_path_factory):
-    from ephgb import workloads as W
+    from golden_io import write_synthetic_beta
 
-    return W.write_beta_file(str(tmp_path_factory.mktemp("beta2") / "NiFe.beta"), elements=("Ni", "Fe"),
-                             numbers=(28, 26))
+    return write_synthetic_beta("NiFe.beta", str(tmp_path_factory.mktemp("beta2")))
 
 
 def pytest_collection_modifyitems(config, items):

@@ -14,11 +14,13 @@ compiled unchanged with the engine stand-in) must exist.  Writes:
                        fixtures of REF_SCEN read (beta files, a grid file, a
                        data file, an eam/alloy file), xz-compressed byte for
                        byte, so that hosts without the reference tree run them
+  synth.beta.xz,       the synthetic beta files the fixtures were made from
+  NiFe.beta.xz         (ephgb.workloads.write_beta_file), kept byte for byte:
+                       numpy's exp may round its last bit differently on
+                       another host, so they are not regenerated there
   beta_tables.npz      the reference splines of the synthetic beta file
   fdm_test1.npz        the reference's own FDM golden vectors
                        (Tests/EPH_FDM/Test1/Out_Ref/T_out_*: x and T_e columns)
-The synthetic beta file is regenerated from its formula by every user, so
-only the knots' provenance (ephgb.workloads.write_beta_file) is recorded.
 """
 import lzma
 import math
@@ -216,6 +218,9 @@ def main():
     with tempfile.TemporaryDirectory() as tmp:
         bf = W.write_beta_file(os.path.join(tmp, "synth.beta"))
         bf2 = W.write_beta_file(os.path.join(tmp, "NiFe.beta"), elements=("Ni", "Fe"), numbers=(28, 26))
+        for path in (bf, bf2):
+            with open(os.path.join(HERE, os.path.basename(path) + ".xz"), "wb") as f:
+                f.write(lzma.compress(open(path, "rb").read(), preset=9))
         for name in SCEN:
             fix_fixture(name, bf, bf2)
         for name in REF_FILES:

@@ -38,18 +38,26 @@ def write_ref_input(name, tmpdir):
     return path
 
 
+def write_synthetic_beta(name, tmpdir):
+    """Write the synthetic beta file `name` ("synth.beta" or "NiFe.beta") the
+    fixtures were made from (ephgb.workloads.write_beta_file on the host that
+    made them, kept byte for byte) into tmpdir; returns its path."""
+    path = os.path.join(tmpdir, name)
+    with open(os.path.join(GOLDEN, name + ".xz"), "rb") as f, open(path, "wb") as out:
+        out.write(lzma.decompress(f.read()))
+    return path
+
+
 def load_fix(name, tmpdir):
-    """(words, atoms, dt, record): the synthetic beta file is regenerated in
-    tmpdir, the reference's input files are unpacked there, and the output
+    """(words, atoms, dt, record): the beta file (synthetic or the
+    reference's) and the grid file are unpacked into tmpdir, and the output
     file word points there too."""
     d = np.load(os.path.join(GOLDEN, f"fix_{name}.npz"))
     words = [str(w) for w in d["words"]]
-    if words[16] == "NiFe.beta":
-        words[16] = W.write_beta_file(os.path.join(tmpdir, "NiFe.beta"), elements=("Ni", "Fe"), numbers=(28, 26))
-    elif words[16] in REF_FILES:
+    if words[16] in REF_FILES:
         words[16] = write_ref_input(words[16], tmpdir)
     else:
-        words[16] = W.write_beta_file(os.path.join(tmpdir, words[16]))
+        words[16] = write_synthetic_beta(words[16], tmpdir)
     if words[13] in REF_FILES:
         words[13] = write_ref_input(words[13], tmpdir)
     words[15] = os.path.join(tmpdir, words[15])
