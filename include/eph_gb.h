@@ -182,6 +182,19 @@ int eph_get_threads_per_atom(eph_ctx *ctx, int *tpa);
  * fastest; *chosen gets it (may be NULL). */
 int eph_autotune(eph_ctx *ctx, int *chosen);
 
+/* Arithmetic of the FAST-mode per-pair work where the density sweep runs
+ * one lane per atom with stage 1 folded (16,384 atoms and more, bin search):
+ * EPH_PAIRS_DF64 (the default) forms every pair term and its sums in
+ * double-float -- pairs of FP32 numbers carrying 48 significand bits, on the
+ * FP32 pipe, which GB300 issues at 64 times its FP64 rate -- and keeps the
+ * per-atom work (beta, alpha, the integrator, the grid) in FP64;
+ * EPH_PAIRS_FP64 keeps the pair terms in FP64 as well.  Results agree with
+ * the reference within the FAST bar (1e-12 relative per atom) either way;
+ * the last bits differ.  No reference counterpart. */
+#define EPH_PAIRS_FP64 0
+#define EPH_PAIRS_DF64 1
+int eph_set_pair_arithmetic(eph_ctx *ctx, int which);
+
 /* Skin s of the kept candidate lists (Angstrom; default 0.3, used from 2^15
  * to 2^20 atoms, where it pays; a skin set here applies at any size, 0 turns
  * the lists off).  The reference takes its pairs from the engine's Verlet list

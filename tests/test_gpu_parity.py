@@ -212,3 +212,41 @@ def test_async_host_copies(built, beta_file):
         out.append((x.copy(), v.copy(), f.copy(), fix.get("T")))
     for a, b in zip(out[0], out[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("two_el", [False, True])
+def test_df64_pair_sums_against_oracle_and_fp64(built, beta_file, beta_file_2el, two_el):
+    """The FAST one-lane sweeps with df64 pair arithmetic (the default from
+    16,384 atoms on) against the oracle, and against the same sweeps in FP64
+    (eph_set_pair_arithmetic): 16^3 fcc cells with a 3 keV knock-on atom, one
+    and two elements (the second: H_ij != H_ji, two rho(r^2) tables), 4 steps,
+    1e-12 per atom."""
+    at = W.fcc_lattice(16, seed=31)
+    W.add_pka(at, 3000.0, seed=32)
+    if two_el:
+        at.type = np.where(np.arange(at.n) % 3 == 1, 2, 1).astype(np.int32)
+        at.mass = np.array([0.0, W.NI_MASS, 55.845])
+        words = W.fix_args(beta_file_2el, grid=(8, 8, 8), elements=("Ni", "Fe"))
+    else:
+        words = W.fix_args(beta_file, grid=(8, 8, 8))
+    dt = 0.0005
+    fixes = {}
+    for arith in (ephgb.PAIRS_DF64, ephgb.PAIRS_FP64):
+        fx = ephgb.FixEPH(words, at, dt=dt, mode=ephgb.MODE_FAST)
+        fx.set_list_skin(0.0)  # the bin search every step (the df64 sweeps' path)
+        fx.set_pair_arithmetic(arith)
+        fixes[arith] = fx
+    ref = OracleFix(words, at, dt)
+    ng = n_in_group(at)
+    for s in range(4):
+        stream = W.gaussian_stream(ng, 5, s)
+        for fx in fixes.values():
+            fx.step(1, xi=xi_rows(at, stream))
+        ref.step(stream)
+        for k in ATOM_KEYS:
+            a, b, o = fixes[ephgb.PAIRS_DF64].get(k), fixes[ephgb.PAIRS_FP64].get(k), ref.get(k)
+            assert key_err(k, a, o) <= TOL, (s, k, key_err(k, a, o))
+            assert key_err(k, a, b) <= TOL, (s, k, key_err(k, a, b))
+        assert atom_err(fixes[ephgb.PAIRS_DF64].get("T"), ref.get("T")) <= TOL
+    # the two arithmetics really ran different kernels: their last bits differ
+    assert not np.array_equal(fixes[ephgb.PAIRS_DF64].get("f_eph"), fixes[ephgb.PAIRS_FP64].get("f_eph"))

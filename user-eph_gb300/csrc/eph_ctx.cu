@@ -25,6 +25,7 @@ namespace ephgb {
 namespace ctxi {
 
 bool fused_friction(const eph_ctx *c);
+bool df_active(const eph_ctx *c);
 
 // pg rows per pair: {rho_j(r^2), rho_i(r^2)} in EXACT mode, {rho_i(r^2)/r^2, 0}
 // in FAST mode with several elements, the y and z of H e with one element
@@ -61,6 +62,45 @@ int upload_tables(eph_ctx *c) {
   CUDA_TRY(c, up(c->tab_rho_r_sq, EPH_SPLINE_RHO_R_SQ, b.n_rho));
   CUDA_TRY(c, up(c->tab_beta, EPH_SPLINE_BETA, b.n_beta));
   CUDA_TRY(c, up(c->tab_alpha, EPH_SPLINE_ALPHA, b.n_beta));
+  // the rho(r^2) tables for the df64 density sweep: each interval's cubic
+  // a + b x + c x^2 + d x^3 (the reference's absolute form) re-expanded about
+  // the knot X_k the device forms (k dx as a double-float product) in long
+  // double: a' = a + X (b + X (c + X d)), b' = b + X (2c + 3 d X),
+  // c' = c + 3 d X, d' = d; each split into FP32 hi and lo parts
+  {
+    const long nk = b.n_rho;
+    const double dx = 1.0 / b.rho_r_sq[0].inv_dx;
+    const float dx_hi = (float)dx, dx_lo = (float)(dx - (double)dx_hi);
+    c->P.dxr_hi = dx_hi;
+    c->P.dxr_lo = dx_lo;
+    c->P.inv_dxr_f = (float)b.rho_r_sq[0].inv_dx;
+    std::vector<float4> h((size_t)b.n_elements * nk * 2);
+    for (int e = 0; e < b.n_elements; ++e) {
+      const Spline &sp = b.table(EPH_SPLINE_RHO_R_SQ, e);
+      for (long k = 0; k < nk; ++k) {
+        const float kr = (float)k;
+        const float p = kr * dx_hi;
+        float pe = std::fma(kr, dx_hi, -p);
+        pe = std::fma(kr, dx_lo, pe);
+        const long double X = (long double)p + (long double)pe;
+        const long double a = sp.c[4 * k], bb = sp.c[4 * k + 1], cc = sp.c[4 * k + 2], d = sp.c[4 * k + 3];
+        const long double q[4] = {a + X * (bb + X * (cc + X * d)), bb + X * (2 * cc + 3 * d * X), cc + 3 * d * X, d};
+        float hi[4], lo[4];
+        for (int m = 0; m < 4; ++m) {
+          hi[m] = (float)q[m];
+          lo[m] = (float)(q[m] - (long double)hi[m]);
+        }
+        h[2 * ((size_t)e * nk + k)] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        h[2 * ((size_t)e * nk + k) + 1] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+      }
+    }
+    if (c->tab_rho_df.n != h.size()) {
+      c->buf_gen += 1;
+      CUDA_TRY(c, c->tab_rho_df.alloc(h.size()));
+    }
+    CUDA_TRY(c, cudaMemcpy(c->tab_rho_df.p, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    c->P.tab_rho_df = c->tab_rho_df.p;
+  }
   return EPH_OK;
 }
 
@@ -205,6 +245,14 @@ bool fused_friction(const eph_ctx *c) {
   return c->mode == EPH_MODE_FAST && c->args.model == 4 && (c->P.flags & FLAG_FRICTION) && c->fuse_w;
 }
 
+// FAST pair sums in df64: the one-lane density sweep with stage 1 folded
+// and the bin search (k_density_df, then k_forces_df at any lanes per atom),
+// bins of at most 1022 per axis (k_bin packs them in 10 bits each)
+bool df_active(const eph_ctx *c) {
+  return c->pair_arith == EPH_PAIRS_DF64 && c->mode == EPH_MODE_FAST && fused_friction(c) && !c->reuse &&
+         !(c->tpa > 1 && c->n < 16384) && c->P.nb[0] <= 1022 && c->P.nb[1] <= 1022 && c->P.nb[2] <= 1022;
+}
+
 template <bool FAST, bool MULTI, bool FUSE>
 void launch_density_f(eph_ctx *c, int xi_mode) {
   // several lanes per atom in the density sweep too below 16,384 atoms, where
@@ -236,6 +284,17 @@ void launch_density_f(eph_ctx *c, int xi_mode) {
       return;
     }
   }
+  if constexpr (FAST && FUSE) {
+    if (df_active(c)) {
+      float4 *pa = reinterpret_cast<float4 *>(c->pe.p), *pb = pa + (size_t)c->kcap * c->n;
+      k_density_df<MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+          c->P, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->dfrec.p, c->dfvrec.p, c->x.p,
+          c->xi.p, xi_mode, c->T0.p, c->pj.p, pa, pb, reinterpret_cast<float4 *>(c->pg.p), c->nshort.p, c->A.p,
+          c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p, c->wrapflag.p, c->d_err.p, c->counters.p, c->v.p,
+          c->Mm.p, c->G.p);
+      return;
+    }
+  }
   k_density<FAST, MULTI, FUSE><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
       c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p,
       c->pj.p, c->pe.p, c->pg.p, c->nshort.p, c->A.p, c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p,
@@ -251,6 +310,20 @@ void launch_density_t(eph_ctx *c, int xi_mode) {
 template <bool FAST, bool MULTI, bool FRIC, bool RAND>
 void launch_forces_t(eph_ctx *c) {
   const int tpa = FAST ? c->tpa : 1;
+  if (FAST && FRIC && df_active(c)) {
+    const float4 *pa = reinterpret_cast<const float4 *>(c->pe.p), *pb = pa + (size_t)c->kcap * c->n;
+#define EPH_FORCES_DF(T)                                                                                          \
+  k_forces_df<MULTI, RAND, T><<<nblocks((long)c->n * T), BLOCK, 0, c->stream>>>(                                   \
+      c->P, c->pj.p, pa, pb, reinterpret_cast<const float4 *>(c->pg.p), c->nshort.p, c->Mm.p,                    \
+      reinterpret_cast<const float4 *>(c->G.p), c->A.p, c->Bw.p, c->Te_i.p, c->f.p, c->f_eph.p, c->f_rng.p,       \
+      c->f_dis.p, c->f_sto.p)
+    if (tpa == 1) EPH_FORCES_DF(1);
+    else if (tpa == 2) EPH_FORCES_DF(2);
+    else if (tpa == 4) EPH_FORCES_DF(4);
+    else EPH_FORCES_DF(8);
+#undef EPH_FORCES_DF
+    return;
+  }
   if (FAST && FRIC && fused_friction(c)) {
 #define EPH_FORCES_M(T)                                                                                      \
   k_forces_m<MULTI, RAND, T><<<nblocks((long)c->n * T), BLOCK, 0, c->stream>>>(                               \
@@ -299,6 +372,8 @@ int set_bin_geometry(eph_ctx *c, double r) {
     c->P.w[k] = c->prd[k] / nb[k];
     c->P.inv_w[k] = 1.0 / c->P.w[k];
     c->P.wf[k] = (float)c->P.w[k];
+    c->P.w_hi[k] = (float)c->P.w[k];
+    c->P.w_lo[k] = (float)(c->P.w[k] - (double)c->P.w_hi[k]);
   }
   c->nbins = nb[0] * nb[1] * nb[2];
   return EPH_OK;
@@ -454,8 +529,10 @@ int launch_bin(eph_ctx *c) {
   }
   ps.launched();
   CUDA_TRY(c, cudaMemsetAsync(c->bin_count.p, 0, sizeof(int) * (size_t)c->nbins, c->stream));
+  const bool df = df_active(c);
   k_bin<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->bin_count.p, c->bins.p,
-                                     c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 1);
+                                     c->atom_bin.p, c->atom_off.p, c->d_err.p, c->counters.p, 1, nullptr, nullptr,
+                                     df ? c->dfrec.p : nullptr, df ? c->dfvrec.p : nullptr, c->v.p);
   ps.launched();
   // a warp per bin where the bins are few (the sort's latency shows), a
   // thread per bin where they are many (measured on GB300: 343 bins 20 ->
@@ -836,6 +913,8 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
   }
   P.rc2 = c->beta.r_cutoff_sq;
   P.rc2_band = (float)(c->beta.r_cutoff_sq * (1.0 + 1e-4));
+  P.rc2_hi = (float)P.rc2;
+  P.rc2_lo = (float)(P.rc2 - (double)P.rc2_hi);
   P.tab_rho_r_sq = c->tab_rho_r_sq.p;
   P.tab_beta = c->tab_beta.p;
   P.tab_alpha = c->tab_alpha.p;
@@ -907,6 +986,16 @@ int eph_set_threads_per_atom(eph_ctx *c, int tpa) {
   c->tpa_auto = tpa == 0;
   c->tpa = tpa == 0 ? auto_tpa(c->n) : tpa;
   return c->n > 0 ? configure_list(c) : EPH_OK;
+}
+
+int eph_set_pair_arithmetic(eph_ctx *c, int which) {
+  if (!c) return EPH_ERR_ARG;
+  if (which != EPH_PAIRS_FP64 && which != EPH_PAIRS_DF64)
+    return fail(c, EPH_ERR_ARG, "pair arithmetic: EPH_PAIRS_FP64 or EPH_PAIRS_DF64");
+  drop_graph(c);
+  c->buf_gen += 1;  // graphs captured elsewhere hold the old kernels
+  c->pair_arith = which;
+  return EPH_OK;
 }
 
 int eph_set_list_skin(eph_ctx *c, double skin) {
@@ -1041,6 +1130,8 @@ int eph_set_atoms(eph_ctx *c, int n, const double *hx, const double *hv, const i
     CUDA_TRY(c, c->stage.alloc(8 * N));
     CUDA_TRY(c, c->atom_bin.alloc(N));
     CUDA_TRY(c, c->atom_off.alloc(N));
+    CUDA_TRY(c, c->dfrec.alloc(2 * N));
+    CUDA_TRY(c, c->dfvrec.alloc(2 * N));
     CUDA_TRY(c, c->part.alloc((size_t)nblocks(n, 256)));
     if (c->fext.p) CUDA_TRY(c, c->fext.alloc(N));
     // capacities from the number density: a bin holds ~density*w^3 atoms, the

@@ -101,6 +101,12 @@ struct eph_ctx {
   DevBuf<D4> xref;  // positions at the last build
 
   DevBuf<D4> tab_rho_r_sq, tab_beta, tab_alpha;
+  // FAST pair sums in df64 (eph_set_pair_arithmetic, on by default): the
+  // rho(r^2) tables in local form (two float4 per knot) and the per-atom
+  // records k_bin writes for them (bin offset and bin, velocity: two float4
+  // each per atom)
+  int pair_arith = EPH_PAIRS_DF64;
+  DevBuf<float4> tab_rho_df, dfrec, dfvrec;
 
   DevBuf<double> T0, T1, kappa, rhoC, irhoC, S, dT;
   // temperature-dependent cells: per-cell C_e and rho_e, the parameter tables

@@ -62,6 +62,15 @@ struct StepParams {
   double half_prd[3];
   float half_prdf[3];
   int lcap;           // rows of the candidate list
+  // FAST pair sums in df64 (k_density_df, k_forces_df): the bin widths, the
+  // cut-off and the rho(r^2) knot spacing as double-floats (hi, lo), and the
+  // rho(r^2) tables in local form about each knot (two float4 per knot:
+  // hi and lo parts of a', b', c', d' with y = a' + t (b' + t (c' + t d')),
+  // t = x - k dx)
+  float w_hi[3], w_lo[3];
+  float rc2_hi, rc2_lo;
+  float dxr_hi, dxr_lo, inv_dxr_f;
+  const float4 *tab_rho_df;
   // splines: tables of element e start at e * n_knots
   const D4 *tab_rho_r_sq;
   const D4 *tab_beta;

@@ -15,6 +15,7 @@
 #pragma once
 
 #include "eph_device.cuh"
+#include "eph_df64.cuh"
 
 namespace ephgb {
 
@@ -108,11 +109,17 @@ __device__ __forceinline__ void wrap_into_box(const StepParams &P, D4 &xi) {
 // (unwrapped) bin corner.
 // With a gate (candidate-list reuse): nothing unless *gate (a build step),
 // no wrap (k_list_check did it), and the positions are kept in xref.
+// With rec (the df64 pair sums), also the atom's records for them: rec[2i] =
+// {offset in its bin, hi parts; bin + 1 packed 10 bits per axis},
+// rec[2i+1] = {offset, lo parts; element}, vrec[2i], vrec[2i+1] = velocity,
+// hi and lo parts.  The offset is x - lo - b w with one rounding; a pair's
+// displacement is then d w + (o_j - o_i), d the bin difference.
 __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, const int *__restrict__ wrapflag,
                       int *__restrict__ bin_count, BinEntry *__restrict__ bins, int4 *__restrict__ atom_bin,
                       float4 *__restrict__ atom_off, unsigned *__restrict__ err,
                       unsigned long long *__restrict__ counters, int bump_step, const int *__restrict__ gate = nullptr,
-                      D4 *__restrict__ xref = nullptr) {
+                      D4 *__restrict__ xref = nullptr, float4 *__restrict__ rec = nullptr,
+                      float4 *__restrict__ vrec = nullptr, const D4 *__restrict__ v = nullptr) {
   if (gate && !*gate) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0 && bump_step) *P.step += 1ull;  // read by the density sweep that follows
@@ -156,6 +163,23 @@ __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, 
   }
   atom_bin[i] = make_int4(B[0], B[1], B[2], flat);
   atom_off[i] = make_float4(o[0], o[1], o[2], 0.f);
+  if (rec) {
+    float oh[3], ol[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double o64 = fma(-(double)B[k], P.w[k], p[k] - P.lo[k]);
+      oh[k] = (float)o64;
+      ol[k] = (float)(o64 - (double)oh[k]);
+    }
+    const unsigned packed = (unsigned)(B[0] + 1) | ((unsigned)(B[1] + 1) << 10) | ((unsigned)(B[2] + 1) << 20);
+    rec[2 * (size_t)i] = make_float4(oh[0], oh[1], oh[2], __uint_as_float(packed));
+    rec[2 * (size_t)i + 1] = make_float4(ol[0], ol[1], ol[2], __int_as_float((int)xi.w));
+    const D4 vi = v[i];
+    const float vh[3] = {(float)vi.x, (float)vi.y, (float)vi.z};
+    vrec[2 * (size_t)i] = make_float4(vh[0], vh[1], vh[2], 0.f);
+    vrec[2 * (size_t)i + 1] = make_float4((float)(vi.x - (double)vh[0]), (float)(vi.y - (double)vh[1]),
+                                          (float)(vi.z - (double)vh[2]), 0.f);
+  }
 }
 
 // -------------------------------------------------------- density sweep
@@ -360,7 +384,12 @@ __device__ __forceinline__ void density_vector(const StepParams &P, const D4 &xi
 
 // The end of the density sweep for atom i (its pairs summed): alpha, beta,
 // the deviates, its grid cell and T_e, and the per-atom records.
-template <bool FAST, bool FUSE_W>
+// With DFG (the df64 force sweep follows) the gathered records go to G as
+// double-floats, three float4 per atom: {W hi, X_x hi}, {W lo, X_x lo},
+// {X_y hi, X_z hi, X_y lo, X_z lo} (W = a_i w_i, X = a_i xi_i); an atom the
+// reference skips as a neighbour (rho <= 0 or outside the group) is marked
+// by a NaN in its first word.
+template <bool FAST, bool FUSE_W, bool DFG = false>
 __device__ __forceinline__ void density_epilogue(
     const StepParams &P, int i, bool active, const D4 &xi, int ei, double rho, int ns, double mxx, double mxy,
     double mxz, double myy, double myz, double mzz, double Sx, double Sy, double Sz,
@@ -412,8 +441,20 @@ __device__ __forceinline__ void density_epilogue(
     Bw[i] = D4{xi3[2], wx, wy, wz};
     Mm[i] = D4{mxx, mxy, mxz, myy};
     Mm[(size_t)P.n + i] = D4{myz, mzz, 0.0, 0.0};
-    G[2 * (size_t)i] = D4{alpha * wx, alpha * wy, alpha * wz, alpha * xi3[0]};
-    G[2 * (size_t)i + 1] = D4{alpha * xi3[1], alpha * xi3[2], active ? rho : 0.0, 0.0};
+    if (DFG) {
+      const df64::df W[3] = {df64::from_double(alpha * wx), df64::from_double(alpha * wy),
+                             df64::from_double(alpha * wz)};
+      const df64::df X[3] = {df64::from_double(alpha * xi3[0]), df64::from_double(alpha * xi3[1]),
+                             df64::from_double(alpha * xi3[2])};
+      const bool live = active && pos_double(rho);
+      float4 *g = reinterpret_cast<float4 *>(G) + 3 * (size_t)i;
+      g[0] = make_float4(live ? W[0].hi : __int_as_float(0x7fc00000), W[1].hi, W[2].hi, X[0].hi);
+      g[1] = make_float4(W[0].lo, W[1].lo, W[2].lo, X[0].lo);
+      g[2] = make_float4(X[1].hi, X[2].hi, X[1].lo, X[2].lo);
+    } else {
+      G[2 * (size_t)i] = D4{alpha * wx, alpha * wy, alpha * wz, alpha * xi3[0]};
+      G[2 * (size_t)i + 1] = D4{alpha * xi3[1], alpha * xi3[2], active ? rho : 0.0, 0.0};
+    }
   } else {
     Bw[i] = D4{xi3[2], 0.0, 0.0, 0.0};
   }
@@ -508,6 +549,210 @@ __global__ void __launch_bounds__(128) k_density(
   if (!valid) return;
   density_epilogue<FAST, FUSE_W>(P, i, active, xi, ei, rho, ns, mxx, mxy, mxz, myy, myz, mzz, Sx, Sy, Sz, xi_given,
                                  xi_mode, T_e, nshort, A, Bw, rho_out, beta_out, cell, Te_i, err, counters, v, Mm, G);
+}
+
+// ------------------------------------------- FAST pair sweeps in df64
+
+// resident blocks of 128 threads per SM the df64 sweeps are compiled for
+// (their register budget: 65,536 / (128 x blocks)); measured on GB300 at
+// 2,048,000 atoms: density 6 and 7 alike, 8 spills and is 17 % slower;
+// forces 6 / 7 / 8: 1.51 / 1.36 / 1.50 ms
+#ifndef EPH_DF_DENSITY_BLOCKS
+#define EPH_DF_DENSITY_BLOCKS 6
+#endif
+#ifndef EPH_DF_FORCES_BLOCKS
+#define EPH_DF_FORCES_BLOCKS 7
+#endif
+// candidates per iteration of the df64 density sweep's pass 2
+#ifndef DF_UNROLL
+#define DF_UNROLL 2
+#endif
+
+// rho_e(x) of element e at x = r^2 from the local-form df64 table: knot
+// k = floor(x / dx) from the FP32 quotient, moved by one where the df64
+// offset t = x - k dx falls outside [0, dx) (so the interval is that of the
+// df64 x, not of its FP32 part), then y = a' + t (b' + t (c' + t d')).  The
+// local form was expanded from the reference's absolute-form cubic on the
+// host (the same polynomial), so the value is the reference's spline to
+// ~1e-14 without the cancellation of evaluating the absolute form at large x.
+__device__ __forceinline__ df64::df spline_rho_df(const StepParams &P, int e, df64::df x, unsigned *err) {
+  using namespace df64;
+  const float q = x.hi * P.inv_dxr_f;
+  // floor(q) for 0 <= q < 2^22 by the 2^23 rounding trick (no conversion
+  // instruction); ties and slips are settled by the sign of t below
+  const float kr = ((q - 0.5f) + 8388608.0f) - 8388608.0f;
+  int k = (int)__float_as_int(kr + 8388608.0f) - 0x4B000000;
+  float p, pe;
+  two_prod(kr, P.dxr_hi, p, pe);
+  pe = fmaf(kr, P.dxr_lo, pe);
+  float th, te;
+  two_sum(x.hi, -p, th, te);
+  df t = make(th, (te + x.lo) - pe);
+  const df dx = df{P.dxr_hi, P.dxr_lo};
+  if (t.hi < 0.0f) {
+    k -= 1;
+    t = add(t, dx);
+  } else if (!(t.hi < P.dxr_hi)) {
+    k += 1;
+    t = sub(t, dx);
+  }
+  if (k < 0 || k >= P.n_rho) {
+    atomicOr(err, ERR_SPLINE_RANGE);
+    k = k < 0 ? 0 : P.n_rho - 1;
+  }
+  const float4 *c = P.tab_rho_df + 2 * ((size_t)e * P.n_rho + k);
+  const float4 hi = c[0], lo = c[1];
+  return horner(df{hi.x, lo.x}, df{hi.y, lo.y}, df{hi.z, lo.z}, df{hi.w, lo.w}, t);
+}
+
+// displacement component d w + (o_j - o_i) of a pair from the bin offsets
+__device__ __forceinline__ df64::df pair_disp(int d, float ojh, float ojl, float oih, float oil, float wh,
+                                              float wl) {
+  using namespace df64;
+  float s, se;
+  two_sum(ojh, -oih, s, se);
+  const float dw = (float)d * wh;  // exact: d is -1, 0 or 1
+  float s2, se2;
+  two_sum(s, dw, s2, se2);
+  return make(s2, ((ojl - oil) + se) + (se2 + (float)d * wl));
+}
+
+// The FAST density sweep of k_density<true, MULTI, true> (one lane per atom,
+// stage 1 and M_i folded) with every per-pair operation in df64 on the FP32
+// pipe: pass 1 is k_density's; pass 2 forms e = d w + (o_j - o_i) from the
+// atoms' bin offsets (k_bin's records, 48 significant bits), r^2, the exact
+// cut-off test, rho_j(r^2) (spline_rho_df), H = rho_j(r^2) / r^2 (a df64
+// Newton reciprocal), H e, and the sums of M_i and S_i (blocked df64 sums,
+// folded every 8 candidates); the epilogue is k_density's in FP64 and writes
+// the records G for k_forces_df.  Pair cache (row k of atom i at k*n + i):
+// pa = {e hi, (H e)_x hi | H_ji hi}, pb = the lo parts, pc = {(H e)_y, (H e)_z}
+// hi, hi, lo, lo with one element, {H_ij hi, H_ij lo} with several.
+template <bool MULTI>
+__global__ void __launch_bounds__(128, EPH_DF_DENSITY_BLOCKS) k_density_df(
+    StepParams P, const int *__restrict__ mask, const int *__restrict__ bin_count, const BinEntry *__restrict__ bins,
+    const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off, const float4 *__restrict__ rec,
+    const float4 *__restrict__ vrec, const D4 *__restrict__ x, const D4 *__restrict__ xi_given, int xi_mode,
+    const double *__restrict__ T_e, unsigned *__restrict__ pj, float4 *__restrict__ pa, float4 *__restrict__ pb,
+    float4 *__restrict__ pc, int *__restrict__ nshort, D4 *__restrict__ A, D4 *__restrict__ Bw,
+    double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell, double *__restrict__ Te_i,
+    int *__restrict__ wrapflag, unsigned *__restrict__ err, unsigned long long *__restrict__ counters,
+    const D4 *__restrict__ v, D4 *__restrict__ Mm, D4 *__restrict__ G) {
+  using namespace df64;
+  __shared__ unsigned s_cand[CAND_SMEM * 128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
+  if (i == 0) *wrapflag = 0;  // the binning kernel has read it
+  const bool valid = i < P.n;
+  const bool active = valid && (mask[i] & P.groupbit) != 0;
+  auto cget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : pj[(size_t)k * P.n + i]; };
+  auto cset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM)
+      s_cand[k * nt + t] = u;
+    else
+      pj[(size_t)k * P.n + i] = u;
+  };
+  int4 Bi = make_int4(0, 0, 0, 0);
+  float4 oi = make_float4(0.f, 0.f, 0.f, 0.f), Ri1 = make_float4(0.f, 0.f, 0.f, 0.f);
+  int ns = 0, nc = 0;
+  if (valid) {
+    Bi = atom_bin[i];
+    oi = rec[2 * (size_t)i];
+    Ri1 = rec[2 * (size_t)i + 1];
+  }
+  const int ei = __float_as_int(Ri1.w);
+  // pass 1: candidates, FP32/integer work only, warp-uniform loop bounds
+  {
+    float4 of = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) of = atom_off[i];
+    nc = collect_candidates<true>(P, i, active, Bi, of, bin_count, bins, err, cget, cset, P.rc2_band, P.kcap);
+  }
+  __syncwarp();
+  // pass 2 in df64: M_i (xx, xy, xz, yy, yz, zz) and S_i (x, y, z), DF_UNROLL
+  // candidates per iteration with no branch between their operations, so
+  // their dependent FP32 chains interleave (the sweep is bound by the latency
+  // of those chains and of the neighbours' records, not by issue).  A
+  // candidate outside the cut-off (or past the lane's list) is evaluated at
+  // r^2 = 1 with H forced to 0: its terms add exact zeros and it writes no
+  // pair.
+  bsum sm[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) sm[q] = bsum_zero();
+  const df rc2{P.rc2_hi, P.rc2_lo};
+  const int nmax = __reduce_max_sync(0xffffffffu, nc);
+  for (int k = 0; k < nmax; k += DF_UNROLL) {
+    unsigned uu[DF_UNROLL];
+    df ex[DF_UNROLL], ey[DF_UNROLL], ez[DF_UNROLL], r2[DF_UNROLL];
+    int ej[DF_UNROLL];
+    bool in[DF_UNROLL];
+#pragma unroll
+    for (int c = 0; c < DF_UNROLL; ++c) {
+      const bool have = k + c < nc;
+      const unsigned u = have ? cget(k + c) : 0u;
+      const unsigned j = u & IDX_MASK, code = have ? u >> IDX_BITS : CODE_NOSHIFT;
+      const float4 R0 = rec[2 * (size_t)j], R1 = rec[2 * (size_t)j + 1];
+      const unsigned pk = __float_as_uint(R0.w);
+      // bin difference of the pair: j's bin + its periodic image - i's bin
+      const int dx = (int)(pk & 1023u) - 1 + ((int)(code % 3u) - 1) * P.nb[0] - Bi.x;
+      const int dy = (int)((pk >> 10) & 1023u) - 1 + ((int)((code / 3u) % 3u) - 1) * P.nb[1] - Bi.y;
+      const int dz = (int)((pk >> 20) & 1023u) - 1 + ((int)(code / 9u) - 1) * P.nb[2] - Bi.z;
+      ex[c] = pair_disp(dx, R0.x, R1.x, oi.x, Ri1.x, P.w_hi[0], P.w_lo[0]);
+      ey[c] = pair_disp(dy, R0.y, R1.y, oi.y, Ri1.y, P.w_hi[1], P.w_lo[1]);
+      ez[c] = pair_disp(dz, R0.z, R1.z, oi.z, Ri1.z, P.w_hi[2], P.w_lo[2]);
+      r2[c] = dot3(ex[c], ey[c], ez[c], ex[c], ey[c], ez[c]);
+      in[c] = have && lt(r2[c], rc2);
+      if (!in[c]) r2[c] = df{1.0f, 0.0f};
+      ej[c] = __float_as_int(R1.w);
+      uu[c] = u;
+    }
+#pragma unroll
+    for (int c = 0; c < DF_UNROLL; ++c) {
+      const df rji = spline_rho_df(P, ej[c], r2[c], err);
+      const df inv = recip(r2[c], rcp_estimate(r2[c].hi));
+      df H = mul(rji, inv);
+      if (!in[c]) H = df{0.0f, 0.0f};
+      const df hx = mul(H, ex[c]), hy = mul(H, ey[c]), hz = mul(H, ez[c]);
+      if (in[c]) {
+        const size_t slot = (size_t)ns * P.n + i;
+        pj[slot] = uu[c];
+        if (MULTI) {
+          const df rij = ej[c] != ei ? spline_rho_df(P, ei, r2[c], err) : rji;
+          const df Hji = mul(rij, inv);
+          pa[slot] = make_float4(ex[c].hi, ey[c].hi, ez[c].hi, Hji.hi);
+          pb[slot] = make_float4(ex[c].lo, ey[c].lo, ez[c].lo, Hji.lo);
+          pc[slot] = make_float4(H.hi, H.lo, 0.f, 0.f);
+        } else {
+          pa[slot] = make_float4(ex[c].hi, ey[c].hi, ez[c].hi, hx.hi);
+          pb[slot] = make_float4(ex[c].lo, ey[c].lo, ez[c].lo, hx.lo);
+          pc[slot] = make_float4(hy.hi, hz.hi, hy.lo, hz.lo);
+        }
+        ++ns;
+      }
+      acc_fma(sm[0].blk, hx, ex[c]);
+      acc_fma(sm[1].blk, hx, ey[c]);
+      acc_fma(sm[2].blk, hx, ez[c]);
+      acc_fma(sm[3].blk, hy, ey[c]);
+      acc_fma(sm[4].blk, hy, ez[c]);
+      acc_fma(sm[5].blk, hz, ez[c]);
+      const unsigned j = uu[c] & IDX_MASK;
+      const float4 V0 = vrec[2 * (size_t)j], V1 = vrec[2 * (size_t)j + 1];
+      const df d = dot3(ex[c], ey[c], ez[c], df{V0.x, V1.x}, df{V0.y, V1.y}, df{V0.z, V1.z});
+      acc_fma(sm[6].blk, d, hx);
+      acc_fma(sm[7].blk, d, hy);
+      acc_fma(sm[8].blk, d, hz);
+    }
+    if ((k & 7) == 8 - DF_UNROLL) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) bsum_fold(sm[q]);
+    }
+  }
+  if (!valid) return;
+  double mq[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) mq[q] = to_double(bsum_value(sm[q]));
+  const D4 xi = x[i];
+  density_epilogue<true, true, true>(P, i, active, xi, ei, 0.0, ns, mq[0], mq[1], mq[2], mq[3], mq[4], mq[5], mq[6],
+                                     mq[7], mq[8], xi_given, xi_mode, T_e, nshort, A, Bw, rho_out, beta_out, cell,
+                                     Te_i, err, counters, v, Mm, G);
 }
 
 // The FAST density sweep with TPA lanes per atom (TPA = 2, 4, 8) for small
@@ -1192,6 +1437,152 @@ __global__ void __launch_bounds__(128) k_forces_m(StepParams P, const unsigned *
       frx = var * (fma(M1.x, Gi1.w, fma(M1.y, Gi2.x, M1.z * Gi2.y)) - crx - frx);
       fry = var * (fma(M1.y, Gi1.w, fma(M1.w, Gi2.x, M2.x * Gi2.y)) - cry - fry);
       frz = var * (fma(M1.z, Gi1.w, fma(M2.x, Gi2.x, M2.y * Gi2.y)) - crz - frz);
+    }
+  }
+  store_forces<true, RAND>(P, i, live, fex, fey, fez, frx, fry, frz, f, f_eph, f_rng, f_dis, f_sto);
+}
+
+// k_forces_m over the df64 pair cache and records of k_density_df: per pair
+// (e.W_j) H e and (e.X_j) H e (several elements: H_ji (e.W_j) e) in df64
+// with blocked sums; the per-atom part (-M_i W_i, the pairs the reference
+// skips, eta sqrt(T_e), the force update) in FP64 as k_forces_m does it, with
+// W_i = a_i w_i and X_i = a_i xi_i formed from A and Bw exactly as the FP64
+// records are.  A neighbour the reference skips (rho_j <= 0 or outside the
+// group) carries a NaN in its record's first word.
+template <bool MULTI, bool RAND, int TPA = 1>
+__global__ void __launch_bounds__(128, EPH_DF_FORCES_BLOCKS)
+    k_forces_df(StepParams P, const unsigned *__restrict__ pj, const float4 *__restrict__ pa,
+                const float4 *__restrict__ pb, const float4 *__restrict__ pc, const int *__restrict__ nshort,
+                const D4 *__restrict__ Mm, const float4 *__restrict__ Gf, const D4 *__restrict__ A,
+                const D4 *__restrict__ Bw, const double *__restrict__ Te_i, D4 *__restrict__ f,
+                D4 *__restrict__ f_eph, D4 *__restrict__ f_rng, D4 *__restrict__ f_dis, D4 *__restrict__ f_sto) {
+  using namespace df64;
+  const long gt = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(gt / TPA), g = (int)(gt % TPA);
+  if (TPA == 1 && i >= P.n) return;  // with TPA > 1 every lane joins the butterfly
+  bsum se[3], sr[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) se[q] = sr[q] = bsum_zero();
+  bool live = false;
+  int ns = 0, skipped = 0;
+  if (i < P.n) {
+    const float g0 = Gf[3 * (size_t)i].x;
+    live = g0 == g0;  // not NaN: rho_i > 0 and in the group
+    if (live) ns = nshort[i];
+  }
+  int m = 0;
+  for (int k = g; k < ns; k += TPA, ++m) {
+    const size_t slot = (size_t)k * P.n + i;
+    const unsigned j = pj[slot] & IDX_MASK;
+    const float4 G0 = Gf[3 * (size_t)j];
+    if (G0.x != G0.x) {  // a pair the reference skips (handled below)
+      skipped = 1;
+    } else {
+      const float4 a = pa[slot], b = pb[slot];
+      const float4 G1 = Gf[3 * (size_t)j + 1];
+      const df ex{a.x, b.x}, ey{a.y, b.y}, ez{a.z, b.z};
+      df hx, hy, hz;
+      if (MULTI) {
+        const df Hji{a.w, b.w};
+        hx = mul(Hji, ex);
+        hy = mul(Hji, ey);
+        hz = mul(Hji, ez);
+      } else {
+        const float4 c = pc[slot];
+        hx = df{a.w, b.w};
+        hy = df{c.x, c.z};
+        hz = df{c.y, c.w};
+      }
+      const df sw = dot3(ex, ey, ez, df{G0.x, G1.x}, df{G0.y, G1.y}, df{G0.z, G1.z});
+      acc_fma(se[0].blk, sw, hx);
+      acc_fma(se[1].blk, sw, hy);
+      acc_fma(se[2].blk, sw, hz);
+      if (RAND) {
+        const float4 G2 = Gf[3 * (size_t)j + 2];
+        const df sx = dot3(ex, ey, ez, df{G0.w, G1.w}, df{G2.x, G2.z}, df{G2.y, G2.w});
+        acc_fma(sr[0].blk, sx, hx);
+        acc_fma(sr[1].blk, sx, hy);
+        acc_fma(sr[2].blk, sx, hz);
+      }
+    }
+    if ((m & 7) == 7) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        bsum_fold(se[q]);
+        if (RAND) bsum_fold(sr[q]);
+      }
+    }
+  }
+  double fex = to_double(bsum_value(se[0])), fey = to_double(bsum_value(se[1])), fez = to_double(bsum_value(se[2]));
+  double frx = 0.0, fry = 0.0, frz = 0.0;
+  if (RAND) {
+    frx = to_double(bsum_value(sr[0]));
+    fry = to_double(bsum_value(sr[1]));
+    frz = to_double(bsum_value(sr[2]));
+  }
+  if (TPA > 1) {
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) {
+      fex += __shfl_xor_sync(0xffffffffu, fex, o);
+      fey += __shfl_xor_sync(0xffffffffu, fey, o);
+      fez += __shfl_xor_sync(0xffffffffu, fez, o);
+      if (RAND) {
+        frx += __shfl_xor_sync(0xffffffffu, frx, o);
+        fry += __shfl_xor_sync(0xffffffffu, fry, o);
+        frz += __shfl_xor_sync(0xffffffffu, frz, o);
+      }
+      skipped |= __shfl_xor_sync(0xffffffffu, skipped, o);
+    }
+    if (i >= P.n || g != 0) return;
+  }
+  if (live) {
+    double cex = 0.0, cey = 0.0, cez = 0.0, crx = 0.0, cry = 0.0, crz = 0.0;
+    const D4 Ai = A[i], Bi = Bw[i];
+    const double a = Ai.y;  // alpha_i / rho_i
+    const double Wx = a * Bi.y, Wy = a * Bi.z, Wz = a * Bi.w;
+    const double Xx = a * Ai.z, Xy = a * Ai.w, Xz = a * Bi.x;
+    if (skipped) {  // rare: the skipped pairs' shares of M_i come back out
+      for (int k = 0; k < ns; ++k) {
+        const size_t slot = (size_t)k * P.n + i;
+        const unsigned j = pj[slot] & IDX_MASK;
+        const float g0 = Gf[3 * (size_t)j].x;
+        if (g0 == g0) continue;
+        const float4 pa4 = pa[slot], pb4 = pb[slot], pc4 = pc[slot];
+        const double ex = to_double(df{pa4.x, pb4.x}), ey = to_double(df{pa4.y, pb4.y}),
+                     ez = to_double(df{pa4.z, pb4.z});
+        double hx, hy, hz, H;
+        if (MULTI) {  // H_ij e
+          H = to_double(df{pc4.x, pc4.y});
+          hx = ex;
+          hy = ey;
+          hz = ez;
+        } else {
+          hx = to_double(df{pa4.w, pb4.w});
+          hy = to_double(df{pc4.x, pc4.z});
+          hz = to_double(df{pc4.y, pc4.w});
+          H = 1.0;
+        }
+        const double sw = H * dot3_fma(ex, ey, ez, Wx, Wy, Wz);
+        cex = fma(sw, hx, cex);
+        cey = fma(sw, hy, cey);
+        cez = fma(sw, hz, cez);
+        if (RAND) {
+          const double sx = H * dot3_fma(ex, ey, ez, Xx, Xy, Xz);
+          crx = fma(sx, hx, crx);
+          cry = fma(sx, hy, cry);
+          crz = fma(sx, hz, crz);
+        }
+      }
+    }
+    const D4 M1 = Mm[i], M2 = Mm[(size_t)P.n + i];  // {xx, xy, xz, yy}, {yz, zz}
+    fex += cex - fma(M1.x, Wx, fma(M1.y, Wy, M1.z * Wz));
+    fey += cey - fma(M1.y, Wx, fma(M1.w, Wy, M2.x * Wz));
+    fez += cez - fma(M1.z, Wx, fma(M2.x, Wy, M2.y * Wz));
+    if (RAND) {
+      const double var = P.eta * sqrt(Te_i[i]);
+      frx = var * (fma(M1.x, Xx, fma(M1.y, Xy, M1.z * Xz)) - crx - frx);
+      fry = var * (fma(M1.y, Xx, fma(M1.w, Xy, M2.x * Xz)) - cry - fry);
+      frz = var * (fma(M1.z, Xx, fma(M2.x, Xy, M2.y * Xz)) - crz - frz);
     }
   }
   store_forces<true, RAND>(P, i, live, fex, fey, fez, frx, fry, frz, f, f_eph, f_rng, f_dis, f_sto);

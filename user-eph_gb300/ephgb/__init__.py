@@ -23,6 +23,7 @@ EPH_OK = 0
 STATUS = {0: "EPH_OK", 1: "EPH_ERR_ARG", 2: "EPH_ERR_FILE", 3: "EPH_ERR_UNSUPPORTED_MODEL", 4: "EPH_ERR_CAPACITY",
           5: "EPH_ERR_TIMEOUT", 6: "EPH_ERR_CUDA", 7: "EPH_ERR_STATE", 8: "EPH_ERR_RANGE"}
 MODE_EXACT, MODE_FAST = 0, 1
+PAIRS_FP64, PAIRS_DF64 = 0, 1
 HOST, DEVICE, HOST_ASYNC = 0, 1, 2
 XI_DEVICE_RNG, XI_GIVEN = 0, 1
 FIELDS = {"x": (0, 3), "v": (1, 3), "f": (2, 3), "xi": (3, 3), "f_eph": (4, 3), "f_rng": (5, 3), "rho": (6, 1),
@@ -76,6 +77,7 @@ SIGNATURES = {
     "eph_set_pair_eam": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_char_p)]),
     "eph_pair_energy": (C.c_int, [C.c_void_p, _dp]),
     "eph_set_threads_per_atom": (C.c_int, [C.c_void_p, C.c_int]),
+    "eph_set_pair_arithmetic": (C.c_int, [C.c_void_p, C.c_int]),
     "eph_get_threads_per_atom": (C.c_int, [C.c_void_p, _ip]),
     "eph_set_list_skin": (C.c_int, [C.c_void_p, C.c_double]),
     "eph_get_list_skin": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), _ip]),
@@ -431,6 +433,11 @@ class FixEPH:
 
     def set_threads_per_atom(self, tpa):
         self._check(self.L.eph_set_threads_per_atom(self.h, int(tpa)))
+
+    def set_pair_arithmetic(self, which):
+        """PAIRS_DF64 (default) or PAIRS_FP64: the FAST one-lane pair sweeps'
+        per-pair arithmetic (eph_set_pair_arithmetic)."""
+        self._check(self.L.eph_set_pair_arithmetic(self.h, int(which)))
 
     def threads_per_atom(self):
         out = C.c_int()

@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # no floating-point contraction anywhere: EXACT mode must round like the
 # reference's source expressions; FAST mode writes its fma() calls explicitly
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                     "-I" + INCLUDE]
+                     "-I" + INCLUDE] + os.environ.get("EPH_NVCC_FLAGS", "").split()
 CXX_FLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-std=c++17", "-I" + INCLUDE]
 
 SOURCES = [("eph_ctx.cu", "nvcc"), ("eph_adjoint.cu", "nvcc"), ("eph_eam.cu", "nvcc"), ("eph_noalloc.cu", "nvcc"), ("eph_host.cpp", "cxx")]
