@@ -245,11 +245,12 @@ bool fused_friction(const eph_ctx *c) {
   return c->mode == EPH_MODE_FAST && c->args.model == 4 && (c->P.flags & FLAG_FRICTION) && c->fuse_w;
 }
 
-// FAST pair sums in df64: the one-lane density sweep with stage 1 folded
-// and the bin search (k_density_df, then k_forces_df at any lanes per atom),
-// bins of at most 1022 per axis (k_bin packs them in 10 bits each)
+// FAST pair sums in df64: the one-lane density sweep with stage 1 folded,
+// over the bin search (k_density_df) or the kept lists (k_density_list_df),
+// then k_forces_df at any lanes per atom; bins of at most 1022 per axis
+// (the records pack them in 10 bits each)
 bool df_active(const eph_ctx *c) {
-  return c->pair_arith == EPH_PAIRS_DF64 && c->mode == EPH_MODE_FAST && fused_friction(c) && !c->reuse &&
+  return c->pair_arith == EPH_PAIRS_DF64 && c->mode == EPH_MODE_FAST && fused_friction(c) &&
          !(c->tpa > 1 && c->n < 16384) && c->P.nb[0] <= 1022 && c->P.nb[1] <= 1022 && c->P.nb[2] <= 1022;
 }
 
@@ -275,6 +276,15 @@ void launch_density_f(eph_ctx *c, int xi_mode) {
     }
   }
   if constexpr (FAST && FUSE) {
+    if (c->reuse && df_active(c)) {
+      float4 *pa = reinterpret_cast<float4 *>(c->pe.p), *pb = pa + (size_t)c->kcap * c->n;
+      k_density_list_df<MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
+          c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->dfrec.p, c->dfvrec.p,
+          c->xi.p, xi_mode, c->T0.p, c->pj.p, pa, pb, reinterpret_cast<float4 *>(c->pg.p), c->nshort.p, c->A.p,
+          c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p, c->wrapflag.p, c->d_err.p, c->counters.p, c->v.p,
+          c->Mm.p, c->G.p, c->cl.p, c->cl_n.p, c->state.p, c->rb.p, c->flist.p);
+      return;
+    }
     if (c->reuse) {
       k_density_list<MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
           c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode,
@@ -509,8 +519,10 @@ int launch_bin(eph_ctx *c) {
     // flags the atoms near moved ones and leaves the bins as they are
     int *rb = c->rb.p;
     CUDA_TRY(c, cudaMemsetAsync(rb + 1, 0, sizeof(int), c->stream));
+    const bool df = df_active(c);
     k_list_check<<<nb, BLOCK, 0, c->stream>>>(c->P, c->x.p, c->xhold.p, c->wrapflag.p, c->xref.p, c->state.p, rb,
-                                              c->flist.p, c->counters.p);
+                                              c->flist.p, c->counters.p, df ? c->dfrec.p : nullptr,
+                                              df ? c->dfvrec.p : nullptr, c->v.p);
     k_list_decide<<<1, 32, 0, c->stream>>>(rb, c->flist.p, c->counters.p);
     k_list_mark<<<LIST_FMAX, BLOCK, 0, c->stream>>>(c->P, c->x.p, rb, c->flist.p, c->bin_count.p, c->bins.p,
                                                     c->state.p);

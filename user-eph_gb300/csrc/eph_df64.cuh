@@ -58,14 +58,53 @@ DF_FN df make(float hi, float lo) {
   return r;
 }
 
+#if defined(__CUDA_ARCH__)
+// double -> nearest float by integer work on the bits (the conversion
+// instruction would take an FP64-pipe slot): the 29 dropped significand bits
+// rounded half away from zero, the exponent rebased; |v| below 2^-126 gives
+// 0 and no value here reaches 2^128.
+__device__ __forceinline__ float round_to_float_bits(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v) + 0x10000000ull;
+  const unsigned hi = (unsigned)(b >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  if (e < 897) return __uint_as_float(hi & 0x80000000u);
+  return __uint_as_float((hi & 0x80000000u) | ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) |
+                         ((unsigned)b >> 29));
+}
+
+// float -> double exactly by integer work on the bits (zero and normal
+// floats; the df64 parts here are never subnormal)
+__device__ __forceinline__ double widen_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)u << 32));
+  const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned long long e = (unsigned long long)(((u >> 23) & 0xffu) + 896u) << 52;
+  const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
+  return __longlong_as_double((long long)(s | e | m));
+}
+#endif
+
+// the nearest df64 to x (hi the nearest float, lo the nearest float to the
+// rest, which hi subtracts exactly); one FP64 addition on the device
 DF_FN df from_double(double x) {
   df r;
+#if defined(__CUDA_ARCH__)
+  r.hi = round_to_float_bits(x);
+  r.lo = round_to_float_bits(x - widen_bits(r.hi));
+#else
   r.hi = (float)x;
   r.lo = (float)(x - (double)r.hi);
+#endif
   return r;
 }
 
-DF_FN double to_double(df a) { return (double)a.hi + (double)a.lo; }
+DF_FN double to_double(df a) {
+#if defined(__CUDA_ARCH__)
+  return widen_bits(a.hi) + widen_bits(a.lo);
+#else
+  return (double)a.hi + (double)a.lo;
+#endif
+}
 
 DF_FN df neg(df a) { return df{-a.hi, -a.lo}; }
 

@@ -109,6 +109,28 @@ __device__ __forceinline__ void wrap_into_box(const StepParams &P, D4 &xi) {
 // (unwrapped) bin corner.
 // With a gate (candidate-list reuse): nothing unless *gate (a build step),
 // no wrap (k_list_check did it), and the positions are kept in xref.
+// The records of atom i for the df64 pair sums (k_density_df,
+// k_density_list_df) in bins B of the current geometry: rec[2i] = {offset
+// x - lo - B w, hi parts; B + 1 packed 10 bits per axis}, rec[2i+1] =
+// {offset, lo parts; element}, vrec[2i], vrec[2i+1] = velocity, hi and lo.
+// The offset is formed with one rounding; a pair's displacement is then
+// d w + (o_j - o_i), d its bin difference.
+__device__ __forceinline__ void df_records(const StepParams &P, int i, const D4 &xi, const int *B,
+                                           const D4 *__restrict__ v, float4 *__restrict__ rec,
+                                           float4 *__restrict__ vrec) {
+  const double p[3] = {xi.x, xi.y, xi.z};
+  df64::df o[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) o[k] = df64::from_double(fma(-(double)B[k], P.w[k], p[k] - P.lo[k]));
+  const unsigned packed = (unsigned)(B[0] + 1) | ((unsigned)(B[1] + 1) << 10) | ((unsigned)(B[2] + 1) << 20);
+  rec[2 * (size_t)i] = make_float4(o[0].hi, o[1].hi, o[2].hi, __uint_as_float(packed));
+  rec[2 * (size_t)i + 1] = make_float4(o[0].lo, o[1].lo, o[2].lo, __int_as_float((int)xi.w));
+  const D4 vi = v[i];
+  const df64::df vx = df64::from_double(vi.x), vy = df64::from_double(vi.y), vz = df64::from_double(vi.z);
+  vrec[2 * (size_t)i] = make_float4(vx.hi, vy.hi, vz.hi, 0.f);
+  vrec[2 * (size_t)i + 1] = make_float4(vx.lo, vy.lo, vz.lo, 0.f);
+}
+
 // With rec (the df64 pair sums), also the atom's records for them: rec[2i] =
 // {offset in its bin, hi parts; bin + 1 packed 10 bits per axis},
 // rec[2i+1] = {offset, lo parts; element}, vrec[2i], vrec[2i+1] = velocity,
@@ -163,23 +185,7 @@ __global__ void k_bin(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold, 
   }
   atom_bin[i] = make_int4(B[0], B[1], B[2], flat);
   atom_off[i] = make_float4(o[0], o[1], o[2], 0.f);
-  if (rec) {
-    float oh[3], ol[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const double o64 = fma(-(double)B[k], P.w[k], p[k] - P.lo[k]);
-      oh[k] = (float)o64;
-      ol[k] = (float)(o64 - (double)oh[k]);
-    }
-    const unsigned packed = (unsigned)(B[0] + 1) | ((unsigned)(B[1] + 1) << 10) | ((unsigned)(B[2] + 1) << 20);
-    rec[2 * (size_t)i] = make_float4(oh[0], oh[1], oh[2], __uint_as_float(packed));
-    rec[2 * (size_t)i + 1] = make_float4(ol[0], ol[1], ol[2], __int_as_float((int)xi.w));
-    const D4 vi = v[i];
-    const float vh[3] = {(float)vi.x, (float)vi.y, (float)vi.z};
-    vrec[2 * (size_t)i] = make_float4(vh[0], vh[1], vh[2], 0.f);
-    vrec[2 * (size_t)i + 1] = make_float4((float)(vi.x - (double)vh[0]), (float)(vi.y - (double)vh[1]),
-                                          (float)(vi.z - (double)vh[2]), 0.f);
-  }
+  if (rec) df_records(P, i, xi, B, v, rec, vrec);
 }
 
 // -------------------------------------------------------- density sweep
@@ -563,9 +569,11 @@ __global__ void __launch_bounds__(128) k_density(
 #ifndef EPH_DF_FORCES_BLOCKS
 #define EPH_DF_FORCES_BLOCKS 7
 #endif
-// candidates per iteration of the df64 density sweep's pass 2
+// candidates per iteration of the df64 density sweep's pass 2 (measured on
+// GB300 at 2,048,000 atoms: 1 -> 3.89 ms, 2 -> 3.91 ms; the sweep waits on
+// the neighbours' records and its pair-cache writes more than on its chains)
 #ifndef DF_UNROLL
-#define DF_UNROLL 2
+#define DF_UNROLL 1
 #endif
 
 // rho_e(x) of element e at x = r^2 from the local-form df64 table: knot
@@ -668,11 +676,9 @@ __global__ void __launch_bounds__(128, EPH_DF_DENSITY_BLOCKS) k_density_df(
   }
   __syncwarp();
   // pass 2 in df64: M_i (xx, xy, xz, yy, yz, zz) and S_i (x, y, z), DF_UNROLL
-  // candidates per iteration with no branch between their operations, so
-  // their dependent FP32 chains interleave (the sweep is bound by the latency
-  // of those chains and of the neighbours' records, not by issue).  A
+  // candidates per iteration with no branch around their arithmetic: a
   // candidate outside the cut-off (or past the lane's list) is evaluated at
-  // r^2 = 1 with H forced to 0: its terms add exact zeros and it writes no
+  // r^2 = 1 with H forced to 0, so its terms add exact zeros and it writes no
   // pair.
   bsum sm[9];
 #pragma unroll
@@ -925,10 +931,14 @@ __device__ __forceinline__ void current_bin(const StepParams &P, const D4 &xi, i
 
 // First kernel of a step with list reuse: the engine's wrap (as k_bin does
 // it), then each atom's displacement since the list build; moved atoms get
-// state 2 and join the list of moved atoms (state 0 otherwise).
+// state 2 and join the list of moved atoms (state 0 otherwise).  With rec
+// (the df64 density sweep), also every atom's records for it from its
+// current position, in the bins of the current geometry (df_records).
 __global__ void k_list_check(StepParams P, D4 *__restrict__ x, D4 *__restrict__ xhold,
                              const int *__restrict__ wrapflag, const D4 *__restrict__ xref, int *__restrict__ state,
-                             int *__restrict__ rb, int *__restrict__ flist, unsigned long long *__restrict__ counters) {
+                             int *__restrict__ rb, int *__restrict__ flist, unsigned long long *__restrict__ counters,
+                             float4 *__restrict__ rec = nullptr, float4 *__restrict__ vrec = nullptr,
+                             const D4 *__restrict__ v = nullptr) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) *P.step += 1ull;  // read by the density sweep that follows
   bool moved = false;
@@ -939,6 +949,16 @@ __global__ void k_list_check(StepParams P, D4 *__restrict__ x, D4 *__restrict__ 
       x[i] = xi;
       xhold[i] = xi;
       if (i == 0) atomicAdd(&counters[CNT_WRAP], 1ull);
+    }
+    if (rec) {
+      const double p[3] = {xi.x, xi.y, xi.z};
+      int B[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int b = (int)floor((p[k] - P.lo[k]) * P.inv_w[k]);
+        B[k] = b < -1 ? -1 : (b > P.nb[k] ? P.nb[k] : b);
+      }
+      df_records(P, i, xi, B, v, rec, vrec);
     }
     const D4 r = xref[i];
     const double dx = min_image(xi.x - r.x, P.prd[0], P.half_prd[0]);
@@ -1153,6 +1173,188 @@ __global__ void __maxnreg__(64) k_density_list(
   if (!valid) return;
   density_epilogue<true, true>(P, i, active, xi, ei, rho, ns < P.kcap ? ns : P.kcap, mxx, mxy, mxz, myy, myz, mzz, Sx, Sy, Sz, xi_given,
                                xi_mode, T_e, nshort, A, Bw, rho_out, beta_out, cell, Te_i, err, counters, v, Mm, G);
+}
+
+// k_density_list with k_density_df's pass 2: the candidates come from the
+// kept lists as there (build steps search the bins, atoms flagged near moved
+// ones search afresh), then every pair term and sum in df64 from the records
+// k_list_check wrote this step (bins of the current positions); the periodic
+// image of a candidate comes from FP32 positions rebuilt from those records
+// (B w + o, good to ~1e-6 of the box: the image test has a margin of
+// tens of angstroms).
+template <bool MULTI>
+__global__ void __launch_bounds__(128, EPH_DF_DENSITY_BLOCKS) k_density_list_df(
+    StepParams P, const D4 *__restrict__ x, const int *__restrict__ mask, const int *__restrict__ bin_count,
+    const BinEntry *__restrict__ bins, const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
+    const float4 *__restrict__ rec, const float4 *__restrict__ vrec, const D4 *__restrict__ xi_given, int xi_mode,
+    const double *__restrict__ T_e, unsigned *__restrict__ pj, float4 *__restrict__ pa, float4 *__restrict__ pb,
+    float4 *__restrict__ pc, int *__restrict__ nshort, D4 *__restrict__ A, D4 *__restrict__ Bw,
+    double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell, double *__restrict__ Te_i,
+    int *__restrict__ wrapflag, unsigned *__restrict__ err, unsigned long long *__restrict__ counters,
+    const D4 *__restrict__ v, D4 *__restrict__ Mm, D4 *__restrict__ G, unsigned *__restrict__ cl,
+    int *__restrict__ cl_n, const int *__restrict__ state, const int *__restrict__ rb,
+    const int *__restrict__ flist) {
+  using namespace df64;
+  __shared__ unsigned s_cand[CAND_SMEM * 128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
+  if (i == 0) *wrapflag = 0;  // k_list_check has read it
+  const bool valid = i < P.n;
+  const bool active = valid && (mask[i] & P.groupbit) != 0;
+  const size_t n = (size_t)P.n;
+  auto sget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : pj[(size_t)k * n + i]; };
+  auto sset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM)
+      s_cand[k * nt + t] = u;
+    else
+      pj[(size_t)k * n + i] = u;
+  };
+  auto lset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM) s_cand[k * nt + t] = u;
+    cl[(size_t)k * n + i] = u;
+  };
+  auto lget = [&](int k) -> unsigned { return cl[(size_t)k * n + i]; };
+  D4 xi = D4{0.0, 0.0, 0.0, 0.0};
+  if (valid) xi = x[i];
+  const bool build = rb[2] != 0;
+  int nc = 0;
+  bool fresh = false;
+  if (build) {
+    int4 Bi = make_int4(0, 0, 0, 0);
+    float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) {
+      Bi = atom_bin[i];
+      oi = atom_off[i];
+    }
+    nc = collect_candidates<true>(P, i, active, Bi, oi, bin_count, bins, err, lget, lset, P.rc2_band, P.lcap);
+    nc = collect_candidates<true>(P, i, active, Bi, oi, bin_count, bins, err, lget, lset, P.rl2_band, P.lcap,
+                                  nullptr, P.rc2_band, nc);
+    if (valid) cl_n[i] = nc;
+  } else {
+    const int st = active ? state[i] : 0;
+    fresh = st != 0;
+    if (__any_sync(0xffffffffu, fresh)) {
+      int4 Bi = make_int4(0, 0, 0, 0);
+      float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (fresh) {
+        if (st & 2) {
+          current_bin(P, xi, Bi, oi);
+        } else {
+          Bi = atom_bin[i];
+          oi = atom_off[i];
+        }
+      }
+      nc = collect_candidates<true, true>(P, i, fresh, Bi, oi, bin_count, bins, err, sget, sset, P.rl2_band, P.kcap,
+                                          state);
+      const int nf = rb[1];  // <= LIST_FMAX on a step without a build
+      for (int q = 0; q < nf; ++q) {
+        const int f = flist[q];
+        if (fresh && f != i) {
+          const D4 xf = x[f];
+          const double dx = min_image(xf.x - xi.x, P.prd[0], P.half_prd[0]);
+          const double dy = min_image(xf.y - xi.y, P.prd[1], P.half_prd[1]);
+          const double dz = min_image(xf.z - xi.z, P.prd[2], P.half_prd[2]);
+          if (dx * dx + dy * dy + dz * dz < P.rc2 * (1.0 + 1e-4)) {
+            if (nc < P.kcap)
+              sset(nc++, (unsigned)f | (CODE_NOSHIFT << IDX_BITS));
+            else
+              atomicOr(err, ERR_PAIR_OVERFLOW);
+          }
+        }
+      }
+    }
+    if (active && !fresh) {
+      nc = cl_n[i];
+      const int nh = nc < CAND_SMEM ? nc : CAND_SMEM;
+#pragma unroll 8
+      for (int k = 0; k < nh; ++k) s_cand[k * nt + t] = __ldcs(cl + (size_t)k * n + i);  // read once a step
+    }
+  }
+  __syncwarp();
+  const unsigned *__restrict__ tail = fresh ? pj : cl;
+  // atom i's records; its FP32 position B w + o for the image test
+  float4 oi = make_float4(0.f, 0.f, 0.f, 0.f), Ri1 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (valid) {
+    oi = rec[2 * (size_t)i];
+    Ri1 = rec[2 * (size_t)i + 1];
+  }
+  const unsigned pki = __float_as_uint(oi.w);
+  const int bix = (int)(pki & 1023u) - 1, biy = (int)((pki >> 10) & 1023u) - 1, biz = (int)((pki >> 20) & 1023u) - 1;
+  const float pix = (float)bix * P.wf[0] + oi.x, piy = (float)biy * P.wf[1] + oi.y, piz = (float)biz * P.wf[2] + oi.z;
+  const int ei = __float_as_int(Ri1.w);
+  bsum sm[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) sm[q] = bsum_zero();
+  const df rc2{P.rc2_hi, P.rc2_lo};
+  int ns = 0;
+  const int nmax = __reduce_max_sync(0xffffffffu, nc);
+  for (int k = 0; k < nmax; ++k) {
+    const bool have = k < nc;
+    const unsigned j = have ? (k < CAND_SMEM ? s_cand[k * nt + t] : __ldcs(tail + (size_t)k * n + i)) & IDX_MASK : 0u;
+    const float4 R0 = rec[2 * (size_t)j], R1 = rec[2 * (size_t)j + 1];
+    const unsigned pk = __float_as_uint(R0.w);
+    const int bjx = (int)(pk & 1023u) - 1, bjy = (int)((pk >> 10) & 1023u) - 1, bjz = (int)((pk >> 20) & 1023u) - 1;
+    const float qx = (float)bjx * P.wf[0] + R0.x - pix, qy = (float)bjy * P.wf[1] + R0.y - piy,
+                qz = (float)bjz * P.wf[2] + R0.z - piz;
+    const int mx = qx > P.half_prdf[0] ? -1 : (qx < -P.half_prdf[0] ? 1 : 0);
+    const int my = qy > P.half_prdf[1] ? -1 : (qy < -P.half_prdf[1] ? 1 : 0);
+    const int mz = qz > P.half_prdf[2] ? -1 : (qz < -P.half_prdf[2] ? 1 : 0);
+    const unsigned code = (unsigned)((mx + 1) + 3 * (my + 1) + 9 * (mz + 1));
+    const df ex = pair_disp(bjx + mx * P.nb[0] - bix, R0.x, R1.x, oi.x, Ri1.x, P.w_hi[0], P.w_lo[0]);
+    const df ey = pair_disp(bjy + my * P.nb[1] - biy, R0.y, R1.y, oi.y, Ri1.y, P.w_hi[1], P.w_lo[1]);
+    const df ez = pair_disp(bjz + mz * P.nb[2] - biz, R0.z, R1.z, oi.z, Ri1.z, P.w_hi[2], P.w_lo[2]);
+    df r2 = dot3(ex, ey, ez, ex, ey, ez);
+    const bool in = have && lt(r2, rc2);
+    if (!in) r2 = df{1.0f, 0.0f};
+    const int ej = __float_as_int(R1.w);
+    const df rji = spline_rho_df(P, ej, r2, err);
+    const df inv = recip(r2, rcp_estimate(r2.hi));
+    df H = mul(rji, inv);
+    if (!in) H = df{0.0f, 0.0f};
+    const df hx = mul(H, ex), hy = mul(H, ey), hz = mul(H, ez);
+    if (in) {
+      if (ns < P.kcap) {
+        const size_t slot = (size_t)ns * n + i;
+        pj[slot] = j | (code << IDX_BITS);
+        if (MULTI) {
+          const df rij = ej != ei ? spline_rho_df(P, ei, r2, err) : rji;
+          const df Hji = mul(rij, inv);
+          pa[slot] = make_float4(ex.hi, ey.hi, ez.hi, Hji.hi);
+          pb[slot] = make_float4(ex.lo, ey.lo, ez.lo, Hji.lo);
+          pc[slot] = make_float4(H.hi, H.lo, 0.f, 0.f);
+        } else {
+          pa[slot] = make_float4(ex.hi, ey.hi, ez.hi, hx.hi);
+          pb[slot] = make_float4(ex.lo, ey.lo, ez.lo, hx.lo);
+          pc[slot] = make_float4(hy.hi, hz.hi, hy.lo, hz.lo);
+        }
+      } else {
+        atomicOr(err, ERR_PAIR_OVERFLOW);
+      }
+      ++ns;
+    }
+    acc_fma(sm[0].blk, hx, ex);
+    acc_fma(sm[1].blk, hx, ey);
+    acc_fma(sm[2].blk, hx, ez);
+    acc_fma(sm[3].blk, hy, ey);
+    acc_fma(sm[4].blk, hy, ez);
+    acc_fma(sm[5].blk, hz, ez);
+    const float4 V0 = vrec[2 * (size_t)j], V1 = vrec[2 * (size_t)j + 1];
+    const df d = dot3(ex, ey, ez, df{V0.x, V1.x}, df{V0.y, V1.y}, df{V0.z, V1.z});
+    acc_fma(sm[6].blk, d, hx);
+    acc_fma(sm[7].blk, d, hy);
+    acc_fma(sm[8].blk, d, hz);
+    if ((k & 7) == 7) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) bsum_fold(sm[q]);
+    }
+  }
+  if (!valid) return;
+  double mq[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) mq[q] = to_double(bsum_value(sm[q]));
+  density_epilogue<true, true, true>(P, i, active, xi, ei, 0.0, ns < P.kcap ? ns : P.kcap, mq[0], mq[1], mq[2],
+                                     mq[3], mq[4], mq[5], mq[6], mq[7], mq[8], xi_given, xi_mode, T_e, nshort, A,
+                                     Bw, rho_out, beta_out, cell, Te_i, err, counters, v, Mm, G);
 }
 
 // -------------------------------------------------------- friction sweep 1
