@@ -119,41 +119,40 @@ class ClockSampler:
 
 
 def density_bytes(n_atoms, n_pairs):
-    """Algorithmic HBM bytes of one launch of the density sweep (k_density,
-    FAST, one element, stage 1 folded in): per atom read x_i, v_i (64 B), mask
-    (4), bin and offset (32), T_e at the atom (8); written pair count (4), A_i,
-    Bw_i (64), M_i (64), G_i (64), rho, beta, T_e at the atom (24), cell (4);
-    per in-cutoff pair the cached index (4), e_ij with the x of H e (32) and
-    the y, z of H e (16) written, H = rho_j(r^2)/r^2.  The neighbours'
-    positions and velocities and the bins are L2 hits and not counted."""
-    return 332 * n_atoms + 52 * n_pairs
+    """Algorithmic HBM bytes of one launch of the density sweep of the bench
+    workload (k_density_list_df: FAST, one element, stage 1 folded, df64 pair
+    sums over the kept candidate lists): per atom read x_i, v_i (64 B), mask,
+    state, list length (12), the atom's df64 record (32), T_e at the atom (8);
+    written pair count (4), A_i, Bw_i (64), M_i (64), G_i (48), rho, beta, T_e
+    at the atom (24), cell (4); per in-cutoff pair its list entry read (4) and
+    the cached index (4), e_ij and H e as double-floats (48) written.  The
+    neighbours' records, the spline table and the list entries of the shell
+    beyond the cut-off are not counted."""
+    return 324 * n_atoms + 56 * n_pairs
 
 
 def forces_bytes(n_atoms, n_pairs):
-    """Algorithmic HBM bytes of one launch of the force sweep (k_forces_m,
-    FAST, one element): per atom G_i and M_i (128 B), pair count (4), T_e at
-    the atom (8), f read and written (64), f_EPH and f_RNG written (64); per
-    in-cutoff pair the cached index (4), e_ij and H e (48).  The neighbours'
-    records G_j are L2 hits and not counted."""
-    return 268 * n_atoms + 52 * n_pairs
+    """Algorithmic HBM bytes of one launch of the force sweep (k_forces_df,
+    FAST, one element): per atom its record flag (16 B), pair count (4), A_i,
+    Bw_i (64), M_i (64), T_e at the atom (8), f read and written (64), f_EPH
+    and f_RNG written (64); per in-cutoff pair the cached index (4), e_ij and
+    H e as double-floats (48).  The neighbours' records G_j are not counted."""
+    return 284 * n_atoms + 52 * n_pairs
 
 
-# DRAM bytes of one launch (dram__bytes_read.sum + dram__bytes_write.sum,
-# one-pass ncu capture of the bench workload itself, 2,048,000 atoms at 42.0
-# pairs per atom) over the algorithmic
-# bytes of that launch; the bench's traffic figure is this ratio times the
-# algorithmic bytes at its own pair count.
-DENSITY_DRAM_OVER_ALGORITHMIC = (0.333330e9 + 4.870853e9) / density_bytes(2048000, 86014654)
-FORCES_DRAM_OVER_ALGORITHMIC = (4.876371e9 + 0.189099e9) / forces_bytes(2048000, 86014654)
-# FP64-pipe utilisation of the two sweeps (ncu, 131,072-atom fcc case)
-DENSITY_FP64_PIPE = 0.670
-FORCES_FP64_PIPE = 0.841
-# FP64 thread instructions per in-cutoff pair (DADD + DMUL + DFMA, predicated
-# on; ncu on the 131,072-atom case, per-atom work included) and the GB300's
-# FP64 issue rate: 2 thread instructions per SM per clock at 2.07 GHz
-DENSITY_FP64_PER_PAIR = 30.23  # 29.23 counted with an FP32 spline index, + the exact index's DMUL
-FORCES_FP64_PER_PAIR = 13.14
-FP64_PEAK = 2 * 152 * 2.07e9
+# DRAM bytes of one launch (dram__bytes_read.sum + dram__bytes_write.sum) over
+# the algorithmic bytes of that launch, from an ncu capture of the same
+# kernels on the 131,072-atom cascade (42.0 pairs per atom, like the bench
+# workload); the bench's traffic figure is this ratio times the algorithmic
+# bytes at its own size.  Under 1: part of a sweep's pair-cache writes is
+# still in L2 when it ends.
+DENSITY_DRAM_OVER_ALGORITHMIC = 0.845
+FORCES_DRAM_OVER_ALGORITHMIC = 0.987
+# pipe and issue figures of the two sweeps (ncu, the same capture)
+DENSITY_PIPES = {"issue_active": 0.534, "fma_pipe": 0.262, "alu_pipe": 0.363, "fp64_pipe": 0.131,
+                 "top_stall": "long_scoreboard"}
+FORCES_PIPES = {"issue_active": 0.363, "fma_pipe": 0.277, "alu_pipe": 0.085, "fp64_pipe": 0.185,
+                "top_stall": "long_scoreboard"}
 
 
 def ranks_reduce(x, op, device):
@@ -712,18 +711,15 @@ def main():
     value = job_value(world, n, args.steps, res["ms"])
     hbm, peak_src = peaks()
 
-    def roofline(phase, kernel, nbytes, dram_ratio, fp64_pipe, fp64_per_pair):
+    def roofline(phase, kernel, nbytes, dram_ratio, pipes):
         ms_p, nl_p = res["phases"][phase]
         t_launch = ms_p / max(nl_p, 1) / 1000.0
         achieved = nbytes / t_launch / 1e9
-        fp64 = fp64_per_pair * res["n_pairs"] / t_launch
         return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_source": peak_src, "traffic": dram_ratio * nbytes,
-                "algorithmic_bytes": nbytes, "launch_ms": t_launch * 1000.0, "fp64_pipe_frac_ncu": fp64_pipe,
-                "fp64": {"achieved": fp64, "peak": FP64_PEAK, "unit": "FP64 thread-instructions/s",
-                         "frac": fp64 / FP64_PEAK, "per_pair": fp64_per_pair},
-                "note": "bound by FP64 issue, not HBM: GB300 issues ~0.6e12 FP64 thread-instructions/s "
-                        "(2 per SM per clock); ncu puts this kernel's FP64 pipe at %.0f%%" % (100 * fp64_pipe)}
+                "algorithmic_bytes": nbytes, "launch_ms": t_launch * 1000.0, "pipes_ncu_131k": pipes,
+                "note": "df64 pair arithmetic on the FP32 pipe; latency-bound on the neighbours' records "
+                        "(ncu: long-scoreboard stalls first)"}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -731,12 +727,12 @@ def main():
         "config": {"workload": WORKLOAD, "atoms_per_gpu": n, "grid": list(GRID), "dt_ps": DT,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 52 // 2 ** 20),
-                   "mode": "fast", "xi": "device Philox4x32-10"},
+                   "mode": "fast", "pair_arithmetic": "df64", "xi": "device Philox4x32-10"},
         "gpu_launches": res["launches"],
-        "roofline": roofline("density", "k_density", density_bytes(n, res["n_pairs"]),
-                             DENSITY_DRAM_OVER_ALGORITHMIC, DENSITY_FP64_PIPE, DENSITY_FP64_PER_PAIR),
-        "roofline_forces": roofline("forces", "k_forces_m", forces_bytes(n, res["n_pairs"]),
-                                    FORCES_DRAM_OVER_ALGORITHMIC, FORCES_FP64_PIPE, FORCES_FP64_PER_PAIR),
+        "roofline": roofline("density", "k_density_list_df", density_bytes(n, res["n_pairs"]),
+                             DENSITY_DRAM_OVER_ALGORITHMIC, DENSITY_PIPES),
+        "roofline_forces": roofline("forces", "k_forces_df", forces_bytes(n, res["n_pairs"]),
+                                    FORCES_DRAM_OVER_ALGORITHMIC, FORCES_PIPES),
         "phases_ms": {k: round(v[0], 3) for k, v in res["phases"].items()},
         "clocks": res["clocks"],
         "pairs_per_atom": res["n_pairs"] / n,

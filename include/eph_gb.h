@@ -196,7 +196,8 @@ int eph_autotune(eph_ctx *ctx, int *chosen);
 int eph_set_pair_arithmetic(eph_ctx *ctx, int which);
 
 /* Skin s of the kept candidate lists (Angstrom; default 0.3, used from 2^15
- * to 2^20 atoms, where it pays; a skin set here applies at any size, 0 turns
+ * atoms on with the df64 pair sums and from 2^15 to 2^20 atoms with FP64
+ * ones, where it pays; a skin set here applies at any size, 0 turns
  * the lists off).  The reference takes its pairs from the engine's Verlet list
  * (fix_eph.cpp:273-275: a full list with cutoff r_cutoff, padded by the
  * engine's skin and rebuilt when an atom moved half of it); here the list is

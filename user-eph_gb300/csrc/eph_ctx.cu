@@ -407,7 +407,12 @@ int auto_bcap(const eph_ctx *c) {
 // 2,048,000 atoms +0.2 %, where both sweeps already run at the FP64 issue
 // limit); a skin set through eph_set_list_skin applies at any size.
 bool want_list(const eph_ctx *c) {
-  const bool size_ok = c->lskin_user || (c->n >= (1 << 15) && c->n <= (1 << 20));
+  // with the df64 pair sums (whose pass 2 no longer hides the bin search) the
+  // lists pay at every size from 2^15 atoms on (measured on GB300, step time
+  // bin search -> lists: 131,072 atoms 0.543 -> 0.482 ms, 500,000 atoms
+  // 1.447 -> 1.112 ms, 1,000,188 atoms 2.663 -> 2.007 ms, 2,048,000 atoms
+  // 5.133 -> 3.849 ms)
+  const bool size_ok = c->lskin_user || (c->n >= (1 << 15) && (c->n <= (1 << 20) || c->pair_arith == EPH_PAIRS_DF64));
   if (c->mode != EPH_MODE_FAST || c->lskin <= 0.0 || c->list_block || c->eam || c->n <= 0 ||
       !(c->tpa == 1 || c->n >= 16384) || !fused_friction(c) || !size_ok)
     return false;
@@ -1007,7 +1012,7 @@ int eph_set_pair_arithmetic(eph_ctx *c, int which) {
   drop_graph(c);
   c->buf_gen += 1;  // graphs captured elsewhere hold the old kernels
   c->pair_arith = which;
-  return EPH_OK;
+  return c->n > 0 ? configure_list(c) : EPH_OK;  // the lists' default range depends on it
 }
 
 int eph_set_list_skin(eph_ctx *c, double skin) {
