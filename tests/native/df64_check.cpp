@@ -141,6 +141,17 @@ int main() {
     const ld fsc = fmaxl(fabsl(Fl[0]), fmaxl(fabsl(Fl[1]), fabsl(Fl[2])));
     for (int k = 0; k < 3; ++k) e_f = fmaxl(e_f, rel(to_double(bsum_value(F[k])), Fl[k], fsc));
   }
+  // the spline index estimate: floor(q) or one less, never negative, for
+  // 0 <= q < 2^22 (the knot counts of the beta files are far below that)
+  int bad_floor = 0;
+  for (int t = 0; t < N; ++t) {
+    const float q = t < 1000 ? (float)t * 0.25f : (float)(4.0e6 * P(g) * P(g) * P(g));
+    const float kr = floor_estimate(q);
+    const int k = floor_estimate_int(kr);
+    const int f = (int)floorf(q);
+    if (!(kr == (float)k && k >= 0 && (k == f || k == f - 1))) ++bad_floor;
+  }
+  printf("floor_estimate_bad %d\n", bad_floor);
   printf("add %.3Le\nmul %.3Le\nrecip %.3Le\ndisplacement %.3Le\ndot3 %.3Le\nhorner %.3Le\n", e_add, e_mul, e_rcp,
          e_disp, e_dot, e_hor);
   printf("atom_M %.3Le\natom_S %.3Le\natom_w %.3Le\natom_force_sum %.3Le\n", e_M, e_S, e_w, e_f);

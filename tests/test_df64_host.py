@@ -36,6 +36,13 @@ def results(tmp_path_factory):
     return {ln.split()[0]: float(ln.split()[1]) for ln in out.splitlines() if ln.strip()}
 
 
+def test_spline_index_estimate(results):
+    """floor_estimate (the density sweep's knot index): floor(q) or one less,
+    never negative, over 0 <= q < 4e6 (dense near 0, where a first version
+    that rounded near 2^23 returned -1 for q < 0.5)."""
+    assert results["floor_estimate_bad"] == 0
+
+
 @pytest.mark.parametrize("name", sorted(BOUNDS))
 def test_df64_error_bound(results, name):
     assert results[name] <= BOUNDS[name] * U, (name, results[name] / U)

@@ -164,6 +164,22 @@ DF_FN float rcp_estimate(float x) {
 #endif
 }
 
+// round(q - 0.5) as an integer-valued float for 0 <= q < 2^22 without a
+// conversion instruction: adding 1.5 * 2^23 puts the sum where FP32 spacing
+// is exactly 1, so the addition rounds to an integer (ties to even), and
+// subtracting the constant again is exact.  The result is floor(q) or, at
+// an exact integer q, one less; it is never negative.  The integer itself is
+// the low bits of (result + 1.5 * 2^23).
+DF_FN float floor_estimate(float q) { return ((q - 0.5f) + 12582912.0f) - 12582912.0f; }
+DF_FN int floor_estimate_int(float kr) {
+  union {
+    float f;
+    int i;
+  } u;
+  u.f = kr + 12582912.0f;
+  return u.i - 0x4B400000;
+}
+
 // A running sum of products kept as an unnormalised pair: hi carries the
 // rounded sum, lo collects every rounding error (each product's by TwoProd,
 // each addition's by TwoSum) -- the cascaded "Dot2" of Ogita, Rump and Oishi

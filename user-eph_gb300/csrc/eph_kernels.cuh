@@ -585,11 +585,11 @@ __global__ void __launch_bounds__(128) k_density(
 // ~1e-14 without the cancellation of evaluating the absolute form at large x.
 __device__ __forceinline__ df64::df spline_rho_df(const StepParams &P, int e, df64::df x, unsigned *err) {
   using namespace df64;
+  // floor(x / dx) from the FP32 quotient without a conversion instruction
+  // (floor_estimate; off by one at most, settled by the sign of t below)
   const float q = x.hi * P.inv_dxr_f;
-  // floor(q) for 0 <= q < 2^22 by the 2^23 rounding trick (no conversion
-  // instruction); ties and slips are settled by the sign of t below
-  const float kr = ((q - 0.5f) + 8388608.0f) - 8388608.0f;
-  int k = (int)__float_as_int(kr + 8388608.0f) - 0x4B000000;
+  const float kr = floor_estimate(q);
+  int k = floor_estimate_int(kr);
   float p, pe;
   two_prod(kr, P.dxr_hi, p, pe);
   pe = fmaf(kr, P.dxr_lo, pe);
