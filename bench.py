@@ -231,23 +231,38 @@ def run_gpu(args, rank, world):
         v.numpy()[:] = fix.get("v")
         e2e_steps = max(1, min(args.steps, 20))
 
-        xn, vn, fn, f0 = x.numpy(), v.numpy(), f.numpy(), f0_t.numpy()
+        arr_t = torch.zeros((n, 8), dtype=torch.float64).pin_memory()
+        xn, vn, fn, f0, arr = x.numpy(), v.numpy(), f.numpy(), f0_t.numpy(), arr_t.numpy()
+        step_no = [0]
 
         def host_step():
-            # the LAMMPS fix's sequence: copies queued on the fix's stream from
-            # pinned host arrays, one synchronisation at the end (compute_vector)
+            # the hooks of the LAMMPS fix eph/gb (user-eph_gb300/lammps/fix_eph_gb.cpp)
+            # with its default settings, on a step where the engine re-neighbours
+            # without re-sorting (the knock-on atom moves more than half the skin
+            # every step, so LAMMPS rebuilds its lists every step here):
+            step_no[0] += 1
+            # initial_integrate: x, v, f in; integrate; x out (queued), v out (synchronising)
             fix.put("x", xn, asynchronous=True)
             fix.put("v", vn, asynchronous=True)
             fix.put("f", fn, asynchronous=True)
             fix.initial_integrate()
-            fix.put("f", f0, asynchronous=True)  # the pair force of this step (none)
-            fix.post_force()
-            fix.final_integrate()
-            fix.end_of_step()
             fix.get_async("x", xn)
-            fix.get_async("v", vn)
-            fix.get_async("f", fn)
-            return fix.compute_vector(0)
+            fix.get("v", vn)
+            # post_force after the engine's re-neighbouring: x (wrapped) and the
+            # engine's pair force (none) in; forces; f out
+            fix.put("x", xn, asynchronous=True)
+            fix.put("f", f0, asynchronous=True)
+            fix.post_force()
+            fix.get("f", fn)
+            # final_integrate: f in; integrate; v out
+            fix.put("f", fn, asynchronous=True)
+            fix.final_integrate()
+            fix.get("v", vn)
+            # end_of_step: deposition and grid; the per-atom array out (peratom
+            # every step, the fix's default)
+            fix.set_timestep(step_no[0])
+            fix.end_of_step()
+            fix.get("array", arr)
 
         for _ in range(2):
             host_step()
@@ -259,7 +274,8 @@ def run_gpu(args, rank, world):
             host_step()
         torch.cuda.synchronize()
         t_e2e = ranks_reduce(time.perf_counter() - t0, "max", "cuda")
-        out.update(t_e2e=t_e2e, e2e_steps=e2e_steps, h2d=4 * 3 * 8 * n, d2h=3 * 3 * 8 * n + 8)
+        # per atom: in x, v, f + x, f + f (6 x 24 B); out x, v + f + v (4 x 24 B) + the array (64 B)
+        out.update(t_e2e=t_e2e, e2e_steps=e2e_steps, h2d=6 * 24 * n, d2h=4 * 24 * n + 64 * n)
     return out
 
 
@@ -742,7 +758,10 @@ def main():
     }
     if "t_e2e" in res:
         line["e2e"] = {"value": world * n * res["e2e_steps"] / res["t_e2e"], "unit": METRIC,
-                       "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"]}
+                       "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"],
+                       "sequence": "the hooks and copies of the LAMMPS fix eph/gb (fix_eph_gb.cpp) with its default "
+                                   "settings on a re-neighbouring step without re-sorting, pinned host arrays",
+                       "timing": "host wall clock, synchronised"}
     if not args.no_batched:
         line["batched"] = run_batched(args, int(os.environ.get("LOCAL_RANK", rank)))
         line["batched"]["value"] = ranks_reduce(line["batched"]["value"], "sum", "cuda")

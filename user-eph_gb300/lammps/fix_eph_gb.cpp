@@ -10,10 +10,11 @@
  *                                      out on steps that are multiples of
  *                                      peratom_freq (`fix_modify ID peratom N`,
  *                                      default 1: every step, as the reference)
- * post_force needs no x or v: between initial_integrate (which copied them
- * back) and post_force the engine changes them only when it re-neighbours
- * (wraps, re-sorts or migrates atoms), and after that the whole atom set is
- * uploaded again.
+ * post_force needs no v: initial_integrate copied it back and the engine
+ * leaves it alone until post_force.  x changes only when the engine
+ * re-neighbours: it wraps atoms into the box (then x goes up again) and may
+ * re-sort or migrate them, which it reports through copy_arrays (then the
+ * whole atom set goes up again: x, v, type, mask, f).
  */
 #include "fix_eph_gb.h"
 
@@ -140,6 +141,7 @@ int FixEPHGB::modify_param(int narg, char **arg) {
 
 void FixEPHGB::upload_atoms() {
   const int n = atom->nlocal;
+  reordered = false;
   check(eph_set_atoms(ctx, n, &atom->x[0][0], &atom->v[0][0], atom->type, atom->mask), "set atoms");
   check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "put f");
   nlocal_dev = n;
@@ -150,7 +152,7 @@ void FixEPHGB::setup(int) { upload_atoms(); }
 
 void FixEPHGB::initial_integrate(int) {
   if (eph_flag & 0x08) return;
-  if (nlocal_dev != atom->nlocal) upload_atoms();
+  if (nlocal_dev != atom->nlocal || reordered) upload_atoms();
   // queued copies; the engine's arrays are read again only after the
   // synchronising get at the end of the hook
   check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "put x");
@@ -166,10 +168,12 @@ void FixEPHGB::post_force(int) {
   // so all of them go up again (x, v, type, mask and f); otherwise the device
   // holds this step's x and v since initial_integrate and only the force the
   // engine computed since then goes up
-  if (neighbor->ago == 0 || nlocal_dev != atom->nlocal)
+  if (nlocal_dev != atom->nlocal || reordered) {
     upload_atoms();
-  else
+  } else {
+    if (neighbor->ago == 0) check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "put x");
     check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
+  }
   int source = EPH_XI_DEVICE_RNG;
   if (xi_on_host && (eph_flag & 0x02)) {
     // the engine's own Gaussian stream, three per in-group atom in atom
@@ -203,6 +207,13 @@ void FixEPHGB::end_of_step() {
 
 void FixEPHGB::reset_dt() {
   if (ctx) check(eph_reset_dt(ctx, update->dt), "reset_dt");
+}
+
+// The engine moves atom i's data to slot j (sorting, deleting, migrating
+// atoms): the device's copy is out of order until the next upload.
+void FixEPHGB::copy_arrays(int i, int j, int) {
+  for (int k = 0; k < 8; ++k) array[j][k] = array[i][k];
+  reordered = true;
 }
 
 void FixEPHGB::grow_arrays(int ngrow) {

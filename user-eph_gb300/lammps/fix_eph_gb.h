@@ -53,6 +53,7 @@ class FixEPHGB : public Fix {
   void end_of_step() override;
   void reset_dt() override;
   void grow_arrays(int) override;
+  void copy_arrays(int, int, int) override;
   double compute_vector(int) override;
   void post_run() override;
   int modify_param(int, char **) override;
@@ -67,6 +68,7 @@ class FixEPHGB : public Fix {
   int device = 0;
   int nlocal_dev = -1;            // atom count the device holds
   double list_skin = -1.0;        // fix_modify list_skin (negative: the library's default)
+  bool reordered = false;         // the engine moved atoms between slots since the last upload
   bigint last_upload_step = -1;   // step of the last full atom upload
   class RanMars *random = nullptr;
   std::vector<double> xi;  // deviates drawn on the host (xi host)
