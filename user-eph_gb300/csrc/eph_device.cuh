@@ -276,22 +276,29 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
   return c;
 }
 
-// Three standard normal deviates for atom i at step s (Box-Muller on 32-bit
-// uniforms in (0, 1)).
+// A uniform in (0, 1) with 53 random bits from two 32-bit words:
+// (27 bits of a, 26 of b, + 1/2) * 2^-53.
+__device__ __forceinline__ double uniform53(unsigned a, unsigned b) {
+  const unsigned long long m = ((unsigned long long)(a >> 5) << 26) | (unsigned long long)(b >> 6);
+  return ((double)m + 0.5) * 1.1102230246251565404236316680908203125e-16;
+}
+
+// Three standard normal deviates for atom i at step s: Box-Muller in FP64 on
+// 53-bit uniforms (two Philox4x32-10 blocks, counters differing in their last
+// word), as the reference draws FP64 deviates from RanMars
+// (fix_eph.cpp:854-860).  CUDA's FP64 log, sqrt and sincospi.
 __device__ __forceinline__ void gaussian3(unsigned seed, unsigned long long step, unsigned i, double *g) {
-  const uint4 r = philox4x32_10(make_uint4(i, (unsigned)step, (unsigned)(step >> 32), 0x45504847u),
-                                make_uint2(seed, 0x9e3779b9u));
-  const float u0 = ((float)r.x + 0.5f) * 2.3283064365386963e-10f;
-  const float u1 = ((float)r.y + 0.5f) * 2.3283064365386963e-10f;
-  const float u2 = ((float)r.z + 0.5f) * 2.3283064365386963e-10f;
-  const float u3 = ((float)r.w + 0.5f) * 2.3283064365386963e-10f;
-  const float ra = sqrtf(-2.0f * logf(u0)), rb = sqrtf(-2.0f * logf(u2));
-  float sa, ca, sb, cb;
-  sincospif(2.0f * u1, &sa, &ca);
-  sincospif(2.0f * u3, &sb, &cb);
-  g[0] = (double)(ra * ca);
-  g[1] = (double)(ra * sa);
-  g[2] = (double)(rb * cb);
+  const uint2 key = make_uint2(seed, 0x9e3779b9u);
+  const uint4 r = philox4x32_10(make_uint4(i, (unsigned)step, (unsigned)(step >> 32), 0x45504847u), key);
+  const uint4 q = philox4x32_10(make_uint4(i, (unsigned)step, (unsigned)(step >> 32), 0x45504848u), key);
+  const double u0 = uniform53(r.x, r.y), u1 = uniform53(r.z, r.w);
+  const double u2 = uniform53(q.x, q.y), u3 = uniform53(q.z, q.w);
+  const double ra = sqrt(-2.0 * log(u0)), rb = sqrt(-2.0 * log(u2));
+  double sa, ca;
+  sincospi(2.0 * u1, &sa, &ca);
+  g[0] = ra * ca;
+  g[1] = ra * sa;
+  g[2] = rb * cospi(2.0 * u3);
 }
 
 // ------------------------------------------------- grid parameter tables
