@@ -553,10 +553,19 @@ def run_adjoint_fit(args, dev):
                 "device_memory_in_use_gb": (total - free) / 1e9}
 
 
+# the reference decks' eam/alloy potential (Tests/MD_Run/Ni.eam: 10001-point
+# tables, 6.5 A cut-off), kept xz-compressed with the test fixtures
+REF_NI_EAM = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "ref_inputs",
+                          "MD_Run_Ni.eam.xz")
+
+
 def run_md_eam(args, dev):
-    """Full MD: the bench workload with the engine's eam/alloy pair force
-    (Sutton-Chen Ni tables, 6 A cut-off) added to fix eph: atom-steps/s of the
-    whole step and the pair force's share (phase timing)."""
+    """Full MD: the bench workload with the engine's eam/alloy pair force on
+    the reference decks' Ni.eam (Tests/MD_Run/run.lmp: pair_style eam/alloy)
+    added to fix eph: atom-steps/s of the whole step and the pair force's
+    share (phase timing)."""
+    import lzma
+
     import torch
 
     import ephgb
@@ -564,7 +573,9 @@ def run_md_eam(args, dev):
 
     with tempfile.TemporaryDirectory() as wd:
         words, atoms = make_system(wd)
-        eam = W.write_eam_sutton_chen(os.path.join(wd, "SC_Ni.eam"))
+        eam = os.path.join(wd, "Ni.eam")
+        with open(REF_NI_EAM, "rb") as src, open(eam, "wb") as dst:
+            dst.write(lzma.decompress(src.read()))
         fix = ephgb.FixEPH(words, atoms, dt=DT, mode=ephgb.MODE_FAST, device=dev, eam=(eam, ["Ni"]))
         stream = torch.cuda.Stream()
         fix.set_stream(stream.cuda_stream)
@@ -584,7 +595,8 @@ def run_md_eam(args, dev):
         ph = fix.phase_times()
         fix.set_profiling(False)
         total = sum(v[0] for v in ph.values())
-        return {"workload": WORKLOAD + " + eam/alloy Sutton-Chen Ni (6 A cut-off)", "atoms": atoms.n, "steps": k,
+        return {"workload": WORKLOAD + " + eam/alloy Ni.eam of the reference's MD_Run deck (6.5 A cut-off)",
+                "atoms": atoms.n, "steps": k,
                 "value": atoms.n * k / (ms / 1000.0), "unit": "MD atom-steps/s (pair force + fix eph)",
                 "ms_per_step": ms / k, "pair_share": ph["pair"][0] / total,
                 "phases_ms_per_step": {p: round(v[0] / 10, 4) for p, v in ph.items()},

@@ -1,22 +1,29 @@
 """The engine's eam/alloy pair force on the GPU (eph_set_pair_eam): against a
 numpy restatement that reads the setfl file and builds its tables on its own
 (oracle/eam_ref.py), against the gradient of its own energy, at rest in the
-perfect lattice, and energy conservation of plain NVE.  Parity with LAMMPS's
-pair_style eam/alloy itself is unpinned (LAMMPS is not available); the
-tables follow the same cubic Hermite scheme with five-point slopes."""
+perfect lattice, and energy conservation of plain NVE.  Two potentials: a
+generated Sutton-Chen Ni setfl (6 A cut-off) and the reference decks' own
+Tests/MD_Run/Ni.eam (10001-point tables, 6.5 A cut-off; kept under
+tests/golden/ref_inputs).  Parity with LAMMPS's pair_style eam/alloy itself is
+unpinned (LAMMPS is not available); the tables follow the same cubic Hermite
+scheme with five-point slopes."""
 import numpy as np
 import pytest
 
 import ephgb
 from ephgb import workloads as W
+from golden_io import write_ref_input
 from oracle.eam_ref import energy_forces, read_setfl
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def setfl(tmp_path_factory):
-    return W.write_eam_sutton_chen(str(tmp_path_factory.mktemp("eam") / "SC_Ni.eam"))
+@pytest.fixture(scope="module", params=["sutton_chen_Ni", "MD_Run_Ni"])
+def setfl(request, tmp_path_factory):
+    d = str(tmp_path_factory.mktemp("eam"))
+    if request.param == "MD_Run_Ni":
+        return write_ref_input("MD_Run_Ni.eam", d)
+    return W.write_eam_sutton_chen(d + "/SC_Ni.eam")
 
 
 def forces_at(setfl, beta_file, at, mode=ephgb.MODE_FAST):
@@ -60,7 +67,7 @@ def test_perfect_lattice_is_at_rest(built, setfl, beta_file):
     at = W.fcc_lattice(6, jitter=0.0, seed=63)
     f, E = forces_at(setfl, beta_file, at)
     assert np.abs(f).max() <= 1e-10
-    assert -4.5 < E / at.n < -4.0  # Sutton-Chen Ni cohesion with the 6 A cut-off
+    assert -4.5 < E / at.n < -4.0  # Ni cohesion: Sutton-Chen with the 6 A cut-off, and the reference's Ni.eam
 
 
 def test_nve_conserves_energy(built, setfl, beta_file):
@@ -103,7 +110,7 @@ def test_setup_errors(built, setfl, beta_file, tmp_path):
     assert e.value.status == 1  # EPH_ERR_ARG: element not in the file
     with pytest.raises(ephgb.EphError) as e:
         ephgb.FixEPH(words, W.fcc_lattice(5, seed=66), dt=0.001, eam=(setfl, ["Ni"]))
-    assert e.value.status == 1  # box narrower than three 6 A cut-offs
+    assert e.value.status == 1  # box narrower than three cut-offs (6 and 6.5 A)
     fix = ephgb.FixEPH(words, at, dt=0.001)
     with pytest.raises(ephgb.EphError) as e:
         fix.set_pair_eam(setfl, ["Ni"])
