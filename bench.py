@@ -241,10 +241,10 @@ def run_gpu(args, rank, world):
             # without re-sorting (the knock-on atom moves more than half the skin
             # every step, so LAMMPS rebuilds its lists every step here):
             step_no[0] += 1
-            # initial_integrate: x, v, f in; integrate; x out (queued), v out (synchronising)
+            # initial_integrate: x, v in (the device holds the f final_integrate
+            # sent); integrate; x out (queued), v out (synchronising)
             fix.put("x", xn, asynchronous=True)
             fix.put("v", vn, asynchronous=True)
-            fix.put("f", fn, asynchronous=True)
             fix.initial_integrate()
             fix.get_async("x", xn)
             fix.get("v", vn)
@@ -274,8 +274,8 @@ def run_gpu(args, rank, world):
             host_step()
         torch.cuda.synchronize()
         t_e2e = ranks_reduce(time.perf_counter() - t0, "max", "cuda")
-        # per atom: in x, v, f + x, f + f (6 x 24 B); out x, v + f + v (4 x 24 B) + the array (64 B)
-        out.update(t_e2e=t_e2e, e2e_steps=e2e_steps, h2d=6 * 24 * n, d2h=4 * 24 * n + 64 * n)
+        # per atom: in x, v + x, f + f (5 x 24 B); out x, v + f + v (4 x 24 B) + the array (64 B)
+        out.update(t_e2e=t_e2e, e2e_steps=e2e_steps, h2d=5 * 24 * n, d2h=4 * 24 * n + 64 * n)
     return out
 
 

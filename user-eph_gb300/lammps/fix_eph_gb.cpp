@@ -3,13 +3,16 @@
  * (fix_eph.cpp:293-302) calling the GB300 C ABI.  Atom data stays owned by
  * the engine on the host; each hook copies in what it reads and copies back
  * what it writes:
- *   initial_integrate  x, v, f in   -> device integrate -> x, v out
+ *   initial_integrate  x, v in      -> device integrate -> x, v out
  *   post_force         f in         -> bins, density, force_prl -> f out
  *   final_integrate    f in         -> device integrate -> v out
  *   end_of_step        (device)     -> deposition, FDM, T output; per-atom array
  *                                      out on steps that are multiples of
  *                                      peratom_freq (`fix_modify ID peratom N`,
  *                                      default 1: every step, as the reference)
+ * initial_integrate needs no f: the engine changes f only in its force
+ * computation and in post_force, and final_integrate sent the device the f
+ * left after every fix's post_force (setup() uploads it for the first step).
  * post_force needs no v: initial_integrate copied it back and the engine
  * leaves it alone until post_force.  x changes only when the engine
  * re-neighbours: it wraps atoms into the box (then x goes up again) and may
@@ -157,7 +160,6 @@ void FixEPHGB::initial_integrate(int) {
   // synchronising get at the end of the hook
   check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "put x");
   check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST_ASYNC), "put v");
-  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
   check(eph_initial_integrate(ctx), "initial_integrate");
   check(eph_get(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "get x");
   check(eph_get(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "get v");
