@@ -537,6 +537,18 @@ def run_adjoint_fit(args, dev):
         def werr(b):  # weighted by the share of atoms in each knot interval
             return float(np.sqrt((hist_w * (b - hidden) ** 2).sum() / (hist_w * hidden ** 2).sum()))
 
+        # how strongly the data constrain each knot: its share of the loss
+        # gradient's mass at the flat start (|dL/dbeta_k| / sum |dL/dbeta|)
+        mass = np.abs(g0) / np.abs(g0).sum()
+        order = np.argsort(-mass)
+        top = order[:int(np.searchsorted(np.cumsum(mass[order]), 0.9)) + 1]  # knots holding 90 % of it
+
+        def merr(b):
+            return float(np.sqrt((mass * (b - hidden) ** 2).sum() / (mass * hidden ** 2).sum()))
+
+        def top_err(b):
+            return float(np.linalg.norm((b - hidden)[top]) / np.linalg.norm(hidden[top]))
+
         return {"workload": f"{R} replicas, {atoms_total:,} atoms in all (16k-64k each), T_e0 1,000-5,000 K, FDM 16^3, "
                             f"{nsteps} steps of 1 fs; 64 shared beta knots, Adam on log(beta), {iters} iterations, "
                             "flat initial guess",
@@ -545,6 +557,12 @@ def run_adjoint_fit(args, dev):
                 "beta_rel_err_density_weighted_initial": werr(beta0),
                 "beta_rel_err_density_weighted_final": werr(beta),
                 "knots_holding_atoms": int((hist_w > 0).sum()), "smoothness_weight": 10.0,
+                "gradient_mass_per_knot": [round(float(m), 4) for m in mass],
+                "knots_holding_90pct_of_gradient_mass": sorted(int(k) for k in top),
+                "beta_rel_err_over_those_knots_initial": top_err(beta0),
+                "beta_rel_err_over_those_knots_final": top_err(beta),
+                "beta_rel_err_gradient_mass_weighted_initial": merr(beta0),
+                "beta_rel_err_gradient_mass_weighted_final": merr(beta),
                 "wall_s_per_iteration": wall / iters, "batched_forward_ms": tb["forward_ms"],
                 "batched_backward_ms": tb["backward_ms"],
                 "sequential_forward_plus_backward_s": seq,
