@@ -439,3 +439,22 @@ def test_specified_step_on_the_adjoint_workload(built, tmp_path):
     fd_c = (loss(b0, C_e0 + d) - loss(b0, C_e0 - d)) / (2 * d)
     err_c = abs(g["C_e"] - fd_c) / abs(fd_c)
     assert err_b <= 1e-6 and err_c <= 1e-6, (err_b, err_c)
+
+
+@pytest.mark.parametrize("mode", [ephgb.MODE_FAST, ephgb.MODE_EXACT])
+def test_df64_reverse_sweeps_match_fp64(built, tmp_path, mode):
+    """The reverse pair sweeps in df64 (the default, with the df64 forward)
+    against the FP64 sweeps (eph_set_pair_arithmetic(EPH_PAIRS_FP64), FP64
+    forward and reverse): the same gradients within 1e-9 per group (the two
+    forwards differ in their last bits; the rest is the df64 arithmetic)."""
+    out = []
+    for arith in (ephgb.PAIRS_DF64, ephgb.PAIRS_FP64):
+        fix, _, at, words = make(tmp_path, mode=mode)
+        fix.set_pair_arithmetic(arith)
+        adj = Adjoint(fix, checkpoint_every=5)
+        E, T = adj.forward(STEPS)
+        wE, wT = weights(E, T)
+        out.append(adjoint_grads(adj, wE, wT))
+    for k in out[0]:
+        a, b = np.asarray(out[0][k], dtype=float), np.asarray(out[1][k], dtype=float)
+        assert np.abs(a - b).max() <= 1e-9 * max(np.abs(b).max(), 1e-300), (k, np.abs(a - b).max())

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "eph_ctx_impl.hpp"
+#include "eph_df_pair.cuh"
 
 using namespace ephgb;
 
@@ -602,6 +603,319 @@ __global__ void __launch_bounds__(ABLOCK)
   }
 }
 
+// ------------------------------------------------ reverse sweeps in df64
+// The same two sweeps with every per-pair operation in df64 on the FP32 pipe
+// (the FP64 versions above are bound by FP64 issue): per step, k_adj_split
+// turns each atom's FP64 records into double-float records that the pair
+// loops gather (12 float4 per atom, rows R_*), the pair terms and their sums
+// are formed in df64, and the per-atom work stays FP64.  Positions are split
+// as they are (the boxes of the adjoint's workloads are < 100 A, so the lo
+// parts carry them to ~1e-13 A); the spline is the forward's local-form df64
+// table (value and derivative from the same interval, whose knot receives the
+// coefficient gradient).  Results agree with the FP64 sweeps to ~1e-12.
+constexpr int R_X = 0, R_V = 2, R_WX = 4, R_C = 7, R_W = 10, R_N = 12;
+
+// rows R_X (x, a_i = alpha_i / rho_i or 0), R_V (v, element, live flag),
+// R_WX (w, xi), R_C (cotangents cE, cR) of atom i
+template <bool FAST>
+__global__ void k_adj_split(int n, Slot S, const D4 *__restrict__ cE, const D4 *__restrict__ cR,
+                            float4 *__restrict__ rec) {
+  using namespace df64;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const D4 x = S.x1[i], v = S.v1[i], A = S.A[i], B = S.Bw[i], ce = cE[i], cr = cR[i];
+  const bool live = A.x > 0.0;
+  const df a = from_double(live ? (FAST ? A.y : A.y / A.x) : 0.0);
+  float4 *r = rec + (size_t)R_N * i;
+  const df x0 = from_double(x.x), x1 = from_double(x.y), x2 = from_double(x.z);
+  r[R_X] = make_float4(x0.hi, x1.hi, x2.hi, a.hi);
+  r[R_X + 1] = make_float4(x0.lo, x1.lo, x2.lo, a.lo);
+  const df v0 = from_double(v.x), v1 = from_double(v.y), v2 = from_double(v.z);
+  r[R_V] = make_float4(v0.hi, v1.hi, v2.hi, __int_as_float((int)x.w));
+  r[R_V + 1] = make_float4(v0.lo, v1.lo, v2.lo, live ? 1.0f : 0.0f);
+  const df w0 = from_double(B.y), w1 = from_double(B.z), w2 = from_double(B.w);
+  const df q0 = from_double(A.z), q1 = from_double(A.w), q2 = from_double(B.x);
+  r[R_WX] = make_float4(w0.hi, w1.hi, w2.hi, q0.hi);
+  r[R_WX + 1] = make_float4(w0.lo, w1.lo, w2.lo, q0.lo);
+  r[R_WX + 2] = make_float4(q1.hi, q2.hi, q1.lo, q2.lo);
+  const df e0 = from_double(ce.x), e1 = from_double(ce.y), e2 = from_double(ce.z);
+  const df c0 = from_double(cr.x), c1 = from_double(cr.y), c2 = from_double(cr.z);
+  r[R_C] = make_float4(e0.hi, e1.hi, e2.hi, c0.hi);
+  r[R_C + 1] = make_float4(e0.lo, e1.lo, e2.lo, c0.lo);
+  r[R_C + 2] = make_float4(c1.hi, c2.hi, c1.lo, c2.lo);
+}
+
+struct df3 {
+  df64::df x, y, z;
+};
+__device__ __forceinline__ df3 df3_of(float4 hi, float4 lo) {
+  return df3{df64::df{hi.x, lo.x}, df64::df{hi.y, lo.y}, df64::df{hi.z, lo.z}};
+}
+// the third-row layout {a.hi, b.hi, a.lo, b.lo} with the first component in .w
+__device__ __forceinline__ df3 df3_split(float4 hi, float4 lo, float4 rest) {
+  return df3{df64::df{hi.w, lo.w}, df64::df{rest.x, rest.z}, df64::df{rest.y, rest.w}};
+}
+__device__ __forceinline__ df64::df ddot(const df3 &a, const df3 &b) {
+  return df64::dot3(a.x, a.y, a.z, b.x, b.y, b.z);
+}
+__device__ __forceinline__ df3 dsub(const df3 &a, const df3 &b) {
+  return df3{df64::sub(a.x, b.x), df64::sub(a.y, b.y), df64::sub(a.z, b.z)};
+}
+__device__ __forceinline__ df3 dscale(df64::df s, const df3 &a) {
+  return df3{df64::mul(s, a.x), df64::mul(s, a.y), df64::mul(s, a.z)};
+}
+__device__ __forceinline__ df3 daxpy(df64::df s, const df3 &a, const df3 &y) {  // s a + y
+  return df3{df64::fma(s, a.x, y.x), df64::fma(s, a.y, y.y), df64::fma(s, a.z, y.z)};
+}
+// (x_j + image of code) - x_i from df64 positions
+__device__ __forceinline__ df3 adj_disp(const StepParams &P, float4 jh, float4 jl, float4 ih, float4 il,
+                                        unsigned code) {
+  const int mx = (int)(code % 3u) - 1, my = (int)((code / 3u) % 3u) - 1, mz = (int)(code / 9u) - 1;
+  return df3{pair_disp(mx, jh.x, jl.x, ih.x, il.x, P.prd_hi[0], P.prd_lo[0]),
+             pair_disp(my, jh.y, jl.y, ih.y, il.y, P.prd_hi[1], P.prd_lo[1]),
+             pair_disp(mz, jh.z, jl.z, ih.z, il.z, P.prd_hi[2], P.prd_lo[2])};
+}
+
+// k_adj_sweep1 with the pair loop in df64 (rows R_X, R_V, R_C of k_adj_split);
+// also writes the df64 row R_W of its result for k_adj_sweep2_df
+template <bool FAST, int AMODE>
+__global__ void __launch_bounds__(ABLOCK)
+    k_adj_sweep1_df(StepParams P, Slot S, const int *__restrict__ mask, float4 *__restrict__ rec,
+                    D4 *__restrict__ adjW, double *__restrict__ gpart, double *__restrict__ gglob, int nt4,
+                    unsigned *__restrict__ err) {
+  using namespace df64;
+  extern __shared__ double s_w[];  // AMODE 0: [warps][nt4]
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (AMODE == 0) {
+    for (int q = t; q < (int)(blockDim.x >> 5) * nt4; q += blockDim.x) s_w[q] = 0.0;
+    __syncthreads();
+  }
+  const int i = blockIdx.x * blockDim.x + t;
+  const bool valid = i < P.n;
+  D4 Ai{0.0, 0.0, 0.0, 0.0};
+  bool act = false;
+  if (valid) {
+    Ai = S.A[i];
+    act = (mask[i] & P.groupbit) && Ai.x > 0.0;
+  }
+  acc U[3] = {acc_zero(), acc_zero(), acc_zero()}, V[3] = {acc_zero(), acc_zero(), acc_zero()};
+  D4 xi{0.0, 0.0, 0.0, 0.0};
+  if (act) {
+    xi = S.x1[i];
+    const float4 *ri = rec + (size_t)R_N * i;
+    const float4 ih = ri[R_X], il = ri[R_X + 1];
+    const df3 cei = df3_of(ri[R_C], ri[R_C + 1]), cri = df3_split(ri[R_C], ri[R_C + 1], ri[R_C + 2]);
+    const int ns = S.ns[i];
+    for (int k = 0; k < ns; ++k) {
+      const unsigned u = S.pj[(size_t)k * P.n + i];
+      const unsigned j = u & IDX_MASK;
+      const float4 *rj = rec + (size_t)R_N * j;
+      const float4 vl = rj[R_V + 1];
+      if (!(vl.w > 0.0f)) continue;  // rho_j <= 0
+      const df3 e = adj_disp(P, rj[R_X], rj[R_X + 1], ih, il, u >> IDX_BITS);
+      const df r2 = ddot(e, e);
+      const df H = mul(spline_rho_df(P, __float_as_int(rj[R_V].w), r2, err), recip(r2, rcp_estimate(r2.hi)));
+      const float4 ch = rj[R_C], cl = rj[R_C + 1];
+      const df3 cej = df3_of(ch, cl), crj = df3_split(ch, cl, rj[R_C + 2]);
+      const df dE = mul(H, ddot(e, dsub(cei, cej)));
+      const df dR = mul(H, ddot(e, dsub(cri, crj)));
+      acc_fma(U[0], dE, e.x);
+      acc_fma(U[1], dE, e.y);
+      acc_fma(U[2], dE, e.z);
+      acc_fma(V[0], dR, e.x);
+      acc_fma(V[1], dR, e.y);
+      acc_fma(V[2], dR, e.z);
+    }
+  }
+  const double Ux = to_double(acc_value(U[0])), Uy = to_double(acc_value(U[1])), Uz = to_double(acc_value(U[2]));
+  const double Vx = to_double(acc_value(V[0])), Vy = to_double(acc_value(V[1])), Vz = to_double(acc_value(V[2]));
+  D4 out{0.0, 0.0, 0.0, 0.0};
+  int key = -1;
+  double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+  if (act) {
+    const D4 Bi = S.Bw[i];
+    const double rho = Ai.x;
+    const double a = FAST ? Ai.y : Ai.y / rho;
+    const double ab = fma(2.0, dotf(Bi.y, Bi.z, Bi.w, Ux, Uy, Uz), dotf(Ai.z, Ai.w, Bi.x, Vx, Vy, Vz));
+    out.x = a * Ux;
+    out.y = a * Uy;
+    out.z = a * Uz;
+    if (rho <= P.rho_cutoff) {  // above it alpha is the constant 0 (eph_beta.h:174-197)
+      const int ei = (int)xi.w;
+      double al, ald;
+      int idx;
+      spline_vd(P.tab_alpha + (size_t)ei * P.n_beta, P.inv_drho, P.n_beta, rho, al, ald, idx);
+      const double q = ab / rho;
+      out.w = q * (ald - a);
+      key = ei * P.n_beta + idx;
+      c0 = q;
+      c1 = q * rho;
+      c2 = c1 * rho;
+      c3 = c2 * rho;
+    }
+  }
+  if (valid) {
+    adjW[i] = out;
+    const df o0 = from_double(out.x), o1 = from_double(out.y), o2 = from_double(out.z), o3 = from_double(out.w);
+    rec[(size_t)R_N * i + R_W] = make_float4(o0.hi, o1.hi, o2.hi, o3.hi);
+    rec[(size_t)R_N * i + R_W + 1] = make_float4(o0.lo, o1.lo, o2.lo, o3.lo);
+  }
+  if (AMODE == 0) {
+    warp_add4(s_w + warp * nt4, key, c0, c1, c2, c3, lane);
+    __syncthreads();
+    for (int q = t; q < nt4; q += blockDim.x) {
+      double sum = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += s_w[w * nt4 + q];
+      gpart[(size_t)blockIdx.x * nt4 + q] += sum;
+    }
+  } else if (key >= 0) {
+    atomicAdd(gglob + 4 * key + 0, c0);
+    atomicAdd(gglob + 4 * key + 1, c1);
+    atomicAdd(gglob + 4 * key + 2, c2);
+    atomicAdd(gglob + 4 * key + 3, c3);
+  }
+}
+
+// k_adj_sweep2 with the pair loop in df64 (the same terms, in the same
+// grouping; rows of k_adj_split and R_W of k_adj_sweep1_df).  RMODE 0 keeps
+// its per-thread coefficient accumulators as df64 pairs in shared memory.
+template <bool FAST, bool MULTI, int RMODE>
+__global__ void __launch_bounds__(ABLOCK)
+    k_adj_sweep2_df(StepParams P, Slot S, const int *__restrict__ mask, const int *__restrict__ type,
+                    const float4 *__restrict__ rec, D4 *__restrict__ xb, D4 *__restrict__ vb, D4 *__restrict__ fb,
+                    double *__restrict__ gpart, double *__restrict__ gglob, int nt4) {
+  using namespace df64;
+  extern __shared__ double s_p[];  // RMODE 0: [nt4][blockDim] (hi, lo) pairs
+  float2 *s_pf = reinterpret_cast<float2 *>(s_p);
+  const int t = threadIdx.x, nt = blockDim.x;
+  if (RMODE == 0)
+    for (int q = 0; q < nt4; ++q) s_pf[q * nt + t] = make_float2(0.f, 0.f);
+  const int i = blockIdx.x * blockDim.x + t;
+  const bool grp = i < P.n && (mask[i] & P.groupbit);
+  if (grp) {
+    const float4 *ri = rec + (size_t)R_N * i;
+    const float4 ih = ri[R_X], il = ri[R_X + 1], vh = ri[R_V], vl = ri[R_V + 1];
+    const bool live_i = vl.w > 0.0f;
+    const df ai{ih.w, il.w};
+    const int ei = __float_as_int(vh.w);
+    const df3 vi = df3_of(vh, vl);
+    const float4 wxh = ri[R_WX], wxl = ri[R_WX + 1];
+    const df3 wi = df3_of(wxh, wxl), xii = df3_split(wxh, wxl, ri[R_WX + 2]);
+    const float4 ch = ri[R_C], cl = ri[R_C + 1];
+    const df3 cei = df3_of(ch, cl), cri = df3_split(ch, cl, ri[R_C + 2]);
+    const float4 Oh = ri[R_W], Ol = ri[R_W + 1];
+    const df3 Wi = df3_of(Oh, Ol);
+    const df Wwi{Oh.w, Ol.w};
+    acc gx[3] = {acc_zero(), acc_zero(), acc_zero()}, gv[3] = {acc_zero(), acc_zero(), acc_zero()};
+    const int ns = S.ns[i];
+    for (int k = 0; k < ns; ++k) {
+      const unsigned u = S.pj[(size_t)k * P.n + i];
+      const unsigned j = u & IDX_MASK;
+      const float4 *rj = rec + (size_t)R_N * j;
+      const float4 jxh = rj[R_X], jxl = rj[R_X + 1], jvh = rj[R_V], jvl = rj[R_V + 1];
+      const df3 e = adj_disp(P, jxh, jxl, ih, il, u >> IDX_BITS);
+      const df r2 = ddot(e, e);
+      const df rinv = recip(r2, rcp_estimate(r2.hi));
+      const int ej = __float_as_int(jvh.w);
+      df gj, gjd;
+      int idx;
+      spline_rho_df_vd(P, ej, r2, gj, gjd, idx);
+      const df Hij = mul(gj, rinv), Hpij = mul(sub(gjd, Hij), rinv);
+      df gid = gjd, Hji = Hij, Hpji = Hpij;
+      if (MULTI && ej != ei) {
+        df gi;
+        int idx2;
+        spline_rho_df_vd(P, ei, r2, gi, gid, idx2);
+        Hji = mul(gi, rinv);
+        Hpji = mul(sub(gid, Hji), rinv);
+      }
+      const bool live_j = jvl.w > 0.0f;
+      const df aj{jxh.w, jxl.w};
+      const float4 jOh = rj[R_W], jOl = rj[R_W + 1];
+      const df3 Wj = df3_of(jOh, jOl);
+      const df Wwj{jOh.w, jOl.w};
+      const df3 dv = dsub(vi, df3_of(jvh, jvl));
+      const df e_dv = ddot(e, dv);
+      const df Pi = mul(ai, Hij), Pj = mul(aj, Hji);
+      const df eoi = ddot(e, Wi), eoj = ddot(e, Wj);
+      const df eOd = sub(mul(Pi, eoi), mul(Pj, eoj));
+      df Bi_ = mul(e_dv, eoi), Bj_ = neg(mul(e_dv, eoj));
+      df3 Vi = dscale(e_dv, Wi), Vj = dscale(e_dv, Wj);
+      df3 g = dscale(eOd, dv);
+      if (live_i && live_j) {
+        const float4 jwh = rj[R_WX], jwl = rj[R_WX + 1], jch = rj[R_C], jcl = rj[R_C + 1];
+        const df3 wj = df3_of(jwh, jwl), xij = df3_split(jwh, jwl, rj[R_WX + 2]);
+        const df3 dE = dsub(cei, df3_of(jch, jcl)), dR = dsub(cri, df3_split(jch, jcl, rj[R_C + 2]));
+        const df e_dE = ddot(e, dE), e_dR = ddot(e, dR);
+        const df ewi = ddot(e, wi), ewj = ddot(e, wj), exi = ddot(e, xii), exj = ddot(e, xij);
+        Bi_ = add(Bi_, add(mul(ewi, e_dE), mul(exi, e_dR)));
+        Bj_ = sub(Bj_, add(mul(ewj, e_dE), mul(exj, e_dR)));
+        Vi = daxpy(e_dE, wi, daxpy(e_dR, xii, Vi));
+        Vj = daxpy(e_dE, wj, daxpy(e_dR, xij, Vj));
+        const df eWd = sub(mul(Pi, ewi), mul(Pj, ewj)), eXd = sub(mul(Pi, exi), mul(Pj, exj));
+        g = daxpy(eWd, dE, daxpy(eXd, dR, g));
+      }
+      g = daxpy(Pi, Vi, daxpy(neg(Pj), Vj, g));
+      const df aBi = mul(ai, Bi_);
+      const df s2h = add(add(mul(aBi, Hpij), mul(mul(aj, Bj_), Hpji)), add(mul(Wwi, gjd), mul(Wwj, gid)));
+      const df s2 = add(s2h, s2h);
+      // x cotangent: -(s2 e + g) summed (e = x_j - x_i); v cotangent: e (e.Od)
+      const df3 gs = daxpy(s2, e, g);
+      acc_add(gx[0], gs.x);
+      acc_add(gx[1], gs.y);
+      acc_add(gx[2], gs.z);
+      acc_fma(gv[0], e.x, eOd);
+      acc_fma(gv[1], e.y, eOd);
+      acc_fma(gv[2], e.z, eOd);
+      const df cS = fma(aBi, rinv, Wwi);
+      const int slot = 4 * (ej * P.n_rho + idx);
+      const df c2 = mul(cS, r2), c4 = mul(c2, r2), c6 = mul(c4, r2);
+      if (RMODE == 0) {
+        const df cs[4] = {cS, c2, c4, c6};
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          float2 &cell = s_pf[(slot + m) * nt + t];
+          const df sum = add(df{cell.x, cell.y}, cs[m]);
+          cell = make_float2(sum.hi, sum.lo);
+        }
+      } else {
+        atomicAdd(gglob + slot + 0, to_double(cS));
+        atomicAdd(gglob + slot + 1, to_double(c2));
+        atomicAdd(gglob + slot + 2, to_double(c4));
+        atomicAdd(gglob + slot + 3, to_double(c6));
+      }
+    }
+    const double gxx = -to_double(acc_value(gx[0])), gxy = -to_double(acc_value(gx[1])),
+                 gxz = -to_double(acc_value(gx[2]));
+    const double gvx = to_double(acc_value(gv[0])), gvy = to_double(acc_value(gv[1])),
+                 gvz = to_double(acc_value(gv[2]));
+    const bool integ = !(P.flags & 0x08);
+    const D4 X = xb[i], V = vb[i];
+    const double xbx = X.x + gxx, xby = X.y + gxy, xbz = X.z + gxz;
+    double vbx = V.x + gvx, vby = V.y + gvy, vbz = V.z + gvz;
+    if (integ) {
+      vbx = fma(P.dtv, xbx, vbx);
+      vby = fma(P.dtv, xby, vby);
+      vbz = fma(P.dtv, xbz, vbz);
+    }
+    const double dtfm = integ ? P.dtfm[type[i]] : 0.0;
+    xb[i] = D4{xbx, xby, xbz, 0.0};
+    vb[i] = D4{vbx, vby, vbz, 0.0};
+    fb[i] = D4{dtfm * vbx, dtfm * vby, dtfm * vbz, 0.0};
+  }
+  if (RMODE == 0) {
+    __syncthreads();
+    for (int q = t; q < nt4; q += nt) {
+      double sum = 0.0;
+      for (int tt = 0; tt < nt; ++tt) {
+        const float2 cell = s_pf[q * nt + tt];
+        sum += to_double(df64::df{cell.x, cell.y});
+      }
+      gpart[(size_t)blockIdx.x * nt4 + q] += sum;
+    }
+  }
+}
+
 // sum of the blocks' partial rows, in block order
 __global__ void k_adj_reduce(const double *__restrict__ gpart, int nparts, int nt4, double *__restrict__ acc) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -643,6 +957,7 @@ struct eph_adjoint {
   DevBuf<double> d_E, d_Tm;
   // adjoint state and work arrays
   DevBuf<D4> xb, vb, fb, cE, cR, W;
+  DevBuf<float4> dfr;  // df64 rows of the reverse sweeps (R_N per atom), the pair arithmetic is df64
   DevBuf<double> Tb, u0, u1, srcbar, gC, gK, rho_e;
   DevBuf<double> fdmW;  // [7][ncells]: transposed substep stencil, see k_adj_fdm_weights
   DevBuf<double> g_rho, g_alpha, part_rho, part_alpha;
@@ -816,8 +1131,40 @@ GridArgs grid_args(eph_adjoint *a) {
 }
 
 template <bool FAST>
+void launch_sweeps_df(eph_adjoint *a, const Slot &S) {
+  eph_ctx *c = a->c;
+  const int nb = nb_of(a->n);
+  k_adj_split<FAST><<<nb, ABLOCK, 0, c->stream>>>(a->n, S, a->cE.p, a->cR.p, a->dfr.p);
+  const size_t sh1 = a->amode == 0 ? sizeof(double) * 4 * (size_t)a->nt4_alpha : 0;
+  if (a->amode == 0)
+    k_adj_sweep1_df<FAST, 0><<<nb, ABLOCK, sh1, c->stream>>>(c->P, S, c->mask.p, a->dfr.p, a->W.p, a->part_alpha.p,
+                                                              a->g_alpha.p, a->nt4_alpha, a->d_err.p);
+  else
+    k_adj_sweep1_df<FAST, 1><<<nb, ABLOCK, 0, c->stream>>>(c->P, S, c->mask.p, a->dfr.p, a->W.p, a->part_alpha.p,
+                                                            a->g_alpha.p, a->nt4_alpha, a->d_err.p);
+  const size_t sh2 = a->rmode == 0 ? sizeof(double) * (size_t)a->nt4_rho * ABLOCK : 0;
+#define ADJ_SWEEP2(M, R)                                                                                        \
+  k_adj_sweep2_df<FAST, M, R><<<nb, ABLOCK, sh2, c->stream>>>(c->P, S, c->mask.p, c->type.p, a->dfr.p, a->xb.p, \
+                                                              a->vb.p, a->fb.p, a->part_rho.p, a->g_rho.p,      \
+                                                              a->nt4_rho)
+  if (c->multi) {
+    if (a->rmode == 0) ADJ_SWEEP2(true, 0);
+    else ADJ_SWEEP2(true, 1);
+  } else {
+    if (a->rmode == 0) ADJ_SWEEP2(false, 0);
+    else ADJ_SWEEP2(false, 1);
+  }
+#undef ADJ_SWEEP2
+  a->launches += 3;
+}
+
+template <bool FAST>
 void launch_sweeps(eph_adjoint *a, const Slot &S) {
   eph_ctx *c = a->c;
+  if (c->pair_arith == EPH_PAIRS_DF64) {
+    launch_sweeps_df<FAST>(a, S);
+    return;
+  }
   const int nb = nb_of(a->n);
   const size_t sh1 = a->amode == 0 ? sizeof(double) * 4 * (size_t)a->nt4_alpha : 0;
   if (a->amode == 0)
@@ -1210,6 +1557,7 @@ int eph_adjoint_create(eph_ctx *c, int checkpoint_every, eph_adjoint **out) {
   for (DevBuf<double> *b : {&a->s_T, &a->Tb, &a->u0, &a->u1, &a->srcbar, &a->gC, &a->gK, &a->rho_e})
     ADJ_TRY(a, b->alloc(nc));
   ADJ_TRY(a, a->fdmW.alloc(7 * nc));
+  ADJ_TRY(a, a->dfr.alloc((size_t)R_N * N));
   ADJ_TRY(a, a->s_step.alloc(1));
   ADJ_TRY(a, a->tbc.alloc(N));
   ADJ_TRY(a, a->tb_acc.alloc(nc));
@@ -1233,6 +1581,12 @@ int eph_adjoint_create(eph_ctx *c, int checkpoint_every, eph_adjoint **out) {
     ADJ_TRY(a, cudaFuncSetAttribute(k_adj_sweep2<true, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh));
     ADJ_TRY(a, cudaFuncSetAttribute(k_adj_sweep2<false, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh));
     ADJ_TRY(a, cudaFuncSetAttribute(k_adj_sweep2<false, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh));
+    ADJ_TRY(a, cudaFuncSetAttribute(k_adj_sweep2_df<true, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh));
+    ADJ_TRY(a, cudaFuncSetAttribute(k_adj_sweep2_df<true, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh));
+    ADJ_TRY(a, cudaFuncSetAttribute(k_adj_sweep2_df<false, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    sh));
+    ADJ_TRY(a, cudaFuncSetAttribute(k_adj_sweep2_df<false, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    sh));
   }
   for (cudaEvent_t &e : a->ev) ADJ_TRY(a, cudaEventCreate(&e));
   // the start of every trajectory: the context as it is now

@@ -927,6 +927,8 @@ int eph_create(int narg, const char *const *arg, const eph_md *md, eph_ctx **out
     P.lo[k] = c->boxlo[k];
     P.hi[k] = c->boxhi[k];
     P.prd[k] = c->prd[k];
+    P.prd_hi[k] = (float)P.prd[k];
+    P.prd_lo[k] = (float)(P.prd[k] - (double)P.prd_hi[k]);
   }
   P.rc2 = c->beta.r_cutoff_sq;
   P.rc2_band = (float)(c->beta.r_cutoff_sq * (1.0 + 1e-4));

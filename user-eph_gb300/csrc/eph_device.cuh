@@ -68,6 +68,7 @@ struct StepParams {
   // hi and lo parts of a', b', c', d' with y = a' + t (b' + t (c' + t d')),
   // t = x - k dx)
   float w_hi[3], w_lo[3];
+  float prd_hi[3], prd_lo[3];  // box edges (the adjoint's df64 sweeps: periodic images)
   float rc2_hi, rc2_lo;
   float dxr_hi, dxr_lo, inv_dxr_f;
   const float4 *tab_rho_df;

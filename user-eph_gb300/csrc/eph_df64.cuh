@@ -204,6 +204,14 @@ DF_FN void acc_fma(acc &s, df a, df b) {
   s.lo += te + pe;
 }
 
+// s += a
+DF_FN void acc_add(acc &s, df a) {
+  float t, te;
+  two_sum(s.hi, a.hi, t, te);
+  s.hi = t;
+  s.lo += te + a.lo;
+}
+
 DF_FN df acc_value(acc s) {
   df r;
   fast_two_sum(s.hi, s.lo, r.hi, r.lo);

@@ -16,6 +16,7 @@
 
 #include "eph_device.cuh"
 #include "eph_df64.cuh"
+#include "eph_df_pair.cuh"
 
 namespace ephgb {
 
@@ -575,55 +576,6 @@ __global__ void __launch_bounds__(128) k_density(
 #ifndef DF_UNROLL
 #define DF_UNROLL 1
 #endif
-
-// rho_e(x) of element e at x = r^2 from the local-form df64 table: knot
-// k = floor(x / dx) from the FP32 quotient, moved by one where the df64
-// offset t = x - k dx falls outside [0, dx) (so the interval is that of the
-// df64 x, not of its FP32 part), then y = a' + t (b' + t (c' + t d')).  The
-// local form was expanded from the reference's absolute-form cubic on the
-// host (the same polynomial), so the value is the reference's spline to
-// ~1e-14 without the cancellation of evaluating the absolute form at large x.
-__device__ __forceinline__ df64::df spline_rho_df(const StepParams &P, int e, df64::df x, unsigned *err) {
-  using namespace df64;
-  // floor(x / dx) from the FP32 quotient without a conversion instruction
-  // (floor_estimate; off by one at most, settled by the sign of t below)
-  const float q = x.hi * P.inv_dxr_f;
-  const float kr = floor_estimate(q);
-  int k = floor_estimate_int(kr);
-  float p, pe;
-  two_prod(kr, P.dxr_hi, p, pe);
-  pe = fmaf(kr, P.dxr_lo, pe);
-  float th, te;
-  two_sum(x.hi, -p, th, te);
-  df t = make(th, (te + x.lo) - pe);
-  const df dx = df{P.dxr_hi, P.dxr_lo};
-  if (t.hi < 0.0f) {
-    k -= 1;
-    t = add(t, dx);
-  } else if (!(t.hi < P.dxr_hi)) {
-    k += 1;
-    t = sub(t, dx);
-  }
-  if (k < 0 || k >= P.n_rho) {
-    atomicOr(err, ERR_SPLINE_RANGE);
-    k = k < 0 ? 0 : P.n_rho - 1;
-  }
-  const float4 *c = P.tab_rho_df + 2 * ((size_t)e * P.n_rho + k);
-  const float4 hi = c[0], lo = c[1];
-  return horner(df{hi.x, lo.x}, df{hi.y, lo.y}, df{hi.z, lo.z}, df{hi.w, lo.w}, t);
-}
-
-// displacement component d w + (o_j - o_i) of a pair from the bin offsets
-__device__ __forceinline__ df64::df pair_disp(int d, float ojh, float ojl, float oih, float oil, float wh,
-                                              float wl) {
-  using namespace df64;
-  float s, se;
-  two_sum(ojh, -oih, s, se);
-  const float dw = (float)d * wh;  // exact: d is -1, 0 or 1
-  float s2, se2;
-  two_sum(s, dw, s2, se2);
-  return make(s2, ((ojl - oil) + se) + (se2 + (float)d * wl));
-}
 
 // The FAST density sweep of k_density<true, MULTI, true> (one lane per atom,
 // stage 1 and M_i folded) with every per-pair operation in df64 on the FP32
