@@ -146,12 +146,12 @@ def forces_bytes(n_atoms, n_pairs):
 # workload); the bench's traffic figure is this ratio times the algorithmic
 # bytes at its own size.  Under 1: part of a sweep's pair-cache writes is
 # still in L2 when it ends.
-DENSITY_DRAM_OVER_ALGORITHMIC = 0.845
+DENSITY_DRAM_OVER_ALGORITHMIC = 0.860
 FORCES_DRAM_OVER_ALGORITHMIC = 0.987
 # pipe and issue figures of the two sweeps (ncu, the same capture)
-DENSITY_PIPES = {"issue_active": 0.534, "fma_pipe": 0.262, "alu_pipe": 0.363, "fp64_pipe": 0.131,
+DENSITY_PIPES = {"issue_active": 0.475, "fma_pipe": 0.341, "alu_pipe": 0.130, "fp64_pipe": 0.285,
                  "top_stall": "long_scoreboard"}
-FORCES_PIPES = {"issue_active": 0.363, "fma_pipe": 0.277, "alu_pipe": 0.085, "fp64_pipe": 0.185,
+FORCES_PIPES = {"issue_active": 0.375, "fma_pipe": 0.287, "alu_pipe": 0.082, "fp64_pipe": 0.156,
                 "top_stall": "long_scoreboard"}
 
 
