@@ -183,7 +183,8 @@ int eph_get_threads_per_atom(eph_ctx *ctx, int *tpa);
 int eph_autotune(eph_ctx *ctx, int *chosen);
 
 /* Arithmetic of the FAST-mode per-pair work where the density sweep runs
- * one lane per atom with stage 1 folded (16,384 atoms and more, bin search):
+ * one lane per atom with stage 1 folded (by default from 16,384 atoms on,
+ * with the bin search or the kept candidate lists; model 4):
  * EPH_PAIRS_DF64 (the default) forms every pair term and its sums in
  * double-float -- pairs of FP32 numbers carrying 48 significand bits, on the
  * FP32 pipe, which GB300 issues at 64 times its FP64 rate -- and keeps the

@@ -68,3 +68,26 @@ def test_fix_eph_gb_peratom_every_n_steps(built, beta_file):
             assert np.array_equal(arr, held, equal_nan=True), s  # not copied back on this step
     with pytest.raises(RuntimeError):
         gb.modify("peratom", 0)
+
+
+@pytest.mark.parametrize("pairs", ["fp64", "df64"])
+def test_fix_eph_gb_pair_arithmetic(built, beta_file, pairs):
+    """`fix_modify ID pairs fp64|df64` (kept when a later `fix_modify ID mode
+    fast` makes a new context): both arithmetics match the reference fix to
+    1e-12 per atom; other words are an error."""
+    words, at, dt = scenario("pka", beta_file)
+    words = list(words)
+    words[2] = "eph/gb"
+    gb = GbFix(words, at, dt, 4.6, mode=1, xi_host=1)
+    gb.modify("pairs", pairs)
+    gb.modify("mode", "fast")
+    ref = OracleFix(words, at, dt)
+    ng = n_in_group(at)
+    for s in range(8):
+        xi = W.gaussian_stream(ng, 31, s)
+        gb.step(xi)
+        ref.step(xi)
+        for k in ("x", "v", "f", "array"):
+            assert key_err(k, gb.get(k), ref.get(k)) <= 1e-12, (pairs, s, k)
+    with pytest.raises(RuntimeError):
+        gb.modify("pairs", "fp32")

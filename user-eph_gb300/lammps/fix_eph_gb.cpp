@@ -98,8 +98,10 @@ void FixEPHGB::create_context() {
   md.device = device;
   md.mode = mode;
   check(eph_create((int)words.size(), words.data(), &md, &ctx), "create");
-  // a list skin set by fix_modify outlives contexts made by later fix_modify words
+  // a list skin or pair arithmetic set by fix_modify outlives contexts made
+  // by later fix_modify words
   if (list_skin >= 0.0) check(eph_set_list_skin(ctx, list_skin), "list skin");
+  if (pair_arith >= 0) check(eph_set_pair_arithmetic(ctx, pair_arith), "pair arithmetic");
   nlocal_dev = -1;
 }
 
@@ -126,6 +128,17 @@ int FixEPHGB::modify_param(int narg, char **arg) {
   } else if (strcmp(arg[0], "list_skin") == 0) {
     list_skin = atof(arg[1]);
     check(eph_set_list_skin(ctx, list_skin), "list skin");
+    return 2;
+  } else if (strcmp(arg[0], "pairs") == 0) {
+    // arithmetic of the FAST pair sums: df64 (double-float on the FP32 pipe,
+    // the default) or fp64
+    if (strcmp(arg[1], "df64") == 0)
+      pair_arith = EPH_PAIRS_DF64;
+    else if (strcmp(arg[1], "fp64") == 0)
+      pair_arith = EPH_PAIRS_FP64;
+    else
+      error->all(FLERR, "fix_modify eph/gb pairs: df64 or fp64");
+    check(eph_set_pair_arithmetic(ctx, pair_arith), "pair arithmetic");
     return 2;
   } else if (strcmp(arg[0], "peratom") == 0) {
     // computes, dumps and variables read the per-atom array only on steps
