@@ -38,6 +38,8 @@ sys.path.insert(0, REPO)
 CELLS = 80
 GRID = (64, 64, 64)
 DT = 0.0005
+# list skins (A) that --autotune-skin times (0: the bin search every step)
+SKIN_CANDIDATES = (0.0, 0.15, 0.2, 0.3, 0.4, 0.6)
 PKA_EV = 10000.0
 SEED = 4242
 WORKLOAD = "fcc Ni 80^3 cells (2,048,000 atoms), 10 keV PKA, dt 0.5 fs, FDM 64^3, flags 7, model 4"
@@ -196,6 +198,12 @@ def run_gpu(args, rank, world):
         # ---------------------------------------------- device-resident value
         fix.step(args.warmup)
         fix.synchronize()
+        tuned = None
+        if args.autotune_skin:
+            # eph_autotune_list_skin: trial windows from this state, restored
+            tuned = fix.autotune_list_skin(SKIN_CANDIDATES, steps=args.autotune_steps)
+            fix.step(2)  # the build of the chosen radius, outside the timed steps
+            fix.synchronize()
         if world > 1:
             torch.distributed.barrier()
         builds0 = fix.counter("build")
@@ -219,7 +227,8 @@ def run_gpu(args, rank, world):
         fix.set_profiling(False)
         n_pairs = fix.pair_count()
         out.update(ms=ms, phases=phases, launches=launches, n_pairs=n_pairs, clocks=clock, n=n,
-                   rebuilds=fix.counter("wrap"), list_builds=fix.counter("build") - builds0, list_skin=fix.list_skin())
+                   rebuilds=fix.counter("wrap"), list_builds=fix.counter("build") - builds0, list_skin=fix.list_skin(),
+                   skin_autotuned=tuned)
         if args.no_e2e:
             return out
         # ------------------------------------------------ end to end (host)
@@ -241,28 +250,19 @@ def run_gpu(args, rank, world):
             # without re-sorting (the knock-on atom moves more than half the skin
             # every step, so LAMMPS rebuilds its lists every step here):
             step_no[0] += 1
-            # initial_integrate: x, v in (the device holds the f final_integrate
-            # sent); integrate; x out (queued), v out (synchronising)
-            fix.put("x", xn, asynchronous=True)
-            fix.put("v", vn, asynchronous=True)
-            fix.initial_integrate()
-            fix.get_async("x", xn)
-            fix.get("v", vn)
-            # post_force after the engine's re-neighbouring: x (wrapped) and the
-            # engine's pair force (none) in; forces; f out
-            fix.put("x", xn, asynchronous=True)
-            fix.put("f", f0, asynchronous=True)
-            fix.post_force()
-            fix.get("f", fn)
-            # final_integrate: f in; integrate; v out
-            fix.put("f", fn, asynchronous=True)
-            fix.final_integrate()
-            fix.get("v", vn)
-            # end_of_step: deposition and grid; the per-atom array out (peratom
-            # every step, the fix's default)
+            # initial_integrate: x, v in, the half kick and drift, x, v out
+            # (the device keeps the f final_integrate sent)
+            fix.initial_integrate_host(xn, vn)
+            # post_force after the engine's re-neighbouring: x (wrapped) and
+            # the engine's pair force (none) in, forces, f out; the per-atom
+            # array (peratom every step, the fix's default) leaves on its own
+            # stream and is in place when end_of_step returns
+            fix.post_force_host(xn, fn, arr, f_in=f0)
+            # final_integrate: f in, the half kick, v out
+            fix.final_integrate_host(fn, vn)
+            # end_of_step: deposition and the grid
             fix.set_timestep(step_no[0])
             fix.end_of_step()
-            fix.get("array", arr)
 
         for _ in range(2):
             host_step()
@@ -730,6 +730,9 @@ def main():
     ap.add_argument("--fit-iters", type=int, default=60)
     ap.add_argument("--cells", type=int, default=CELLS, help="fcc cells per edge (profiling cases)")
     ap.add_argument("--grid", type=int, default=GRID[0], help="FDM cells per edge (profiling cases)")
+    ap.add_argument("--autotune-skin", action="store_true",
+                    help="choose the list skin by eph_autotune_list_skin before the timed steps")
+    ap.add_argument("--autotune-steps", type=int, default=40, help="steps per trial window of --autotune-skin")
     ap.add_argument("--list-skin", type=float, default=None,
                     help="skin of the kept candidate lists in A (0: bin search every step; default: the library's)")
     args = ap.parse_args()
@@ -806,6 +809,9 @@ def main():
         "list_skin_A": res["list_skin"][0] if res["list_skin"][1] else 0.0,
         "list_builds": res["list_builds"],  # in the timed steps
     }
+    if res.get("skin_autotuned") is not None:
+        line["list_skin_autotuned"] = {"candidates_A": list(SKIN_CANDIDATES), "chosen_A": res["skin_autotuned"],
+                                       "window_steps": args.autotune_steps}
     if "t_e2e" in res:
         line["e2e"] = {"value": world * n * res["e2e_steps"] / res["t_e2e"], "unit": METRIC,
                        "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"], "steps": res["e2e_steps"],

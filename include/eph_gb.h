@@ -17,6 +17,8 @@
 #ifndef EPH_GB_H
 #define EPH_GB_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -121,6 +123,32 @@ int eph_final_integrate(eph_ctx *ctx);
  * steps, Ee accumulation. */
 int eph_end_of_step(eph_ctx *ctx);
 
+/* The hooks with the engine's own host arrays (n x 3 doubles, atom order;
+ * pinned or registered with eph_pin for the copies to run at the host
+ * link's rate), each equal to the eph_put / hook / eph_get sequence it
+ * replaces, with the copies overlapped: the atoms go in chunks whose
+ * host->device and device->host copies run at once on two copy streams, and
+ * the context's stream runs one fused kernel per chunk.  Each returns when
+ * the arrays it writes hold the results (the per-atom array of
+ * eph_post_force_host: when eph_end_of_step or eph_synchronize returns).
+ * initial_integrate: x, v in; the half kick and drift; x, v out (in place). */
+int eph_initial_integrate_host(eph_ctx *ctx, double *x, double *v);
+/* post_force: x in when not NULL (a re-neighbouring step: the engine wrapped
+ * it; otherwise the device keeps the x of initial_integrate), f_in in (the
+ * engine's force; its copy overlaps the binning and the density sweep),
+ * f_EPH + f_RNG added, the total out into f_out (which may be f_in: the
+ * engine's own f array); with array not NULL the fix's per-atom array
+ * (n x 8: rho, beta, f_EPH, f_RNG, fix_eph.cpp:406-428) is copied into it on
+ * a third stream while the next hooks run. */
+int eph_post_force_host(eph_ctx *ctx, const double *x, const double *f_in, double *f_out, double *array,
+                        int xi_source);
+/* final_integrate: f in; the half kick; v out. */
+int eph_final_integrate_host(eph_ctx *ctx, const double *f, double *v);
+/* Page-lock (and unlock) a host range for the copies above (the engine's
+ * atom arrays, which it allocates itself); a range may be pinned once. */
+int eph_pin(void *p, size_t bytes);
+int eph_unpin(void *p);
+
 /* nsteps engine steps on the device (Verlet::run order): initial_integrate,
  * position wrap when an atom moved > skin/2, force = external force,
  * post_force, final_integrate, end_of_step.  Device-resident; with
@@ -181,6 +209,25 @@ int eph_get_threads_per_atom(eph_ctx *ctx, int *tpa);
  * (after at least one step; forces and memories are restored) and keep the
  * fastest; *chosen gets it (may be NULL). */
 int eph_autotune(eph_ctx *ctx, int *chosen);
+/* Time a window of `steps` engine steps (eph_step with device deviates,
+ * direct launches) from the current state with each list skin of
+ * skins[0..nskins-1] (0 = the bin search every step), each window starting
+ * with a list build as a run does after eph_set_list_skin (one untimed
+ * window first), then restore the state -- positions, velocities, forces,
+ * memories, deviates, per-atom records, the grid, the vector, counters and
+ * step counters; no T_out file is written -- and keep the skin of the fastest
+ * window; *chosen gets it (may be NULL).  The bins' edge is r_cutoff + skin
+ * (their 27-bin stencil), so this chooses the bin size too.  A window that
+ * overflows the bins or pair rows rules its skin out.  The trajectory from
+ * here is the one eph_set_list_skin(ctx, *chosen) would give at this point:
+ * the order of the sums, and so the last bits, depend on the skin.  Where no
+ * skin turns the lists on (EXACT mode, model 1, several lanes per atom below
+ * 16,384 atoms, the EAM engine, an adjoint, a box narrower than three list
+ * radii) nothing runs and *chosen gets the current skin.  Needs one step (or
+ * post_force) first and ~0.4 KB of device memory per atom for the saved
+ * state.  No reference counterpart (the reference takes its pairs from the
+ * engine's Verlet list, whose skin the user sets, fix_eph.cpp:273-275). */
+int eph_autotune_list_skin(eph_ctx *ctx, const double *skins, int nskins, int steps, double *chosen);
 
 /* Arithmetic of the FAST-mode per-pair work where the density sweep runs
  * one lane per atom with stage 1 folded (by default from 16,384 atoms on,

@@ -179,3 +179,47 @@ def test_when_reuse_is_off(built, beta_file):
     fix.step(2)
     with pytest.raises(ephgb.EphError):
         fix.set_list_skin(-1.0)
+
+
+def test_autotune_list_skin_restores_the_state(built, beta_file, tmp_path):
+    """eph_autotune_list_skin times windows of steps with each candidate skin
+    from the current state and restores it: afterwards the context holds the
+    state it had (x, v, f, T_e, the vector, the per-atom records), writes no
+    temperature file of its trial steps, and steps on bit for bit as a twin
+    context given eph_set_list_skin(chosen) at the same point."""
+    at = W.fcc_lattice(16, seed=71)  # 16,384 atoms: one lane per atom
+    W.add_pka(at, 2000.0, seed=72)
+    tout = str(tmp_path / "Te_out")
+    words = W.fix_args(beta_file, grid=(8, 8, 8), T_freq=5, T_out=tout)
+    fixes = [ephgb.FixEPH(words, at, dt=0.0005, mode=ephgb.MODE_FAST) for _ in range(2)]
+    for f in fixes:
+        f.step(6)
+    before = {k: fixes[0].get(k) for k in ("x", "v", "f", "T", "rho", "w", "f_eph", "f_rng")}
+    E0 = fixes[0].compute_vector(0)
+    written = sorted(p.name for p in tmp_path.iterdir())
+    chosen = fixes[0].autotune_list_skin((0.0, 0.15, 0.3, 0.6), steps=8)
+    assert chosen in (0.0, 0.15, 0.3, 0.6)
+    assert fixes[0].list_skin()[0] == chosen
+    for k, a in before.items():
+        assert np.array_equal(fixes[0].get(k), a), k
+    assert fixes[0].compute_vector(0) == E0
+    assert sorted(p.name for p in tmp_path.iterdir()) == written  # no T_out of the trial steps
+    fixes[1].set_list_skin(chosen)
+    for f in fixes:
+        f.step(12)
+    for k in ("x", "v", "f", "T", "f_eph"):
+        assert np.array_equal(fixes[0].get(k), fixes[1].get(k)), k
+    assert fixes[0].compute_vector(0) == fixes[1].compute_vector(0)
+    assert sorted(p.name for p in tmp_path.iterdir()) != written  # the real steps write theirs
+
+
+def test_autotune_list_skin_where_lists_do_not_apply(built, beta_file):
+    """EXACT mode keeps the bin search: nothing runs, the skin stays"""
+    at = W.fcc_lattice(16, seed=73)
+    fix = ephgb.FixEPH(W.fix_args(beta_file, grid=(8, 8, 8)), at, dt=0.0005, mode=ephgb.MODE_EXACT)
+    fix.step(2)
+    x = fix.get("x")
+    assert fix.autotune_list_skin((0.2, 0.5), steps=4) == fix.list_skin()[0]
+    assert np.array_equal(fix.get("x"), x)
+    with pytest.raises(ephgb.EphError):
+        fix.autotune_list_skin((-1.0,), steps=4)

@@ -576,6 +576,14 @@ int launch_pair_sweeps(eph_ctx *c, int xi_mode) {
       else launch_density_t<false, false>(c, xi_mode);
     }
   }
+  // eph_post_force_host: the engine's force, uploaded while the density
+  // sweep ran, goes into f before the force sweeps add to it
+  if (c->f_pending) {
+    CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->f_ready, 0));
+    k_pack3<<<nblocks(c->n), BLOCK, 0, c->stream>>>(c->n, c->hstage.p + 3 * (size_t)c->n, c->f.p);
+    c->f_pending = false;
+    c->launches += 1;
+  }
   if (c->args.model == 1) {  // force_ttm: per-atom, no pair sums
     PhaseScope ps(c, EPH_PHASE_FORCES);
     ps.launched();
@@ -971,6 +979,14 @@ void eph_destroy(eph_ctx *c) {
   drop_graph(c);
   collect_marks(c);
   for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
+  for (cudaStream_t s : {c->s_in, c->s_out, c->s_arr})
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  for (cudaEvent_t e : c->xev) cudaEventDestroy(e);
+  if (c->f_ready) cudaEventDestroy(c->f_ready);
+  if (c->arr_done) cudaEventDestroy(c->arr_done);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->h_bounds) cudaFreeHost(c->h_bounds);
@@ -1017,11 +1033,13 @@ int eph_set_pair_arithmetic(eph_ctx *c, int which) {
   return c->n > 0 ? configure_list(c) : EPH_OK;  // the lists' default range depends on it
 }
 
-int eph_set_list_skin(eph_ctx *c, double skin) {
-  if (!c || !(skin >= 0.0)) return EPH_ERR_ARG;
+namespace {
+// the list skin and whether it was the caller's choice (a caller's skin
+// applies at any size), then the bins and lists of the new radius
+int apply_list_skin(eph_ctx *c, double skin, bool user) {
   drop_graph(c);
   c->lskin = skin;
-  c->lskin_user = true;
+  c->lskin_user = user;
   if (c->n <= 0) return EPH_OK;
   const bool was = c->reuse;
   if (was) drop_list(c);  // a new radius: new bins and lists
@@ -1036,6 +1054,12 @@ int eph_set_list_skin(eph_ctx *c, double skin) {
     c->buf_gen += 1;
   }
   return EPH_OK;
+}
+}  // namespace
+
+int eph_set_list_skin(eph_ctx *c, double skin) {
+  if (!c || !(skin >= 0.0)) return EPH_ERR_ARG;
+  return apply_list_skin(c, skin, true);
 }
 
 int eph_get_list_skin(eph_ctx *c, double *skin, int *active) {
@@ -1109,6 +1133,139 @@ int eph_autotune(eph_ctx *c, int *chosen) {
   cudaEventDestroy(e1);
   r = eph_set_threads_per_atom(c, best);
   if (r) return r;
+  if (chosen) *chosen = best;
+  return EPH_OK;
+}
+
+int eph_autotune_list_skin(eph_ctx *c, const double *skins, int nskins, int steps, double *chosen) {
+  if (!c || !skins || nskins < 1 || steps < 1) return EPH_ERR_ARG;
+  for (int k = 0; k < nskins; ++k)
+    if (!(skins[k] >= 0.0)) return fail(c, EPH_ERR_ARG, "list skin must be >= 0");
+  int r = require_atoms(c);
+  if (r) return r;
+  // where no skin can turn the lists on (EXACT, model 1, several lanes per
+  // atom below 16,384 atoms, the EAM engine, an adjoint, a box narrower
+  // than three list radii for every candidate) nothing runs
+  bool applies = false;
+  {
+    const double keep_s = c->lskin;
+    const bool keep_u = c->lskin_user;
+    c->lskin_user = true;
+    for (int k = 0; k < nskins && !applies; ++k) {
+      c->lskin = skins[k];
+      applies = skins[k] > 0.0 && want_list(c);
+    }
+    c->lskin = keep_s;
+    c->lskin_user = keep_u;
+  }
+  if (!applies) {
+    if (chosen) *chosen = c->lskin;
+    return EPH_OK;
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  unsigned long long calls = 0;
+  CUDA_TRY(c, cudaMemcpy(&calls, c->step_ctr.p, sizeof(calls), cudaMemcpyDeviceToHost));
+  if (calls == 0) return fail(c, EPH_ERR_STATE, "list-skin autotune needs one step (or post_force) first");
+  // the state a step reads or a caller may read back afterwards
+  const size_t N = (size_t)c->n, NC = (size_t)c->grid.ntotal;
+  DevBuf<D4> *d4[] = {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->f_dis, &c->f_sto, &c->xi, &c->A, &c->Bw};
+  const int ND4 = (int)(sizeof(d4) / sizeof(d4[0]));
+  DevBuf<D4> s_d4[ND4];
+  DevBuf<double> s_rho, s_beta, s_T, s_scal;
+  DevBuf<unsigned long long> s_cnt, s_step;
+  DevBuf<int> s_wrap;
+  for (int k = 0; k < ND4; ++k) CUDA_TRY(c, s_d4[k].alloc(N));
+  CUDA_TRY(c, s_rho.alloc(N));
+  CUDA_TRY(c, s_beta.alloc(N));
+  CUDA_TRY(c, s_T.alloc(NC));
+  CUDA_TRY(c, s_scal.alloc(4));
+  CUDA_TRY(c, s_cnt.alloc(NCOUNTERS));
+  CUDA_TRY(c, s_step.alloc(1));
+  CUDA_TRY(c, s_wrap.alloc(1));
+  auto copy_all = [&](bool save) -> cudaError_t {
+    cudaError_t e = cudaSuccess;
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+      if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, c->stream);
+    };
+    auto pair = [&](void *live, void *kept, size_t bytes) { save ? cp(kept, live, bytes) : cp(live, kept, bytes); };
+    for (int k = 0; k < ND4; ++k) pair(d4[k]->p, s_d4[k].p, sizeof(D4) * N);
+    pair(c->rho.p, s_rho.p, sizeof(double) * N);
+    pair(c->beta_i.p, s_beta.p, sizeof(double) * N);
+    pair(c->T0.p, s_T.p, sizeof(double) * NC);
+    pair(c->scal.p, s_scal.p, sizeof(double) * 4);
+    pair(c->counters.p, s_cnt.p, sizeof(unsigned long long) * NCOUNTERS);
+    pair(c->step_ctr.p, s_step.p, sizeof(unsigned long long));
+    pair(c->wrapflag.p, s_wrap.p, sizeof(int));
+    return e;
+  };
+  CUDA_TRY(c, copy_all(true));
+  const long keep_ts = c->ntimestep, keep_launches = c->launches;
+  const int keep_freq = c->args.T_freq;
+  const bool keep_prof = c->profiling;
+  const double keep_skin = c->lskin;
+  const bool keep_user = c->lskin_user;
+  c->args.T_freq = 0;  // no temperature files from trial steps
+  c->profiling = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CUDA_TRY(c, cudaEventCreate(&e0));
+  CUDA_TRY(c, cudaEventCreate(&e1));
+  const int xi_mode = 0;  // device deviates: timing only
+  double best = keep_skin;
+  float best_ms = 1e30f;
+  int status = EPH_OK;
+  for (int k = 0; k < nskins && status == EPH_OK; ++k) {
+    // each window starts from the saved state with a list build, as a run
+    // does after eph_set_list_skin; one untimed window first settles the
+    // allocations of the new radius
+    for (int rep = 0; rep < 2 && status == EPH_OK; ++rep) {
+      if (copy_all(false) != cudaSuccess) {
+        status = fail(c, EPH_ERR_CUDA, "restoring the state");
+        break;
+      }
+      if ((status = apply_list_skin(c, skins[k], true)) != EPH_OK) break;
+      if (cudaEventRecord(e0, c->stream) != cudaSuccess) {
+        status = fail(c, EPH_ERR_CUDA, "event");
+        break;
+      }
+      for (int s = 0; s < steps && status == EPH_OK; ++s) {
+        c->ntimestep += 1;
+        status = record_step(c, xi_mode);
+      }
+      if (status != EPH_OK) break;
+      float ms = 0.f;
+      if (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        status = fail(c, EPH_ERR_CUDA, "timing a trial window");
+        break;
+      }
+      if ((status = check_device(c)) == EPH_ERR_CAPACITY) {
+        status = EPH_OK;  // this radius overflows the bins or pair rows: not a candidate
+        break;
+      }
+      if (status != EPH_OK) break;
+      if (rep == 1 && ms < best_ms) {
+        best_ms = ms;
+        best = skins[k];
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->args.T_freq = keep_freq;
+  c->profiling = keep_prof;
+  c->ntimestep = keep_ts;
+  c->launches = keep_launches;
+  if (copy_all(false) != cudaSuccess && status == EPH_OK) status = fail(c, EPH_ERR_CUDA, "restoring the state");
+  if (status != EPH_OK) {
+    apply_list_skin(c, keep_skin, keep_user);  // as it was (the lists rebuild on the next step)
+    return status;
+  }
+  if (!(best_ms < 1e30f)) {
+    apply_list_skin(c, keep_skin, keep_user);
+    return fail(c, EPH_ERR_CAPACITY, "every candidate list skin overflows the bins or pair rows");
+  }
+  if ((r = apply_list_skin(c, best, true))) return r;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   if (chosen) *chosen = best;
   return EPH_OK;
 }
@@ -1309,7 +1466,196 @@ int eph_end_of_step(eph_ctx *c) {
   if (r) return r;
   r = launch_end_of_step(c);
   if (r) return r;
+  if (c->arr_pending) {  // the per-atom array eph_post_force_host sent out
+    CUDA_TRY(c, cudaEventSynchronize(c->arr_done));
+    c->arr_pending = false;
+  }
   return write_T_output(c);
+}
+
+}  // extern "C"
+
+namespace {
+
+constexpr int HOST_CHUNKS = 8;          // chunks of a pipelined host exchange
+constexpr int HOST_CHUNK_MIN = 1 << 16;  // atoms per chunk at least
+
+// the copy streams, chunk events and staging rows of the host-array hooks
+int host_io_ready(eph_ctx *c) {
+  for (cudaStream_t *s : {&c->s_in, &c->s_out, &c->s_arr})
+    if (!*s) CUDA_TRY(c, cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
+  while (c->xev.size() < 2 * HOST_CHUNKS + 2) {
+    cudaEvent_t e;
+    CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->xev.push_back(e);
+  }
+  if (!c->f_ready) CUDA_TRY(c, cudaEventCreateWithFlags(&c->f_ready, cudaEventDisableTiming));
+  if (!c->arr_done) CUDA_TRY(c, cudaEventCreateWithFlags(&c->arr_done, cudaEventDisableTiming));
+  const size_t need = 20 * (size_t)c->n;
+  if (c->hstage.n != need) {
+    if (c->arr_pending) CUDA_TRY(c, cudaEventSynchronize(c->arr_done));
+    c->arr_pending = false;
+    CUDA_TRY(c, c->hstage.alloc(need));
+  }
+  return EPH_OK;
+}
+
+// the per-atom array copied out by eph_post_force_host: written before the
+// host reads it or its staging is reused
+int host_array_wait(eph_ctx *c) {
+  if (c->arr_pending) {
+    CUDA_TRY(c, cudaEventSynchronize(c->arr_done));
+    c->arr_pending = false;
+  }
+  return EPH_OK;
+}
+
+// Chunk k of n atoms in `chunks` pieces: [base, base + count)
+void chunk_range(int n, int chunks, int k, int &base, int &count) {
+  const long b = (long)n * k / chunks, e = (long)n * (k + 1) / chunks;
+  base = (int)b;
+  count = (int)(e - b);
+}
+
+// A hook with the engine's host arrays, pipelined over chunks of atoms: the
+// rows of `in` (n x 3 doubles each) go up on the copy-in stream, `kernel`
+// (the fused pack + hook + unpack of one chunk) runs on the context's
+// stream, and the rows it staged for `out` come back on the copy-out
+// stream, so that the copies of one chunk overlap those of its neighbours in
+// both directions of the host link.  Returns when `out` is written.
+template <class Kernel>
+int host_pipeline(eph_ctx *c, const double *const *in, int nin, double *const *out, int nout, Kernel kernel) {
+  const size_t N = (size_t)c->n;
+  const int chunks = std::max(1, std::min(HOST_CHUNKS, c->n / HOST_CHUNK_MIN));
+  double *sin = c->hstage.p, *sout = c->hstage.p + 3 * N * (size_t)nin;
+  for (int k = 0; k < chunks; ++k) {
+    int base, count;
+    chunk_range(c->n, chunks, k, base, count);
+    const size_t off = 3 * (size_t)base, bytes = 3 * sizeof(double) * (size_t)count;
+    for (int q = 0; q < nin; ++q)
+      CUDA_TRY(c, cudaMemcpyAsync(sin + 3 * N * q + off, in[q] + off, bytes, cudaMemcpyHostToDevice, c->s_in));
+    cudaEvent_t e_in = c->xev[2 * k], e_done = c->xev[2 * k + 1];
+    CUDA_TRY(c, cudaEventRecord(e_in, c->s_in));
+    CUDA_TRY(c, cudaStreamWaitEvent(c->stream, e_in, 0));
+    kernel(base, count, sin + off, sout + off);
+    c->launches += 1;
+    CUDA_TRY(c, cudaGetLastError());
+    CUDA_TRY(c, cudaEventRecord(e_done, c->stream));
+    CUDA_TRY(c, cudaStreamWaitEvent(c->s_out, e_done, 0));
+    for (int q = 0; q < nout; ++q)
+      CUDA_TRY(c, cudaMemcpyAsync(out[q] + off, sout + 3 * N * q + off, bytes, cudaMemcpyDeviceToHost, c->s_out));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->s_out));
+  return EPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int eph_initial_integrate_host(eph_ctx *c, double *x, double *v) {
+  if (!c || !x || !v) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r || (r = host_io_ready(c))) return r;
+  const size_t N = (size_t)c->n;
+  const double *in[2] = {x, v};
+  double *out[2] = {x, v};
+  PhaseScope ps(c, EPH_PHASE_INTEGRATE);
+  return host_pipeline(c, in, 2, out, 2, [&](int base, int count, const double *s, double *o) {
+    StepParams P = c->P;
+    const int nb = nblocks(count);
+    const size_t b = (size_t)base;
+    if (c->mode == EPH_MODE_FAST)
+      k_initial_host<true><<<nb, BLOCK, 0, c->stream>>>(P, count, s, s + 3 * N, c->x.p + b, c->v.p + b, c->f.p + b,
+                                                        c->type.p + b, c->mask.p + b, o, o + 3 * N);
+    else
+      k_initial_host<false><<<nb, BLOCK, 0, c->stream>>>(P, count, s, s + 3 * N, c->x.p + b, c->v.p + b, c->f.p + b,
+                                                         c->type.p + b, c->mask.p + b, o, o + 3 * N);
+  });
+}
+
+int eph_final_integrate_host(eph_ctx *c, const double *f, double *v) {
+  if (!c || !f || !v) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r || (r = host_io_ready(c))) return r;
+  const double *in[1] = {f};
+  double *out[1] = {v};
+  PhaseScope ps(c, EPH_PHASE_INTEGRATE);
+  return host_pipeline(c, in, 1, out, 1, [&](int base, int count, const double *s, double *o) {
+    const int nb = nblocks(count);
+    const size_t b = (size_t)base;
+    if (c->mode == EPH_MODE_FAST)
+      k_final_host<true><<<nb, BLOCK, 0, c->stream>>>(c->P, count, s, c->f.p + b, c->v.p + b, c->type.p + b,
+                                                      c->mask.p + b, o);
+    else
+      k_final_host<false><<<nb, BLOCK, 0, c->stream>>>(c->P, count, s, c->f.p + b, c->v.p + b, c->type.p + b,
+                                                       c->mask.p + b, o);
+  });
+}
+
+int eph_pin(void *p, size_t bytes) {
+  if (!p || !bytes) return EPH_ERR_ARG;
+  if (cudaHostRegister(p, bytes, cudaHostRegisterDefault) == cudaSuccess) return EPH_OK;
+  cudaGetLastError();  // not sticky: the copies then run from pageable memory
+  return EPH_ERR_CUDA;
+}
+
+int eph_unpin(void *p) {
+  if (!p) return EPH_ERR_ARG;
+  if (cudaHostUnregister(p) == cudaSuccess) return EPH_OK;
+  cudaGetLastError();
+  return EPH_ERR_CUDA;
+}
+
+int eph_post_force_host(eph_ctx *c, const double *x, const double *f_in, double *f_out, double *array,
+                        int xi_source) {
+  if (!c || !f_in || !f_out) return EPH_ERR_ARG;
+  int r = require_atoms(c);
+  if (r || (r = host_io_ready(c)) || (r = host_array_wait(c))) return r;
+  if (xi_source == EPH_XI_GIVEN && !c->have_xi && (c->P.flags & FLAG_RANDOM))
+    return fail(c, EPH_ERR_STATE, "EPH_XI_GIVEN without eph_put(EPH_FIELD_XI)");
+  const size_t N = (size_t)c->n;
+  double *sx = c->hstage.p, *sf = c->hstage.p + 3 * N, *so = c->hstage.p + 6 * N, *sa = c->hstage.p + 12 * N;
+  // positions first (the bins need them), then the engine's force, which
+  // the force sweep waits for: its copy overlaps the binning and the density
+  // sweep
+  if (x) {
+    CUDA_TRY(c, cudaMemcpyAsync(sx, x, 3 * sizeof(double) * N, cudaMemcpyHostToDevice, c->s_in));
+    CUDA_TRY(c, cudaEventRecord(c->xev[0], c->s_in));
+    CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->xev[0], 0));
+    k_pack3<<<nblocks(c->n), BLOCK, 0, c->stream>>>(c->n, sx, c->x.p);
+    c->launches += 1;
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(sf, f_in, 3 * sizeof(double) * N, cudaMemcpyHostToDevice, c->s_in));
+  CUDA_TRY(c, cudaEventRecord(c->f_ready, c->s_in));
+  c->f_pending = true;
+  r = launch_post_force(c, xi_source == EPH_XI_GIVEN ? 1 : 0);
+  if (c->f_pending) {  // no force sweep ran (no pair sweeps): f as the engine gave it
+    CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->f_ready, 0));
+    k_pack3<<<nblocks(c->n), BLOCK, 0, c->stream>>>(c->n, sf, c->f.p);
+    c->f_pending = false;
+  }
+  if (r) return r;
+  k_unpack3<<<nblocks(c->n), BLOCK, 0, c->stream>>>(c->n, c->f.p, so);
+  c->launches += 1;
+  CUDA_TRY(c, cudaEventRecord(c->xev[1], c->stream));
+  if (array) {
+    // the per-atom array (fix_eph.cpp:406-428) is final here; it leaves on
+    // its own stream while the next hooks run and is waited for by
+    // eph_end_of_step (or any call that synchronises the context)
+    k_peratom<<<nblocks(c->n), BLOCK, 0, c->stream>>>(c->n, c->groupbit, c->mask.p, c->rho.p, c->beta_i.p,
+                                                      c->f_eph.p, c->f_rng.p, sa);
+    c->launches += 1;
+    CUDA_TRY(c, cudaEventRecord(c->xev[2], c->stream));
+    CUDA_TRY(c, cudaStreamWaitEvent(c->s_arr, c->xev[2], 0));
+    CUDA_TRY(c, cudaMemcpyAsync(array, sa, 8 * sizeof(double) * N, cudaMemcpyDeviceToHost, c->s_arr));
+    CUDA_TRY(c, cudaEventRecord(c->arr_done, c->s_arr));
+    c->arr_pending = true;
+  }
+  CUDA_TRY(c, cudaStreamWaitEvent(c->s_out, c->xev[1], 0));
+  CUDA_TRY(c, cudaMemcpyAsync(f_out, so, 3 * sizeof(double) * N, cudaMemcpyDeviceToHost, c->s_out));
+  CUDA_TRY(c, cudaStreamSynchronize(c->s_out));
+  return check_device(c);
 }
 
 int eph_step(eph_ctx *c, int nsteps, int xi_source) {
@@ -1345,6 +1691,10 @@ int eph_set_graph(eph_ctx *c, int on) {
 int eph_synchronize(eph_ctx *c) {
   if (!c) return EPH_ERR_ARG;
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (c->arr_pending) {
+    CUDA_TRY(c, cudaEventSynchronize(c->arr_done));
+    c->arr_pending = false;
+  }
   return check_device(c);
 }
 

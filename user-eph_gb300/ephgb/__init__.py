@@ -82,6 +82,12 @@ SIGNATURES = {
     "eph_set_list_skin": (C.c_int, [C.c_void_p, C.c_double]),
     "eph_get_list_skin": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), _ip]),
     "eph_autotune": (C.c_int, [C.c_void_p, _ip]),
+    "eph_initial_integrate_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "eph_post_force_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "eph_final_integrate_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "eph_pin": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "eph_unpin": (C.c_int, [C.c_void_p]),
+    "eph_autotune_list_skin": (C.c_int, [C.c_void_p, _dp, C.c_int, C.c_int, _dp]),
     "eph_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.POINTER(C.c_char_p)),
                                    C.POINTER(eph_md), C.POINTER(C.c_void_p)]),
     "eph_batch_destroy": (None, [C.c_void_p]),
@@ -356,6 +362,32 @@ class FixEPH:
     def end_of_step(self):
         self._check(self.L.eph_end_of_step(self.h))
 
+    # the hooks with the engine's host arrays (contiguous float64 n x 3,
+    # ideally pinned), in place; equal to put / hook / get with overlapped
+    # copies
+    def _rows(self, a, k=3):
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous
+                and a.shape == (self.n, k)):
+            raise ValueError(f"expected a C-contiguous float64 array of shape ({self.n}, {k})")
+        return _ptr(a)
+
+    def initial_integrate_host(self, x, v):
+        self._check(self.L.eph_initial_integrate_host(self.h, self._rows(x), self._rows(v)))
+
+    def post_force_host(self, x, f, array=None, xi=None, f_in=None):
+        """x: positions to upload (None: the device's), f: the engine's force
+        in (or f_in when given), the total out; array (n x 8): the per-atom
+        array, written by the time end_of_step returns"""
+        if xi is not None:
+            self.put("xi", xi)
+        fi = self._rows(f if f_in is None else f_in)
+        self._check(self.L.eph_post_force_host(self.h, None if x is None else self._rows(x), fi, self._rows(f),
+                                               None if array is None else self._rows(array, 8),
+                                               XI_GIVEN if xi is not None else XI_DEVICE_RNG))
+
+    def final_integrate_host(self, f, v):
+        self._check(self.L.eph_final_integrate_host(self.h, self._rows(f), self._rows(v)))
+
     def step(self, nsteps=1, xi=None):
         """nsteps engine steps; xi (n x 3) feeds the deviates of a single step."""
         if xi is not None:
@@ -457,6 +489,16 @@ class FixEPH:
     def autotune(self):
         out = C.c_int()
         self._check(self.L.eph_autotune(self.h, C.byref(out)))
+        return out.value
+
+    def autotune_list_skin(self, skins=(0.0, 0.2, 0.3, 0.5, 0.8), steps=20):
+        """eph_autotune_list_skin: time `steps` steps from the current state
+        with each skin (each window starting with a list build), restore the
+        state and keep the fastest skin; returns it"""
+        sk = np.ascontiguousarray(skins, dtype=np.float64)
+        out = C.c_double()
+        self._check(self.L.eph_autotune_list_skin(self.h, sk.ctypes.data_as(_dp), sk.size, int(steps),
+                                                   C.byref(out)))
         return out.value
 
     def set_beta_knots(self, elem, rho_knots, beta_knots):
