@@ -4,9 +4,10 @@ numpy restatement that reads the setfl file and builds its tables on its own
 perfect lattice, and energy conservation of plain NVE.  Two potentials: a
 generated Sutton-Chen Ni setfl (6 A cut-off) and the reference decks' own
 Tests/MD_Run/Ni.eam (10001-point tables, 6.5 A cut-off; kept under
-tests/golden/ref_inputs).  Parity with LAMMPS's pair_style eam/alloy itself is
-unpinned (LAMMPS is not available); the tables follow the same cubic Hermite
-scheme with five-point slopes."""
+tests/golden/ref_inputs).  FAST mode sums the pair terms in double-float
+(the default) or in FP64; both are checked.  Parity with LAMMPS's
+pair_style eam/alloy itself is unpinned (LAMMPS is not available); the
+tables follow the same cubic Hermite scheme with five-point slopes."""
 import numpy as np
 import pytest
 
@@ -26,22 +27,28 @@ def setfl(request, tmp_path_factory):
     return W.write_eam_sutton_chen(d + "/SC_Ni.eam")
 
 
-def forces_at(setfl, beta_file, at, mode=ephgb.MODE_FAST):
+def forces_at(setfl, beta_file, at, mode=ephgb.MODE_FAST, pairs=ephgb.PAIRS_DF64):
     """EAM forces and energy at the atoms' positions: one step of a fix that
     applies nothing (flags 0) from zero velocities and forces (the box must
-    be at least three cut-offs, 6 A, wide: 6^3 fcc cells)"""
+    be at least three cut-offs, 6 A, wide: 6^3 fcc cells); FAST mode sums the
+    pairs in df64 by default, or in FP64"""
     a = W.Atoms(x=at.x.copy(), v=np.zeros_like(at.v), type=at.type, mask=at.mask, boxlo=at.boxlo, boxhi=at.boxhi,
                 mass=at.mass)
     fix = ephgb.FixEPH(W.fix_args(beta_file, flags=0, grid=(4, 4, 4)), a, dt=0.001, mode=mode,
                        eam=(setfl, ["Ni"]))
+    fix.set_pair_arithmetic(pairs)
     fix.step(1)
     np.testing.assert_array_equal(fix.get("x"), a.x)  # v = f = 0: the step did not move them
     return fix.get("f"), fix.pair_energy()
 
 
-def test_matches_the_numpy_restatement(built, setfl, beta_file):
+@pytest.mark.parametrize("mode,pairs", [(ephgb.MODE_FAST, ephgb.PAIRS_DF64), (ephgb.MODE_FAST, ephgb.PAIRS_FP64),
+                                        (ephgb.MODE_EXACT, ephgb.PAIRS_DF64)])
+def test_matches_the_numpy_restatement(built, setfl, beta_file, mode, pairs):
+    """df64 pair sums (FAST, the default) and FP64 ones (FAST with
+    EPH_PAIRS_FP64, EXACT) against the numpy restatement"""
     at = W.fcc_lattice(6, jitter=0.08, seed=61)
-    f, E = forces_at(setfl, beta_file, at)
+    f, E = forces_at(setfl, beta_file, at, mode, pairs)
     En, fn = energy_forces(read_setfl(setfl), at.x, at.type, {1: 0}, at.boxhi - at.boxlo)
     assert abs(E - En) <= 1e-12 * abs(En)
     assert np.abs(f - fn).max() <= 1e-11 * np.abs(fn).max()
@@ -63,9 +70,10 @@ def test_forces_are_minus_the_energy_gradient(built, setfl, beta_file):
         assert abs(f[i, k] + (Ep - Em) / (2 * h)) <= 1e-6 * np.abs(f).max(), (i, k)
 
 
-def test_perfect_lattice_is_at_rest(built, setfl, beta_file):
+@pytest.mark.parametrize("pairs", [ephgb.PAIRS_DF64, ephgb.PAIRS_FP64])
+def test_perfect_lattice_is_at_rest(built, setfl, beta_file, pairs):
     at = W.fcc_lattice(6, jitter=0.0, seed=63)
-    f, E = forces_at(setfl, beta_file, at)
+    f, E = forces_at(setfl, beta_file, at, pairs=pairs)
     assert np.abs(f).max() <= 1e-10
     assert -4.5 < E / at.n < -4.0  # Ni cohesion: Sutton-Chen with the 6 A cut-off, and the reference's Ni.eam
 

@@ -214,6 +214,64 @@ def test_async_host_copies(built, beta_file):
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("cells,pinned", [(5, False), (16, True), (40, True)])
+def test_host_array_hooks(built, beta_file, cells, pinned):
+    """eph_initial_integrate_host / eph_post_force_host / eph_final_integrate_host
+    (chunked copies overlapped on two copy streams, fused kernels, the per-atom
+    array sent out on a third stream) equal the put / hook / get sequence bit
+    for bit over several steps: 500 and 16,384 atoms (one chunk), 256,000
+    atoms (3 chunks), pageable and pinned host arrays, with and without the
+    positions uploaded in post_force and the per-atom array."""
+    import torch
+
+    at = W.fcc_lattice(cells, seed=81, temperature=300.0)
+    W.add_pka(at, 500.0, seed=82)
+    words = W.fix_args(beta_file, grid=(6, 6, 6))
+    n = at.n
+
+    def rows(a, k=3):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(n, k)
+        return torch.from_numpy(a.copy()).pin_memory().numpy() if pinned else a.copy()
+
+    ref = ephgb.FixEPH(words, at, dt=0.0005)
+    fix = ephgb.FixEPH(words, at, dt=0.0005)
+    xr, vr, fr = rows(at.x), rows(at.v), rows(np.zeros((n, 3)))
+    x, v, f, arr = rows(at.x), rows(at.v), rows(np.zeros((n, 3))), rows(np.zeros((n, 8)), 8)
+    for s in range(6):
+        fpair = np.full((n, 3), 1e-3 * (s + 1))  # an engine force
+        # the reference sequence
+        ref.set_timestep(s + 1)
+        ref.put("x", xr)
+        ref.put("v", vr)
+        ref.initial_integrate()
+        ref.get("x", out=xr)
+        ref.get("v", out=vr)
+        if s % 2 == 0:
+            ref.put("x", xr)
+        fr[:] = fpair
+        ref.put("f", fr)
+        ref.post_force()
+        ref.get("f", out=fr)
+        ref.put("f", fr)
+        ref.final_integrate()
+        ref.get("v", out=vr)
+        ref.end_of_step()
+        arr_ref = ref.get("array")
+        # the host-array hooks
+        fix.set_timestep(s + 1)
+        fix.initial_integrate_host(x, v)
+        f[:] = fpair
+        fix.post_force_host(x if s % 2 == 0 else None, f, arr if s % 3 != 1 else None)
+        fix.final_integrate_host(f, v)
+        fix.end_of_step()
+        for a, b, k in ((x, xr, "x"), (v, vr, "v"), (f, fr, "f")):
+            assert np.array_equal(a, b), (s, k)
+        if s % 3 != 1:
+            assert np.array_equal(arr, arr_ref), s
+        assert np.array_equal(fix.get("T"), ref.get("T")), s
+        assert fix.compute_vector(0) == ref.compute_vector(0)
+
+
 @pytest.mark.parametrize("two_el", [False, True])
 def test_df64_pair_sums_against_oracle_and_fp64(built, beta_file, beta_file_2el, two_el):
     """The FAST one-lane sweeps with df64 pair arithmetic (the default from

@@ -79,6 +79,16 @@ struct eph_ctx {
   bool have_fext = false, have_xi = false;
   DevBuf<int> type, mask, nshort, cell, tmap;
   DevBuf<double> rho, beta_i, Te_i, stage;
+  // the hooks with the engine's host arrays (eph_*_host): two copy streams
+  // (host->device, device->host) and one for the per-atom array, events of
+  // the chunks, staging rows (20 n doubles: 12 n for the hooks' rows, 8 n
+  // for the per-atom array, which may still be on its way out while the
+  // next hook runs)
+  cudaStream_t s_in = nullptr, s_out = nullptr, s_arr = nullptr;
+  std::vector<cudaEvent_t> xev;
+  DevBuf<double> hstage;
+  cudaEvent_t f_ready = nullptr, arr_done = nullptr;
+  bool f_pending = false, arr_pending = false;
   DevBuf<int> bin_count;
   DevBuf<BinEntry> bins;
   DevBuf<int4> atom_bin;

@@ -14,12 +14,17 @@
 #include <vector>
 
 #include "eph_ctx_impl.hpp"
+#include "eph_df64.cuh"
 
 using namespace ephgb;
 
 struct EamDevice {
   Eam host;
   DevBuf<D4> F, f, z2r;  // [element][nrho], [element][nr], [pair][nr]
+  // f and z2r as double-floats for the df64 pair sums (FAST mode with
+  // EPH_PAIRS_DF64): two float4 per interval, hi and lo parts
+  DevBuf<float4> fd, zd;
+  DevBuf<float2> fpd;  // F'(rho_i) / dr as a double-float, gathered per pair
   DevBuf<double> fp, energy, esum;
   DevBuf<unsigned> pj;    // pair list, [kcap][n]
   DevBuf<int> ns;         // pairs per atom
@@ -34,9 +39,11 @@ constexpr unsigned FULL = 0xffffffffu;
 
 struct EamParams {
   const D4 *F, *f, *z2r;
+  const float4 *fd, *zd;
   int nel, nrho, nr;
   double inv_drho, inv_dr, rho_max, rc2;
   float rc2_band;
+  float inv_dr_hi, inv_dr_lo, rc2_hi, rc2_lo;  // 1/dr and rc^2 as double-floats
   int map[65];
 };
 
@@ -66,38 +73,14 @@ __device__ __forceinline__ void image_vector(const StepParams &P, const D4 &xi, 
   ez = cz - xi.z;
 }
 
-// rho_i = sum_j f_b(r_ij) over the 27 bins around atom i (bin edge >= the
-// cutoff), the pairs within the cutoff written to the EAM pair list
-// (u32: neighbour index | periodic-image code << 27, row k of atom i at
-// k * n + i), then F_a(rho_i) and F'_a(rho_i) (beyond the table F continues
-// linearly with the slope at its end).  Two passes as in the fix's density
-// sweep: FP32/integer candidates (warp-uniform loop bounds) kept in shared
-// memory with the overflow in the list rows, then the FP64 pass over the
-// candidates in lockstep.
-__global__ void __launch_bounds__(128)
-    k_eam_density(StepParams P, EamParams E, const D4 *__restrict__ x, const int *__restrict__ type,
-                  const int *__restrict__ bin_count, const BinEntry *__restrict__ bins,
-                  const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
-                  unsigned *__restrict__ epj, int *__restrict__ ens, int kcap, double *__restrict__ fp,
-                  double *__restrict__ energy, unsigned *__restrict__ err) {
-  __shared__ unsigned s_cand[CAND_SMEM * 128];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int t = threadIdx.x, nt = blockDim.x;
-  const bool valid = i < P.n;
-  auto cget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : epj[(size_t)k * P.n + i]; };
-  auto cset = [&](int k, unsigned u) {
-    if (k < CAND_SMEM)
-      s_cand[k * nt + t] = u;
-    else
-      epj[(size_t)k * P.n + i] = u;
-  };
-  const D4 xi = valid ? x[i] : D4{0.0, 0.0, 0.0, 0.0};
-  int4 Bi = make_int4(0, 0, 0, 0);
-  float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (valid) {
-    Bi = atom_bin[i];
-    oi = atom_off[i];
-  }
+// Pass 1 of the EAM density sweeps: atom i's candidates in the 27 bins
+// around it (FP32/integer work, warp-uniform loop bounds), stored by cset as
+// neighbour index | periodic-image code << 27; returns their count
+template <class Set>
+__device__ __forceinline__ int eam_candidates(const StepParams &P, const EamParams &E, int i, bool valid, int4 Bi,
+                                              float4 oi, const int *__restrict__ bin_count,
+                                              const BinEntry *__restrict__ bins, int kcap, unsigned *__restrict__ err,
+                                              Set cset) {
   int nc = 0;
   for (int dz = -1; dz <= 1; ++dz) {
     const int Tz = Bi.z + dz, tz = Tz < 0 ? Tz + P.nb[2] : (Tz >= P.nb[2] ? Tz - P.nb[2] : Tz);
@@ -139,6 +122,42 @@ __global__ void __launch_bounds__(128)
       }
     }
   }
+  return nc;
+}
+
+// rho_i = sum_j f_b(r_ij) over the 27 bins around atom i (bin edge >= the
+// cutoff), the pairs within the cutoff written to the EAM pair list
+// (u32: neighbour index | periodic-image code << 27, row k of atom i at
+// k * n + i), then F_a(rho_i) and F'_a(rho_i) (beyond the table F continues
+// linearly with the slope at its end).  Two passes as in the fix's density
+// sweep: FP32/integer candidates (warp-uniform loop bounds) kept in shared
+// memory with the overflow in the list rows, then the FP64 pass over the
+// candidates in lockstep.
+__global__ void __launch_bounds__(128)
+    k_eam_density(StepParams P, EamParams E, const D4 *__restrict__ x, const int *__restrict__ type,
+                  const int *__restrict__ bin_count, const BinEntry *__restrict__ bins,
+                  const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
+                  unsigned *__restrict__ epj, int *__restrict__ ens, int kcap, double *__restrict__ fp,
+                  double *__restrict__ energy, unsigned *__restrict__ err) {
+  __shared__ unsigned s_cand[CAND_SMEM * 128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
+  const bool valid = i < P.n;
+  auto cget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : epj[(size_t)k * P.n + i]; };
+  auto cset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM)
+      s_cand[k * nt + t] = u;
+    else
+      epj[(size_t)k * P.n + i] = u;
+  };
+  const D4 xi = valid ? x[i] : D4{0.0, 0.0, 0.0, 0.0};
+  int4 Bi = make_int4(0, 0, 0, 0);
+  float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (valid) {
+    Bi = atom_bin[i];
+    oi = atom_off[i];
+  }
+  const int nc = eam_candidates(P, E, i, valid, Bi, oi, bin_count, bins, kcap, err, cset);
   __syncwarp();
   double rho = 0.0;
   int ns = 0;
@@ -217,6 +236,185 @@ __global__ void __launch_bounds__(128)
   energy[i] += ep;
 }
 
+// ---------------------------------------------- df64 pair sums (FAST mode)
+
+// sqrt(a), a > 0, as a double-float: the FP32 estimate s0 = a y (y the
+// rsqrt estimate) corrected twice by s + y (a - s^2) / 2 with the residual
+// formed exactly (Karp and Markstein's form of Newton's iteration); the
+// second correction takes the error from ~(2^-23)^2 to the double-float's
+// own ~2^-48
+__device__ __forceinline__ df64::df sqrt_df(df64::df a) {
+  using namespace df64;
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(a.hi));
+  const float s0 = a.hi * y;
+  float p, pe;
+  two_prod(s0, s0, p, pe);
+  const float res = ((a.hi - p) - pe) + a.lo;
+  df s;
+  fast_two_sum(s0, 0.5f * y * res, s.hi, s.lo);
+  const df r2 = sub(a, mul(s, s));
+  return add(s, df{0.5f * y * r2.hi, 0.0f});
+}
+
+// herm() on a double-float table at q >= 0 (knot units): the interval from
+// the FP32 part of q settled by the sign of the double-float remainder, the
+// same clamps (at most the last interval, p at most 1), the value and the
+// derivative per knot unit
+__device__ __forceinline__ void herm_df(const float4 *__restrict__ t, int n, df64::df q, df64::df &v,
+                                        df64::df &dv) {
+  using namespace df64;
+  const df one{1.0f, 0.0f};
+  const float kr = floor_estimate(q.hi);
+  int m = floor_estimate_int(kr);
+  float th, te;
+  two_sum(q.hi, -kr, th, te);
+  df p = make(th, te + q.lo);
+  if (lt(p, df{0.0f, 0.0f})) {
+    m -= 1;
+    p = add(p, one);
+  } else if (!lt(p, one)) {
+    m += 1;
+    p = sub(p, one);
+  }
+  if (m > n - 2) {
+    p = add(p, df{(float)(m - (n - 2)), 0.0f});
+    m = n - 2;
+    if (!lt(p, one)) p = one;
+  }
+  if (m < 0) m = 0;
+  const float4 hi = t[2 * (size_t)m], lo = t[2 * (size_t)m + 1];
+  const df c0{hi.x, lo.x}, c1{hi.y, lo.y}, c2{hi.z, lo.z}, c3{hi.w, lo.w};
+  v = horner(c0, c1, c2, c3, p);
+  dv = fma(p, fma(p, mul(df{3.0f, 0.0f}, c3), mul(df{2.0f, 0.0f}, c2)), c1);
+}
+
+// k_eam_density with the pair arithmetic in double-float: e from the FP64
+// positions (the periodic image added as k_eam_density adds it), then r^2,
+// the cut-off test, r and f_b(r) in df64, rho_i in blocked sums; F and F'
+// per atom in FP64; F' / dr also as a double-float for k_eam_force_df
+__global__ void __launch_bounds__(128)
+    k_eam_density_df(StepParams P, EamParams E, const D4 *__restrict__ x, const int *__restrict__ type,
+                     const int *__restrict__ bin_count, const BinEntry *__restrict__ bins,
+                     const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
+                     unsigned *__restrict__ epj, int *__restrict__ ens, int kcap, double *__restrict__ fp,
+                     float2 *__restrict__ fpd, double *__restrict__ energy, unsigned *__restrict__ err) {
+  using namespace df64;
+  __shared__ unsigned s_cand[CAND_SMEM * 128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
+  const bool valid = i < P.n;
+  auto cget = [&](int k) -> unsigned { return k < CAND_SMEM ? s_cand[k * nt + t] : epj[(size_t)k * P.n + i]; };
+  auto cset = [&](int k, unsigned u) {
+    if (k < CAND_SMEM)
+      s_cand[k * nt + t] = u;
+    else
+      epj[(size_t)k * P.n + i] = u;
+  };
+  const D4 xi = valid ? x[i] : D4{0.0, 0.0, 0.0, 0.0};
+  int4 Bi = make_int4(0, 0, 0, 0);
+  float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (valid) {
+    Bi = atom_bin[i];
+    oi = atom_off[i];
+  }
+  const int nc = eam_candidates(P, E, i, valid, Bi, oi, bin_count, bins, kcap, err, cset);
+  __syncwarp();
+  const df rc2{E.rc2_hi, E.rc2_lo}, inv_dr{E.inv_dr_hi, E.inv_dr_lo};
+  bsum rs = bsum_zero();
+  int ns = 0;
+  const int nmax = __reduce_max_sync(FULL, nc);
+  for (int k = 0; k < nmax; ++k) {
+    if (k >= nc) continue;
+    const unsigned u = cget(k);
+    const unsigned j = u & IDX_MASK;
+    double ex, ey, ez;
+    image_vector(P, xi, x[j], u >> IDX_BITS, ex, ey, ez);
+    const df dx = from_double(ex), dy = from_double(ey), dz = from_double(ez);
+    const df r2 = dot3(dx, dy, dz, dx, dy, dz);
+    if (lt(r2, rc2)) {
+      epj[(size_t)ns * P.n + i] = u;  // ns <= k: the candidate there is consumed
+      ++ns;
+      df v, dv;
+      herm_df(E.fd + 2 * (size_t)E.map[type[j]] * E.nr, E.nr, mul(sqrt_df(r2), inv_dr), v, dv);
+      acc_add(rs.blk, v);
+      if ((ns & 7) == 0) bsum_fold(rs);
+    }
+  }
+  if (!valid) return;
+  const double rho = to_double(bsum_value(rs));
+  ens[i] = ns;
+  const int a = E.map[type[i]];
+  double F, dF;
+  herm(E.F + (size_t)a * E.nrho, E.nrho, rho * E.inv_drho, F, dF);
+  dF *= E.inv_drho;
+  if (rho > E.rho_max) F += dF * (rho - E.rho_max);
+  fp[i] = dF;
+  const df g = from_double(dF * E.inv_dr);
+  fpd[i] = make_float2(g.hi, g.lo);
+  energy[i] = F;
+}
+
+// k_eam_force with the pair arithmetic in double-float: per pair r, 1/r,
+// the Hermite tables f_b, f_a and z2r = r phi, dE/dr and (dE/dr / r) e in
+// df64, the force and 1/2 sum phi in blocked sums
+__global__ void __launch_bounds__(128)
+    k_eam_force_df(StepParams P, EamParams E, const D4 *__restrict__ x, const int *__restrict__ type,
+                   const unsigned *__restrict__ epj, const int *__restrict__ ens, const float2 *__restrict__ fpd,
+                   const D4 *__restrict__ fext, D4 *__restrict__ f, double *__restrict__ energy) {
+  using namespace df64;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const D4 xi = x[i];
+  const int a = E.map[type[i]];
+  const float2 gi = fpd[i];
+  const df fpi{gi.x, gi.y}, inv_dr{E.inv_dr_hi, E.inv_dr_lo};
+  bsum sx = bsum_zero(), sy = bsum_zero(), sz = bsum_zero(), se = bsum_zero();
+  const int ns = ens[i];
+  for (int k = 0; k < ns; ++k) {
+    const unsigned u = epj[(size_t)k * P.n + i];
+    const unsigned j = u & IDX_MASK;
+    double ex, ey, ez;
+    image_vector(P, xi, x[j], u >> IDX_BITS, ex, ey, ez);
+    const df dx = from_double(ex), dy = from_double(ey), dz = from_double(ez);
+    const df r2 = dot3(dx, dy, dz, dx, dy, dz);
+    const df r = sqrt_df(r2);
+    const df rinv = recip(r, rcp_estimate(r.hi));
+    const df q = mul(r, inv_dr);
+    const int b = E.map[type[j]];
+    df fb, dfb, fa, dfa, z, dzz;
+    herm_df(E.fd + 2 * (size_t)b * E.nr, E.nr, q, fb, dfb);
+    dfa = dfb;
+    if (a != b) herm_df(E.fd + 2 * (size_t)a * E.nr, E.nr, q, fa, dfa);
+    const int hi = a > b ? a : b, lo = a > b ? b : a;
+    herm_df(E.zd + 2 * (size_t)(hi * (hi + 1) / 2 + lo) * E.nr, E.nr, q, z, dzz);
+    const df phi = mul(z, rinv);
+    const df dphi = mul(sub(mul(dzz, inv_dr), phi), rinv);
+    const float2 gj = fpd[j];
+    const df dEdr = add(add(mul(fpi, dfb), mul(df{gj.x, gj.y}, dfa)), dphi);
+    const df s = mul(dEdr, rinv);
+    acc_fma(sx.blk, s, dx);
+    acc_fma(sy.blk, s, dy);
+    acc_fma(sz.blk, s, dz);
+    acc_add(se.blk, df{0.5f * phi.hi, 0.5f * phi.lo});
+    if ((k & 7) == 7) {
+      bsum_fold(sx);
+      bsum_fold(sy);
+      bsum_fold(sz);
+      bsum_fold(se);
+    }
+  }
+  D4 out{to_double(bsum_value(sx)), to_double(bsum_value(sy)), to_double(bsum_value(sz)), 0.0};
+  if (fext) {
+    const D4 g = fext[i];
+    out.x += g.x;
+    out.y += g.y;
+    out.z += g.z;
+  }
+  f[i] = out;
+  energy[i] += to_double(bsum_value(se));
+}
+
 // sum of the per-atom energies, one block, fixed order
 __global__ void k_eam_energy_sum(const double *__restrict__ e, int n, double *__restrict__ out) {
   __shared__ double s[256];
@@ -245,11 +443,23 @@ EamParams eam_params(const eph_ctx *c) {
   E.rho_max = d->host.drho * (double)(d->host.nrho - 1);
   E.rc2 = d->host.rc * d->host.rc;
   E.rc2_band = (float)d->rc2_band;
+  E.fd = d->fd.p;
+  E.zd = d->zd.p;
+  const df64::df idr = df64::from_double(E.inv_dr), rc2 = df64::from_double(E.rc2);
+  E.inv_dr_hi = idr.hi;
+  E.inv_dr_lo = idr.lo;
+  E.rc2_hi = rc2.hi;
+  E.rc2_lo = rc2.lo;
   std::memcpy(E.map, d->map, sizeof(E.map));
   return E;
 }
 
-int upload_table(eph_ctx *c, DevBuf<D4> &dst, const std::vector<std::vector<double>> &tabs) {
+// The Hermite tables in FP64 (D4 {c0, c1, c2, c3} per interval) and, with
+// df not NULL, as double-floats (float4 hi parts, float4 lo parts per
+// interval; each coefficient the nearest float plus the nearest float to
+// the rest)
+int upload_table(eph_ctx *c, DevBuf<D4> &dst, const std::vector<std::vector<double>> &tabs,
+                 DevBuf<float4> *dfo = nullptr) {
   std::vector<double> all;
   for (const auto &t : tabs) {
     std::vector<double> coef;
@@ -258,6 +468,17 @@ int upload_table(eph_ctx *c, DevBuf<D4> &dst, const std::vector<std::vector<doub
   }
   CUDA_TRY(c, dst.alloc(all.size() / 4));
   CUDA_TRY(c, cudaMemcpy(dst.p, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
+  if (dfo) {
+    std::vector<float> split(2 * all.size());
+    for (size_t m = 0; m < all.size() / 4; ++m)
+      for (int k = 0; k < 4; ++k) {
+        const df64::df v = df64::from_double(all[4 * m + k]);
+        split[8 * m + k] = v.hi;
+        split[8 * m + 4 + k] = v.lo;
+      }
+    CUDA_TRY(c, dfo->alloc(all.size() / 2));
+    CUDA_TRY(c, cudaMemcpy(dfo->p, split.data(), split.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   return EPH_OK;
 }
 
@@ -278,6 +499,7 @@ int eam_resize(eph_ctx *c) {
   CUDA_TRY(c, d->fp.alloc(N));
   CUDA_TRY(c, d->energy.alloc(N));
   CUDA_TRY(c, d->ns.alloc(N));
+  CUDA_TRY(c, d->fpd.alloc(N));
   CUDA_TRY(c, cudaMemset(d->energy.p, 0, sizeof(double) * N));
   // pair rows from the number density: twice the cut-off sphere, plus slack
   const double dens = (double)c->n / (c->prd[0] * c->prd[1] * c->prd[2]);
@@ -294,11 +516,20 @@ int launch_eam(eph_ctx *c) {
   if (d->fp.n < (size_t)c->n) return fail(c, EPH_ERR_STATE, "pair force buffers not sized for the atoms");
   PhaseScope ps(c, EPH_PHASE_PAIR);
   ps.launched(2);
-  k_eam_density<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, c->bin_count.p, c->bins.p, c->atom_bin.p,
-                                              c->atom_off.p, d->pj.p, d->ns.p, d->kcap, d->fp.p, d->energy.p,
-                                              c->d_err.p);
-  k_eam_force<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, d->pj.p, d->ns.p, d->fp.p,
-                                            c->have_fext ? c->fext.p : nullptr, c->f.p, d->energy.p);
+  const D4 *fext = c->have_fext ? c->fext.p : nullptr;
+  if (c->mode == EPH_MODE_FAST && c->pair_arith == EPH_PAIRS_DF64) {
+    k_eam_density_df<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, c->bin_count.p, c->bins.p,
+                                                   c->atom_bin.p, c->atom_off.p, d->pj.p, d->ns.p, d->kcap, d->fp.p,
+                                                   d->fpd.p, d->energy.p, c->d_err.p);
+    k_eam_force_df<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, d->pj.p, d->ns.p, d->fpd.p, fext,
+                                                 c->f.p, d->energy.p);
+  } else {
+    k_eam_density<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, c->bin_count.p, c->bins.p,
+                                                c->atom_bin.p, c->atom_off.p, d->pj.p, d->ns.p, d->kcap, d->fp.p,
+                                                d->energy.p, c->d_err.p);
+    k_eam_force<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, d->pj.p, d->ns.p, d->fp.p, fext, c->f.p,
+                                              d->energy.p);
+  }
   CUDA_TRY(c, cudaGetLastError());
   return EPH_OK;
 }
@@ -334,8 +565,8 @@ int eph_set_pair_eam(eph_ctx *c, const char *path, int ntypes, const char *const
   c->eam = d;
   int r;
   CUDA_TRY(c, cudaSetDevice(c->device));
-  if ((r = upload_table(c, d->F, d->host.F)) || (r = upload_table(c, d->f, d->host.f)) ||
-      (r = upload_table(c, d->z2r, d->host.z2r)))
+  if ((r = upload_table(c, d->F, d->host.F)) || (r = upload_table(c, d->f, d->host.f, &d->fd)) ||
+      (r = upload_table(c, d->z2r, d->host.z2r, &d->zd)))
     return r;
   CUDA_TRY(c, d->esum.alloc(1));
   d->rc2_band = d->host.rc * d->host.rc * (1.0 + 1e-4);

@@ -22,6 +22,41 @@ namespace ephgb {
 
 // ------------------------------------------------------------- integrator
 
+// The half kick and drift of FixEPH::initial_integrate (fix_eph.cpp:305-328)
+// for one atom of the group
+template <bool FAST>
+__device__ __forceinline__ void kick_drift(const StepParams &P, double dtfm, const D4 &fi, D4 &xi, D4 &vi) {
+  if (FAST) {
+    vi.x = fma(dtfm, fi.x, vi.x);
+    vi.y = fma(dtfm, fi.y, vi.y);
+    vi.z = fma(dtfm, fi.z, vi.z);
+    xi.x = fma(P.dtv, vi.x, xi.x);
+    xi.y = fma(P.dtv, vi.y, xi.y);
+    xi.z = fma(P.dtv, vi.z, xi.z);
+  } else {
+    vi.x += dtfm * fi.x;
+    vi.y += dtfm * fi.y;
+    vi.z += dtfm * fi.z;
+    xi.x += P.dtv * vi.x;
+    xi.y += P.dtv * vi.y;
+    xi.z += P.dtv * vi.z;
+  }
+}
+
+// The half kick of FixEPH::final_integrate (fix_eph.cpp:330-348)
+template <bool FAST>
+__device__ __forceinline__ void kick(double dtfm, const D4 &fi, D4 &vi) {
+  if (FAST) {
+    vi.x = fma(dtfm, fi.x, vi.x);
+    vi.y = fma(dtfm, fi.y, vi.y);
+    vi.z = fma(dtfm, fi.z, vi.z);
+  } else {
+    vi.x += dtfm * fi.x;
+    vi.y += dtfm * fi.y;
+    vi.z += dtfm * fi.z;
+  }
+}
+
 // FixEPH::initial_integrate (fix_eph.cpp:305-328) and the engine's rebuild
 // test (an atom moved more than skin/2 since the last wrap).
 template <bool FAST>
@@ -35,23 +70,7 @@ __global__ void k_initial_integrate(StepParams P, D4 *__restrict__ x, D4 *__rest
     D4 xi = x[i];
     if (!(P.flags & 0x08) && (mask[i] & P.groupbit)) {
       D4 vi = v[i];
-      const D4 fi = f[i];
-      const double dtfm = P.dtfm[type[i]];
-      if (FAST) {
-        vi.x = fma(dtfm, fi.x, vi.x);
-        vi.y = fma(dtfm, fi.y, vi.y);
-        vi.z = fma(dtfm, fi.z, vi.z);
-        xi.x = fma(P.dtv, vi.x, xi.x);
-        xi.y = fma(P.dtv, vi.y, xi.y);
-        xi.z = fma(P.dtv, vi.z, xi.z);
-      } else {
-        vi.x += dtfm * fi.x;
-        vi.y += dtfm * fi.y;
-        vi.z += dtfm * fi.z;
-        xi.x += P.dtv * vi.x;
-        xi.y += P.dtv * vi.y;
-        xi.z += P.dtv * vi.z;
-      }
+      kick_drift<FAST>(P, P.dtfm[type[i]], f[i], xi, vi);
       v[i] = vi;
       x[i] = xi;
     }
@@ -71,18 +90,64 @@ __global__ void k_final_integrate(StepParams P, D4 *__restrict__ v, const D4 *__
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n || (P.flags & 0x08) || !(mask[i] & P.groupbit)) return;
   D4 vi = v[i];
-  const D4 fi = f[i];
-  const double dtfm = P.dtfm[type[i]];
-  if (FAST) {
-    vi.x = fma(dtfm, fi.x, vi.x);
-    vi.y = fma(dtfm, fi.y, vi.y);
-    vi.z = fma(dtfm, fi.z, vi.z);
-  } else {
-    vi.x += dtfm * fi.x;
-    vi.y += dtfm * fi.y;
-    vi.z += dtfm * fi.z;
-  }
+  kick<FAST>(P.dtfm[type[i]], f[i], vi);
   v[i] = vi;
+}
+
+// The hooks with the engine's host arrays (eph_initial_integrate_host,
+// eph_final_integrate_host), one chunk of `count` atoms per launch (the
+// pointers start at the chunk): the staged host rows (n x 3 doubles) go into
+// the D4 records (x.w, the element, kept), the hook's arithmetic runs, and
+// the rows the engine reads back are written to staging for the
+// device->host copies -- the work of k_pack3, the hook's kernel and
+// k_unpack3 in one pass.
+template <bool FAST>
+__global__ void k_initial_host(StepParams P, int count, const double *__restrict__ sx, const double *__restrict__ sv,
+                               D4 *__restrict__ x, D4 *__restrict__ v, const D4 *__restrict__ f,
+                               const int *__restrict__ type, const int *__restrict__ mask, double *__restrict__ ox,
+                               double *__restrict__ ov) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const size_t r = 3 * (size_t)i;
+  D4 xi = x[i];
+  xi.x = sx[r];
+  xi.y = sx[r + 1];
+  xi.z = sx[r + 2];
+  D4 vi = v[i];
+  vi.x = sv[r];
+  vi.y = sv[r + 1];
+  vi.z = sv[r + 2];
+  if (!(P.flags & 0x08) && (mask[i] & P.groupbit)) kick_drift<FAST>(P, P.dtfm[type[i]], f[i], xi, vi);
+  x[i] = xi;
+  v[i] = vi;
+  ox[r] = xi.x;
+  ox[r + 1] = xi.y;
+  ox[r + 2] = xi.z;
+  ov[r] = vi.x;
+  ov[r + 1] = vi.y;
+  ov[r + 2] = vi.z;
+}
+
+template <bool FAST>
+__global__ void k_final_host(StepParams P, int count, const double *__restrict__ sf, D4 *__restrict__ f,
+                             D4 *__restrict__ v, const int *__restrict__ type, const int *__restrict__ mask,
+                             double *__restrict__ ov) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const size_t r = 3 * (size_t)i;
+  D4 fi = f[i];
+  fi.x = sf[r];
+  fi.y = sf[r + 1];
+  fi.z = sf[r + 2];
+  f[i] = fi;
+  D4 vi = v[i];
+  if (!(P.flags & 0x08) && (mask[i] & P.groupbit)) {
+    kick<FAST>(P.dtfm[type[i]], fi, vi);
+    v[i] = vi;
+  }
+  ov[r] = vi.x;
+  ov[r + 1] = vi.y;
+  ov[r + 2] = vi.z;
 }
 
 // ------------------------------------------------------------------ binning

@@ -68,6 +68,8 @@ FixEPHGB::FixEPHGB(LAMMPS *lmp, int narg, char **arg) : Fix(lmp, narg, arg) {
 
 FixEPHGB::~FixEPHGB() {
   if (ctx) eph_destroy(ctx);
+  for (void *p : pinned)
+    if (p) eph_unpin(p);
   for (char *w : words) free(w);
   delete random;
   atom->delete_callback(id, 0);
@@ -169,26 +171,20 @@ void FixEPHGB::setup(int) { upload_atoms(); }
 void FixEPHGB::initial_integrate(int) {
   if (eph_flag & 0x08) return;
   if (nlocal_dev != atom->nlocal || reordered) upload_atoms();
-  // queued copies; the engine's arrays are read again only after the
-  // synchronising get at the end of the hook
-  check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "put x");
-  check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST_ASYNC), "put v");
-  check(eph_initial_integrate(ctx), "initial_integrate");
-  check(eph_get(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "get x");
-  check(eph_get(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "get v");
+  pin_engine_arrays();
+  // x, v in (the device keeps the f final_integrate sent), the half kick
+  // and drift, x, v out: the copies of chunks of atoms overlap both ways
+  check(eph_initial_integrate_host(ctx, &atom->x[0][0], &atom->v[0][0]), "initial_integrate");
 }
 
 void FixEPHGB::post_force(int) {
   // the engine re-neighboured this step: atoms may be re-sorted or wrapped,
   // so all of them go up again (x, v, type, mask and f); otherwise the device
-  // holds this step's x and v since initial_integrate and only the force the
-  // engine computed since then goes up
-  if (nlocal_dev != atom->nlocal || reordered) {
-    upload_atoms();
-  } else {
-    if (neighbor->ago == 0) check(eph_put(ctx, EPH_FIELD_X, &atom->x[0][0], EPH_HOST_ASYNC), "put x");
-    check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
-  }
+  // holds this step's x and v since initial_integrate, and x goes up again
+  // only on re-neighbouring steps (the engine wrapped it)
+  const bool full = nlocal_dev != atom->nlocal || reordered;
+  if (full) upload_atoms();
+  pin_engine_arrays();
   int source = EPH_XI_DEVICE_RNG;
   if (xi_on_host && (eph_flag & 0x02)) {
     // the engine's own Gaussian stream, three per in-group atom in atom
@@ -201,23 +197,49 @@ void FixEPHGB::post_force(int) {
     check(eph_put(ctx, EPH_FIELD_XI, xi.data(), EPH_HOST), "put xi");
     source = EPH_XI_GIVEN;
   }
-  check(eph_post_force(ctx, source), "post_force");
-  check(eph_get(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST), "get f");
+  // the engine's force in, f_EPH + f_RNG added, f out; the per-atom array
+  // (final here, fix_eph.cpp:406-428) leaves on its own stream on the steps
+  // the engine reads it and is in place when end_of_step returns
+  const double *x = (!full && neighbor->ago == 0) ? &atom->x[0][0] : nullptr;
+  double *arr = (update->ntimestep % peratom_freq == 0) ? &array[0][0] : nullptr;
+  check(eph_post_force_host(ctx, x, &atom->f[0][0], &atom->f[0][0], arr, source), "post_force");
 }
 
 void FixEPHGB::final_integrate() {
   if (eph_flag & 0x08) return;
-  check(eph_put(ctx, EPH_FIELD_F, &atom->f[0][0], EPH_HOST_ASYNC), "put f");
-  check(eph_final_integrate(ctx), "final_integrate");
-  check(eph_get(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "get v");
+  pin_engine_arrays();
+  check(eph_final_integrate_host(ctx, &atom->f[0][0], &atom->v[0][0]), "final_integrate");
 }
 
 void FixEPHGB::end_of_step() {
   check(eph_set_timestep(ctx, (long)update->ntimestep), "set timestep");
   if (eph_flag & 0x08) check(eph_put(ctx, EPH_FIELD_V, &atom->v[0][0], EPH_HOST), "put v");
   check(eph_end_of_step(ctx), "end_of_step");
-  if (update->ntimestep % peratom_freq == 0)
-    check(eph_get(ctx, EPH_FIELD_PERATOM, &array[0][0], EPH_HOST), "get per-atom array");
+}
+
+// The engine's x, v, f and the per-atom array page-locked for the hooks'
+// copies; pinned again when the engine reallocates them (a range the engine
+// has already freed is unpinned as well as the runtime allows).  Pinning
+// that fails leaves the copies on pageable memory: slower, not wrong.
+void FixEPHGB::pin_engine_arrays() {
+  const size_t nmax = atom->nmax > 0 ? (size_t)atom->nmax : 0;
+  struct Want {
+    void *p;
+    size_t bytes;
+  } want[4] = {{atom->x ? &atom->x[0][0] : nullptr, 3 * sizeof(double) * nmax},
+               {atom->v ? &atom->v[0][0] : nullptr, 3 * sizeof(double) * nmax},
+               {atom->f ? &atom->f[0][0] : nullptr, 3 * sizeof(double) * nmax},
+               {array ? &array[0][0] : nullptr, 8 * sizeof(double) * nmax}};
+  for (int k = 0; k < 4; ++k) {
+    if (want[k].p == pinned[k] && want[k].bytes == pinned_bytes[k]) continue;
+    if (pinned[k]) eph_unpin(pinned[k]);
+    pinned[k] = nullptr;
+    pinned_bytes[k] = 0;
+    if (want[k].p && want[k].bytes && eph_pin(want[k].p, want[k].bytes) == EPH_OK) {
+      pinned[k] = want[k].p;
+      pinned_bytes[k] = want[k].bytes;
+    }
+  }
 }
 
 void FixEPHGB::reset_dt() {
@@ -232,6 +254,11 @@ void FixEPHGB::copy_arrays(int i, int j, int) {
 }
 
 void FixEPHGB::grow_arrays(int ngrow) {
+  if (pinned[3]) {  // unpinned before the reallocation frees it
+    eph_unpin(pinned[3]);
+    pinned[3] = nullptr;
+    pinned_bytes[3] = 0;
+  }
   memory->grow(array, ngrow, 8, "eph/gb:array");
   array_atom = array;
 }

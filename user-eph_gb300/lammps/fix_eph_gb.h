@@ -77,7 +77,11 @@ class FixEPHGB : public Fix {
   std::vector<double> xi;  // deviates drawn on the host (xi host)
   double **array = nullptr;
 
+  void *pinned[4] = {nullptr, nullptr, nullptr, nullptr};  // x, v, f, the per-atom array
+  size_t pinned_bytes[4] = {0, 0, 0, 0};
+
   void create_context();
+  void pin_engine_arrays();
   void check(int status, const char *where);
   void upload_atoms();  // x, v, type, mask when the engine re-neighboured
 };
