@@ -14,6 +14,7 @@ import pytest
 import ephgb
 from ephgb import workloads as W
 from golden_io import write_ref_input
+from helpers import key_err
 from oracle.eam_ref import energy_forces, read_setfl
 
 pytestmark = pytest.mark.gpu
@@ -123,3 +124,21 @@ def test_setup_errors(built, setfl, beta_file, tmp_path):
     with pytest.raises(ephgb.EphError) as e:
         fix.set_pair_eam(setfl, ["Ni"])
     assert e.value.status == 7  # EPH_ERR_STATE: after the atoms
+
+
+def test_fix_density_from_the_eam_pair_list(built, setfl, beta_file):
+    """With the EAM force and one lane per atom, the fix's df64 density sweep
+    takes its candidates from the step's EAM pair list instead of scanning
+    the EAM-sized bins: five steps of the fix (friction, random force, grid)
+    on top of the pair force agree per atom, to the FAST bar, with the FP64
+    path (bin search, FP64 pair terms everywhere)."""
+    at = W.fcc_lattice(6, seed=91, temperature=300.0)
+    out = []
+    for pairs in (ephgb.PAIRS_DF64, ephgb.PAIRS_FP64):
+        fix = ephgb.FixEPH(W.fix_args(beta_file, flags=7, grid=(4, 4, 4)), at, dt=0.0005, eam=(setfl, ["Ni"]))
+        fix.set_threads_per_atom(1)
+        fix.set_pair_arithmetic(pairs)
+        fix.step(5)
+        out.append({k: fix.get(k) for k in ("x", "v", "f", "rho", "w", "f_eph", "f_rng")})
+    for k in out[0]:
+        assert key_err(k, out[0][k], out[1][k]) <= 1e-12, (k, key_err(k, out[0][k], out[1][k]))

@@ -297,11 +297,17 @@ void launch_density_f(eph_ctx *c, int xi_mode) {
   if constexpr (FAST && FUSE) {
     if (df_active(c)) {
       float4 *pa = reinterpret_cast<float4 *>(c->pe.p), *pb = pa + (size_t)c->kcap * c->n;
+      // with the standalone engine's EAM force the candidates come from its
+      // pair list of this step (the same bins and order; no bin scan)
+      const unsigned *elist = nullptr;
+      const int *ens = nullptr;
+      if (!(c->eam_list_fresh && eam_pair_list(c, &elist, &ens))) elist = nullptr, ens = nullptr;
       k_density_df<MULTI><<<nblocks(c->n), BLOCK, 0, c->stream>>>(
           c->P, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->dfrec.p, c->dfvrec.p, c->x.p,
           c->xi.p, xi_mode, c->T0.p, c->pj.p, pa, pb, reinterpret_cast<float4 *>(c->pg.p), c->nshort.p, c->A.p,
           c->Bw.p, c->rho.p, c->beta_i.p, c->cell.p, c->Te_i.p, c->wrapflag.p, c->d_err.p, c->counters.p, c->v.p,
-          c->Mm.p, c->G.p);
+          c->Mm.p, c->G.p, elist, ens);
+      c->eam_list_fresh = false;
       return;
     }
   }
@@ -575,6 +581,7 @@ int launch_pair_sweeps(eph_ctx *c, int xi_mode) {
       if (c->multi) launch_density_t<false, true>(c, xi_mode);
       else launch_density_t<false, false>(c, xi_mode);
     }
+    c->eam_list_fresh = false;  // read (or not) by this step's density sweep only
   }
   // eph_post_force_host: the engine's force, uploaded while the density
   // sweep ran, goes into f before the force sweeps add to it

@@ -131,6 +131,7 @@ struct eph_ctx {
   double inner_dt = 0;
   // eam/alloy pair force of the standalone engine (eph_set_pair_eam), or none
   EamDevice *eam = nullptr;
+  bool eam_list_fresh = false;  // the EAM pair list is this step's (launch_eam ran since the last density sweep)
   // set by the adjoint while it records a step: substep k of the grid solve
   // writes its output to fdm_rec + k * ncells instead of the ping-pong buffer
   double *fdm_rec = nullptr;
@@ -189,7 +190,14 @@ int configure_list(eph_ctx *c);
 void drop_list(eph_ctx *c);
 int launch_pair_sweeps(eph_ctx *c, int xi_mode);
 // the engine's pair force for this step into f (plus the external force)
+// bins of edge >= r (1 + 5e-5), at least three per axis (all of P's bin geometry)
+int set_bin_geometry(eph_ctx *c, double r);
+// the df64 pair sums run (and k_bin writes the atoms' df64 records)
+bool df_active(const eph_ctx *c);
 int launch_eam(eph_ctx *c);
+// the EAM pair list of the step (rows k * n + i, counts) if it holds every
+// candidate of the fix's density sweep
+bool eam_pair_list(const eph_ctx *c, const unsigned **pj, const int **ns);
 int eam_resize(eph_ctx *c);  // per-atom buffers of the pair force for c->n atoms
 void eam_free(eph_ctx *c);
 

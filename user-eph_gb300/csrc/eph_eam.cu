@@ -15,6 +15,7 @@
 
 #include "eph_ctx_impl.hpp"
 #include "eph_df64.cuh"
+#include "eph_df_pair.cuh"
 
 using namespace ephgb;
 
@@ -289,6 +290,31 @@ __device__ __forceinline__ void herm_df(const float4 *__restrict__ t, int n, df6
   dv = fma(p, fma(p, mul(df{3.0f, 0.0f}, c3), mul(df{2.0f, 0.0f}, c2)), c1);
 }
 
+// A pair's displacement as double-floats: from the atoms' df64 records of
+// this step's bins when there are any (the bin difference with the periodic
+// image plus the offsets in the bins, no FP64 work), else from the FP64
+// positions as k_eam_density forms it
+__device__ __forceinline__ void pair_e_df(const StepParams &P, const float4 *__restrict__ rec, int4 Bi, float4 oi,
+                                          float4 ol, const D4 &xi, const D4 *__restrict__ x, unsigned j,
+                                          unsigned code, df64::df &ex, df64::df &ey, df64::df &ez) {
+  if (rec) {
+    const float4 R0 = rec[2 * (size_t)j], R1 = rec[2 * (size_t)j + 1];
+    const unsigned pk = __float_as_uint(R0.w);
+    const int dx = (int)(pk & 1023u) - 1 + ((int)(code % 3u) - 1) * P.nb[0] - Bi.x;
+    const int dy = (int)((pk >> 10) & 1023u) - 1 + ((int)((code / 3u) % 3u) - 1) * P.nb[1] - Bi.y;
+    const int dz = (int)((pk >> 20) & 1023u) - 1 + ((int)(code / 9u) - 1) * P.nb[2] - Bi.z;
+    ex = pair_disp(dx, R0.x, R1.x, oi.x, ol.x, P.w_hi[0], P.w_lo[0]);
+    ey = pair_disp(dy, R0.y, R1.y, oi.y, ol.y, P.w_hi[1], P.w_lo[1]);
+    ez = pair_disp(dz, R0.z, R1.z, oi.z, ol.z, P.w_hi[2], P.w_lo[2]);
+  } else {
+    double a, b, c;
+    image_vector(P, xi, x[j], code, a, b, c);
+    ex = df64::from_double(a);
+    ey = df64::from_double(b);
+    ez = df64::from_double(c);
+  }
+}
+
 // k_eam_density with the pair arithmetic in double-float: e from the FP64
 // positions (the periodic image added as k_eam_density adds it), then r^2,
 // the cut-off test, r and f_b(r) in df64, rho_i in blocked sums; F and F'
@@ -298,7 +324,8 @@ __global__ void __launch_bounds__(128)
                      const int *__restrict__ bin_count, const BinEntry *__restrict__ bins,
                      const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
                      unsigned *__restrict__ epj, int *__restrict__ ens, int kcap, double *__restrict__ fp,
-                     float2 *__restrict__ fpd, double *__restrict__ energy, unsigned *__restrict__ err) {
+                     float2 *__restrict__ fpd, double *__restrict__ energy, unsigned *__restrict__ err,
+                     const float4 *__restrict__ rec) {
   using namespace df64;
   __shared__ unsigned s_cand[CAND_SMEM * 128];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -320,6 +347,11 @@ __global__ void __launch_bounds__(128)
   }
   const int nc = eam_candidates(P, E, i, valid, Bi, oi, bin_count, bins, kcap, err, cset);
   __syncwarp();
+  float4 rh = make_float4(0.f, 0.f, 0.f, 0.f), rl = rh;
+  if (rec && valid) {
+    rh = rec[2 * (size_t)i];
+    rl = rec[2 * (size_t)i + 1];
+  }
   const df rc2{E.rc2_hi, E.rc2_lo}, inv_dr{E.inv_dr_hi, E.inv_dr_lo};
   bsum rs = bsum_zero();
   int ns = 0;
@@ -328,9 +360,8 @@ __global__ void __launch_bounds__(128)
     if (k >= nc) continue;
     const unsigned u = cget(k);
     const unsigned j = u & IDX_MASK;
-    double ex, ey, ez;
-    image_vector(P, xi, x[j], u >> IDX_BITS, ex, ey, ez);
-    const df dx = from_double(ex), dy = from_double(ey), dz = from_double(ez);
+    df dx, dy, dz;
+    pair_e_df(P, rec, Bi, rh, rl, xi, x, j, u >> IDX_BITS, dx, dy, dz);
     const df r2 = dot3(dx, dy, dz, dx, dy, dz);
     if (lt(r2, rc2)) {
       epj[(size_t)ns * P.n + i] = u;  // ns <= k: the candidate there is consumed
@@ -361,11 +392,19 @@ __global__ void __launch_bounds__(128)
 __global__ void __launch_bounds__(128)
     k_eam_force_df(StepParams P, EamParams E, const D4 *__restrict__ x, const int *__restrict__ type,
                    const unsigned *__restrict__ epj, const int *__restrict__ ens, const float2 *__restrict__ fpd,
-                   const D4 *__restrict__ fext, D4 *__restrict__ f, double *__restrict__ energy) {
+                   const D4 *__restrict__ fext, D4 *__restrict__ f, double *__restrict__ energy,
+                   const float4 *__restrict__ rec, const int4 *__restrict__ atom_bin) {
   using namespace df64;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const D4 xi = x[i];
+  int4 Bi = make_int4(0, 0, 0, 0);
+  float4 rh = make_float4(0.f, 0.f, 0.f, 0.f), rl = rh;
+  if (rec) {
+    Bi = atom_bin[i];
+    rh = rec[2 * (size_t)i];
+    rl = rec[2 * (size_t)i + 1];
+  }
   const int a = E.map[type[i]];
   const float2 gi = fpd[i];
   const df fpi{gi.x, gi.y}, inv_dr{E.inv_dr_hi, E.inv_dr_lo};
@@ -374,9 +413,8 @@ __global__ void __launch_bounds__(128)
   for (int k = 0; k < ns; ++k) {
     const unsigned u = epj[(size_t)k * P.n + i];
     const unsigned j = u & IDX_MASK;
-    double ex, ey, ez;
-    image_vector(P, xi, x[j], u >> IDX_BITS, ex, ey, ez);
-    const df dx = from_double(ex), dy = from_double(ey), dz = from_double(ez);
+    df dx, dy, dz;
+    pair_e_df(P, rec, Bi, rh, rl, xi, x, j, u >> IDX_BITS, dx, dy, dz);
     const df r2 = dot3(dx, dy, dz, dx, dy, dz);
     const df r = sqrt_df(r2);
     const df rinv = recip(r, rcp_estimate(r.hi));
@@ -509,6 +547,17 @@ int eam_resize(eph_ctx *c) {
   return EPH_OK;
 }
 
+bool eam_pair_list(const eph_ctx *c, const unsigned **pj, const int **ns) {
+  const EamDevice *d = c->eam;
+  if (!d || !d->pj.p || !d->ns.p || d->ns.n < (size_t)c->n) return false;
+  // every pair within the fix's FP32 candidate threshold must be in the list
+  // (within the EAM cut-off, by the FP64 test), with room for FP32 rounding
+  if (!((double)c->P.rc2_band * (1.0 + 1e-5) < d->host.rc * d->host.rc)) return false;
+  *pj = d->pj.p;
+  *ns = d->ns.p;
+  return true;
+}
+
 int launch_eam(eph_ctx *c) {
   EamDevice *d = c->eam;
   const EamParams E = eam_params(c);
@@ -518,11 +567,13 @@ int launch_eam(eph_ctx *c) {
   ps.launched(2);
   const D4 *fext = c->have_fext ? c->fext.p : nullptr;
   if (c->mode == EPH_MODE_FAST && c->pair_arith == EPH_PAIRS_DF64) {
+    // the atoms' df64 records of this step's bins, where k_bin wrote them
+    const float4 *rec = ctxi::df_active(c) ? c->dfrec.p : nullptr;
     k_eam_density_df<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, c->bin_count.p, c->bins.p,
                                                    c->atom_bin.p, c->atom_off.p, d->pj.p, d->ns.p, d->kcap, d->fp.p,
-                                                   d->fpd.p, d->energy.p, c->d_err.p);
+                                                   d->fpd.p, d->energy.p, c->d_err.p, rec);
     k_eam_force_df<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, d->pj.p, d->ns.p, d->fpd.p, fext,
-                                                 c->f.p, d->energy.p);
+                                                 c->f.p, d->energy.p, rec, c->atom_bin.p);
   } else {
     k_eam_density<<<nb, BLOCK, 0, c->stream>>>(c->P, E, c->x.p, c->type.p, c->bin_count.p, c->bins.p,
                                                 c->atom_bin.p, c->atom_off.p, d->pj.p, d->ns.p, d->kcap, d->fp.p,
@@ -531,6 +582,7 @@ int launch_eam(eph_ctx *c) {
                                               d->energy.p);
   }
   CUDA_TRY(c, cudaGetLastError());
+  c->eam_list_fresh = true;  // this step's pairs: the fix's density sweep may read them
   return EPH_OK;
 }
 
@@ -570,17 +622,10 @@ int eph_set_pair_eam(eph_ctx *c, const char *path, int ntypes, const char *const
     return r;
   CUDA_TRY(c, d->esum.alloc(1));
   d->rc2_band = d->host.rc * d->host.rc * (1.0 + 1e-4);
-  // the bins must hold every pair within the larger of the two cutoffs
-  const double edge = std::max(c->beta.r_cutoff, d->host.rc) * (1.0 + 5e-5);
-  for (int k = 0; k < 3; ++k) {
-    const int nb = (int)(c->prd[k] / edge);
-    if (nb < 3) return ctxi::fail(c, EPH_ERR_ARG, "box edge shorter than three EAM cutoffs");
-    c->P.nb[k] = nb;
-    c->P.w[k] = c->prd[k] / nb;
-    c->P.inv_w[k] = 1.0 / c->P.w[k];
-    c->P.wf[k] = (float)c->P.w[k];
-  }
-  c->nbins = c->P.nb[0] * c->P.nb[1] * c->P.nb[2];
+  // the bins must hold every pair within the larger of the two cutoffs (all
+  // of their geometry: the FP64, FP32 and double-float bin edges)
+  if ((r = ctxi::set_bin_geometry(c, std::max(c->beta.r_cutoff, d->host.rc))))
+    return ctxi::fail(c, EPH_ERR_ARG, "box edge shorter than three EAM cutoffs");
   c->bin_count.free();
   c->bcap = 0;
   ctxi::drop_graph(c);

@@ -338,6 +338,46 @@ __device__ __forceinline__ int collect_candidates(const StepParams &P, int i, bo
   return nc;
 }
 
+// Pass 1 from the standalone engine's EAM pair list of this step
+// (k_eam_density's rows: the same bins, the same stencil order, every pair
+// within the EAM cut-off, which exceeds r2band): its entries within the
+// FP32 threshold r2band, tested with bin_candidates' arithmetic on the
+// neighbours' bins and offsets -- the candidates of the bin search, in its
+// order, without scanning the bins.  Returns their number.
+template <class Set>
+__device__ __forceinline__ int list_candidates(const StepParams &P, int i, bool active, int4 Bi, float4 oi,
+                                               const unsigned *__restrict__ elist, const int *__restrict__ ens,
+                                               const int4 *__restrict__ atom_bin, const float4 *__restrict__ atom_off,
+                                               unsigned *__restrict__ err, Set cset, float r2band, int cap) {
+  int nc = 0;
+  const int ne = active ? ens[i] : 0;
+  const int nmax = __reduce_max_sync(0xffffffffu, ne);
+  for (int k = 0; k < nmax; ++k) {
+    if (k >= ne) continue;
+    const unsigned u = elist[(size_t)k * P.n + i];
+    const unsigned j = u & IDX_MASK, code = u >> IDX_BITS;
+    const int4 Bj = atom_bin[j];
+    const float4 oj = atom_off[j];
+    // the stencil cell of the pair: j's (unwrapped) bin moved by its image
+    const int dx = Bj.x + ((int)(code % 3u) - 1) * P.nb[0] - Bi.x;
+    const int dy = Bj.y + ((int)((code / 3u) % 3u) - 1) * P.nb[1] - Bi.y;
+    const int dz = Bj.z + ((int)(code / 9u) - 1) * P.nb[2] - Bi.z;
+    if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
+      atomicOr(err, ERR_DRIFT);
+      continue;
+    }
+    const float bx = (float)dx * P.wf[0] - oi.x, by = (float)dy * P.wf[1] - oi.y, bz = (float)dz * P.wf[2] - oi.z;
+    const float ex = bx + oj.x, ey = by + oj.y, ez = bz + oj.z;
+    if (ex * ex + ey * ey + ez * ez < r2band) {
+      if (nc >= cap)
+        atomicOr(err, ERR_PAIR_OVERFLOW);
+      else
+        cset(nc++, u);
+    }
+  }
+  return nc;
+}
+
 // The same sort with one warp per bin, for bins of at most 64 entries: lane l
 // holds entries l and l + 32, each entry's place is the number of entries
 // with a smaller atom index (indices are distinct), found by broadcasting
@@ -661,7 +701,8 @@ __global__ void __launch_bounds__(128, EPH_DF_DENSITY_BLOCKS) k_density_df(
     float4 *__restrict__ pc, int *__restrict__ nshort, D4 *__restrict__ A, D4 *__restrict__ Bw,
     double *__restrict__ rho_out, double *__restrict__ beta_out, int *__restrict__ cell, double *__restrict__ Te_i,
     int *__restrict__ wrapflag, unsigned *__restrict__ err, unsigned long long *__restrict__ counters,
-    const D4 *__restrict__ v, D4 *__restrict__ Mm, D4 *__restrict__ G) {
+    const D4 *__restrict__ v, D4 *__restrict__ Mm, D4 *__restrict__ G, const unsigned *__restrict__ elist = nullptr,
+    const int *__restrict__ ens = nullptr) {
   using namespace df64;
   __shared__ unsigned s_cand[CAND_SMEM * 128];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -685,11 +726,15 @@ __global__ void __launch_bounds__(128, EPH_DF_DENSITY_BLOCKS) k_density_df(
     Ri1 = rec[2 * (size_t)i + 1];
   }
   const int ei = __float_as_int(Ri1.w);
-  // pass 1: candidates, FP32/integer work only, warp-uniform loop bounds
+  // pass 1: candidates, FP32/integer work only, warp-uniform loop bounds;
+  // from the EAM pair list when the standalone engine made one this step
   {
     float4 of = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) of = atom_off[i];
-    nc = collect_candidates<true>(P, i, active, Bi, of, bin_count, bins, err, cget, cset, P.rc2_band, P.kcap);
+    if (elist)
+      nc = list_candidates(P, i, active, Bi, of, elist, ens, atom_bin, atom_off, err, cset, P.rc2_band, P.kcap);
+    else
+      nc = collect_candidates<true>(P, i, active, Bi, of, bin_count, bins, err, cget, cset, P.rc2_band, P.kcap);
   }
   __syncwarp();
   // pass 2 in df64: M_i (xx, xy, xz, yy, yz, zz) and S_i (x, y, z), DF_UNROLL
