@@ -1,6 +1,6 @@
 """Benchmark of the fix-eph hot path on GB300: fix-eph atom-steps/s.
 
-Workload (the plain FP64 cascade at scale): fcc Ni 80x80x80 cells (2,048,000
+Workload (the plain cascade at scale): fcc Ni 80x80x80 cells (2,048,000
 atoms) at 300 K, a 10 keV primary knock-on atom at the box centre, dt 0.5 fs,
 the synthetic beta file (rho(r) = exp(-r/0.6) cut at 4.6 A, beta(rho) = 0.05
 + 0.02 tanh(rho - 2), 2,000 knots each), flags 7 (friction + random + FDM),
@@ -9,11 +9,13 @@ inputs stand in for the reference's LAMMPS decks; no pair potential (the metric
 excludes pair forces: external force zero).
 
 One step = one engine step through the fix: initial_integrate, position wrap
-check, binning + in-cutoff pair list, density, friction pre-vector, friction +
-random forces, final_integrate, energy deposition, FDM substeps.  `value` is
-device-resident (CUDA events on the fix's stream); `e2e` drives the same
-step through the C ABI hooks with host buffers (positions, velocities, forces
-copied in and out every step).
+check, binning + in-cutoff pair list (kept candidate lists), density,
+friction pre-vector, friction + random forces, final_integrate, energy
+deposition, FDM substeps; FAST mode, the per-atom work in FP64 and the pair
+terms in double-float (df64).  `value` is device-resident (CUDA events on the
+fix's stream); `e2e` drives the same step through the C ABI hooks the LAMMPS
+fix calls, with its host arrays (positions, velocities, forces and the
+per-atom array copied in and out every step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -792,7 +794,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64 (pair terms df64)", "data": "synthetic",
         "config": {"workload": WORKLOAD, "atoms_per_gpu": n, "grid": list(GRID), "dt_ps": DT,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (pair cache ~%d MB)" % (res["n_pairs"] * 52 // 2 ** 20),
