@@ -539,7 +539,12 @@ def run_adjoint_fit(args, dev):
         hist_w = np.bincount(np.clip((rho / drho).astype(int), 0, 63), minlength=64).astype(float)
         hist_w /= hist_w.sum()
         t0 = time.perf_counter()
-        beta, hist = fit_beta_batch(batch, nsteps, target, beta0, iters=iters, lr=0.05)
+
+        def progress(it, loss):  # one line per Adam iteration on stderr (long runs)
+            print(json.dumps({"fit_iteration": it, "loss": loss, "wall_s": time.perf_counter() - t0}),
+                  file=sys.stderr, flush=True)
+
+        beta, hist = fit_beta_batch(batch, nsteps, target, beta0, iters=iters, lr=0.05, log=progress)
         wall = time.perf_counter() - t0
         import torch
         free, total = torch.cuda.mem_get_info(dev)
