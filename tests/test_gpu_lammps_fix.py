@@ -91,3 +91,24 @@ def test_fix_eph_gb_pair_arithmetic(built, beta_file, pairs):
             assert key_err(k, gb.get(k), ref.get(k)) <= 1e-12, (pairs, s, k)
     with pytest.raises(RuntimeError):
         gb.modify("pairs", "fp32")
+
+
+def test_fix_eph_gb_list_skin_auto(built, beta_file):
+    """`fix_modify ID list_skin auto`: after the first post_force the fix runs
+    eph_autotune_list_skin (trial windows of steps on the device, the state
+    restored); the run goes on matching the reference fix per atom (16,384
+    atoms, one lane per atom, a knock-on atom)."""
+    at = W.fcc_lattice(16, seed=93, temperature=300.0)
+    W.add_pka(at, 1000.0, seed=94)
+    words = W.fix_args(beta_file, grid=(8, 8, 8))
+    words[2] = "eph/gb"
+    gb = GbFix(words, at, 0.0005, 4.6, mode=1, xi_host=1)
+    gb.modify("list_skin", "auto")
+    ref = OracleFix(words, at, 0.0005)
+    ng = n_in_group(at)
+    for s in range(6):
+        xi = W.gaussian_stream(ng, 37, s)
+        gb.step(xi)
+        ref.step(xi)
+        for k in ("x", "v", "f", "array"):
+            assert key_err(k, gb.get(k), ref.get(k)) <= 1e-12, (s, k, key_err(k, gb.get(k), ref.get(k)))

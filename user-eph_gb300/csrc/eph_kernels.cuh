@@ -1367,6 +1367,15 @@ __global__ void __launch_bounds__(128, EPH_DF_DENSITY_BLOCKS) k_density_list_df(
     const df ez = pair_disp(bjz + mz * P.nb[2] - biz, R0.z, R1.z, oi.z, Ri1.z, P.w_hi[2], P.w_lo[2]);
     df r2 = dot3(ex, ey, ez, ex, ey, ez);
     const bool in = have && lt(r2, rc2);
+    // the shell beyond the cut-off sits at the end of the lists: where no
+    // lane of the warp has a pair inside, the iteration would add only zeros
+    if (!__any_sync(0xffffffffu, in)) {
+      if ((k & 7) == 7) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) bsum_fold(sm[q]);
+      }
+      continue;
+    }
     if (!in) r2 = df{1.0f, 0.0f};
     const int ej = __float_as_int(R1.w);
     const df rji = spline_rho_df(P, ej, r2, err);

@@ -128,7 +128,15 @@ int FixEPHGB::modify_param(int narg, char **arg) {
   } else if (strcmp(arg[0], "device") == 0) {
     device = atoi(arg[1]);
   } else if (strcmp(arg[0], "list_skin") == 0) {
+    // a skin in distance units, or `auto`: eph_autotune_list_skin picks one
+    // after the first post_force (trial windows from the device state,
+    // restored afterwards)
+    if (strcmp(arg[1], "auto") == 0) {
+      tune_skin = true;
+      return 2;
+    }
     list_skin = atof(arg[1]);
+    tune_skin = false;
     check(eph_set_list_skin(ctx, list_skin), "list skin");
     return 2;
   } else if (strcmp(arg[0], "pairs") == 0) {
@@ -203,6 +211,13 @@ void FixEPHGB::post_force(int) {
   const double *x = (!full && neighbor->ago == 0) ? &atom->x[0][0] : nullptr;
   double *arr = (update->ntimestep % peratom_freq == 0) ? &array[0][0] : nullptr;
   check(eph_post_force_host(ctx, x, &atom->f[0][0], &atom->f[0][0], arr, source), "post_force");
+  if (tune_skin) {
+    static const double candidates[] = {0.0, 0.15, 0.2, 0.3, 0.4, 0.6};
+    check(eph_autotune_list_skin(ctx, candidates, (int)(sizeof(candidates) / sizeof(candidates[0])), 20,
+                                 &list_skin),
+          "list skin autotune");
+    tune_skin = false;
+  }
 }
 
 void FixEPHGB::final_integrate() {

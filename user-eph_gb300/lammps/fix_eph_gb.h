@@ -15,7 +15,8 @@
  * fix_modify options: `mode exact|fast` (EPH_MODE_*), `xi host|device`
  * (deviates from the engine's RanMars stream on the host, or the device
  * Philox generator), `device N`, `list_skin S` (skin of the kept candidate
- * lists in distance units, 0: search the bins every step), `pairs df64|fp64`
+ * lists in distance units, 0: search the bins every step, `auto`: timed
+ * trial windows after the next post_force, eph_autotune_list_skin), `pairs df64|fp64`
  * (arithmetic of the FAST-mode pair sums, eph_set_pair_arithmetic; default
  * df64), `peratom N` (copy
  * the per-atom array back only on steps that are multiples of N and declare
@@ -70,6 +71,7 @@ class FixEPHGB : public Fix {
   int device = 0;
   int nlocal_dev = -1;            // atom count the device holds
   double list_skin = -1.0;        // fix_modify list_skin (negative: the library's default)
+  bool tune_skin = false;         // fix_modify list_skin auto: autotune after the next post_force
   int pair_arith = -1;            // fix_modify pairs (negative: the library's default, df64)
   bool reordered = false;         // the engine moved atoms between slots since the last upload
   bigint last_upload_step = -1;   // step of the last full atom upload
