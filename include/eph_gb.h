@@ -214,8 +214,9 @@ int eph_autotune(eph_ctx *ctx, int *chosen);
  * skins[0..nskins-1] (0 = the bin search every step), each window starting
  * with a list build as a run does after eph_set_list_skin (one untimed
  * window first), then restore the state -- positions, velocities, forces,
- * memories, deviates, per-atom records, the grid, the vector, counters and
- * step counters; no T_out file is written -- and keep the skin of the fastest
+ * memories, deviates, per-atom records, the atoms' grid cells and T_e there,
+ * the grid, the vector, counters and step counters; no T_out file is
+ * written, so it may also run between post_force and end_of_step -- and keep the skin of the fastest
  * window; *chosen gets it (may be NULL).  The bins' edge is r_cutoff + skin
  * (their 27-bin stencil), so this chooses the bin size too.  A window that
  * overflows the bins or pair rows rules its skin out.  The trajectory from

@@ -1178,12 +1178,14 @@ int eph_autotune_list_skin(eph_ctx *c, const double *skins, int nskins, int step
   DevBuf<D4> *d4[] = {&c->x, &c->v, &c->f, &c->xhold, &c->f_eph, &c->f_rng, &c->f_dis, &c->f_sto, &c->xi, &c->A, &c->Bw};
   const int ND4 = (int)(sizeof(d4) / sizeof(d4[0]));
   DevBuf<D4> s_d4[ND4];
-  DevBuf<double> s_rho, s_beta, s_T, s_scal;
+  DevBuf<double> s_rho, s_beta, s_tei, s_T, s_scal;
   DevBuf<unsigned long long> s_cnt, s_step;
-  DevBuf<int> s_wrap;
+  DevBuf<int> s_wrap, s_cell;
   for (int k = 0; k < ND4; ++k) CUDA_TRY(c, s_d4[k].alloc(N));
   CUDA_TRY(c, s_rho.alloc(N));
   CUDA_TRY(c, s_beta.alloc(N));
+  CUDA_TRY(c, s_tei.alloc(N));
+  CUDA_TRY(c, s_cell.alloc(N));
   CUDA_TRY(c, s_T.alloc(NC));
   CUDA_TRY(c, s_scal.alloc(4));
   CUDA_TRY(c, s_cnt.alloc(NCOUNTERS));
@@ -1198,6 +1200,10 @@ int eph_autotune_list_skin(eph_ctx *c, const double *skins, int nskins, int step
     for (int k = 0; k < ND4; ++k) pair(d4[k]->p, s_d4[k].p, sizeof(D4) * N);
     pair(c->rho.p, s_rho.p, sizeof(double) * N);
     pair(c->beta_i.p, s_beta.p, sizeof(double) * N);
+    // the atoms' grid cells and T_e there: between post_force and
+    // end_of_step (an engine's hooks) the deposition still reads them
+    pair(c->Te_i.p, s_tei.p, sizeof(double) * N);
+    pair(c->cell.p, s_cell.p, sizeof(int) * N);
     pair(c->T0.p, s_T.p, sizeof(double) * NC);
     pair(c->scal.p, s_scal.p, sizeof(double) * 4);
     pair(c->counters.p, s_cnt.p, sizeof(unsigned long long) * NCOUNTERS);
