@@ -141,6 +141,17 @@ int main() {
     const ld fsc = fmaxl(fabsl(Fl[0]), fmaxl(fabsl(Fl[1]), fabsl(Fl[2])));
     for (int k = 0; k < 3; ++k) e_f = fmaxl(e_f, rel(to_double(bsum_value(F[k])), Fl[k], fsc));
   }
+  // the square root of the EAM sweeps (r from r^2), with the host's seed and
+  // with seeds off by +-2^-22 relative (the device estimate's error class)
+  ld e_sqrt = 0, e_sqrt_seed = 0;
+  for (int t = 0; t < N; ++t) {
+    const ld x = 0.01L + 60.0L * (ld)P(g);
+    const df X = D(x);
+    const ld want = sqrtl(L(X));
+    e_sqrt = fmaxl(e_sqrt, rel(L(sqrt(X, rsqrt_estimate(X.hi))), want, want));
+    const float y = rsqrt_estimate(X.hi) * (t & 1 ? 1.0f + 2.384185791015625e-7f : 1.0f - 2.384185791015625e-7f);
+    e_sqrt_seed = fmaxl(e_sqrt_seed, rel(L(sqrt(X, y)), want, want));
+  }
   // the spline index estimate: floor(q) or one less, never negative, for
   // 0 <= q < 2^22 (the knot counts of the beta files are far below that)
   int bad_floor = 0;
@@ -155,5 +166,6 @@ int main() {
   printf("add %.3Le\nmul %.3Le\nrecip %.3Le\ndisplacement %.3Le\ndot3 %.3Le\nhorner %.3Le\n", e_add, e_mul, e_rcp,
          e_disp, e_dot, e_hor);
   printf("atom_M %.3Le\natom_S %.3Le\natom_w %.3Le\natom_force_sum %.3Le\n", e_M, e_S, e_w, e_f);
+  printf("sqrt %.3Le\nsqrt_seed_2e-7 %.3Le\n", e_sqrt, e_sqrt_seed);
   return 0;
 }

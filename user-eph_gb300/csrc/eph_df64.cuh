@@ -164,6 +164,34 @@ DF_FN float rcp_estimate(float x) {
 #endif
 }
 
+// FP32 reciprocal square root estimate: rsqrt.approx.ftz.f32 on the device,
+// 1 / sqrtf on the host
+DF_FN float rsqrt_estimate(float x) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return 1.0f / sqrtf(x);
+#endif
+}
+
+// sqrt(a) for a > 0 in the FP32 normal range from y ~ 1/sqrt(a.hi): the
+// estimate s0 = a.hi y, then twice s + y (a - s^2) / 2 (Karp and Markstein's
+// form of Newton's iteration, "High-precision division and square root",
+// ACM TOMS 23 (1997)) with the first residual formed exactly by TwoProd; the
+// second step takes the error from ~(2^-23)^2 to a few u
+DF_FN df sqrt(df a, float y) {
+  const float s0 = a.hi * y;
+  float p, pe;
+  two_prod(s0, s0, p, pe);
+  const float res = ((a.hi - p) - pe) + a.lo;
+  df s;
+  fast_two_sum(s0, 0.5f * y * res, s.hi, s.lo);
+  const df r2 = sub(a, mul(s, s));
+  return add(s, df{0.5f * y * r2.hi, 0.0f});
+}
+
 // round(q - 0.5) as an integer-valued float for 0 <= q < 2^22 without a
 // conversion instruction: adding 1.5 * 2^23 puts the sum where FP32 spacing
 // is exactly 1, so the addition rounds to an integer (ties to even), and

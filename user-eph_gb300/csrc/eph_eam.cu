@@ -239,25 +239,6 @@ __global__ void __launch_bounds__(128)
 
 // ---------------------------------------------- df64 pair sums (FAST mode)
 
-// sqrt(a), a > 0, as a double-float: the FP32 estimate s0 = a y (y the
-// rsqrt estimate) corrected twice by s + y (a - s^2) / 2 with the residual
-// formed exactly (Karp and Markstein's form of Newton's iteration); the
-// second correction takes the error from ~(2^-23)^2 to the double-float's
-// own ~2^-48
-__device__ __forceinline__ df64::df sqrt_df(df64::df a) {
-  using namespace df64;
-  float y;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(a.hi));
-  const float s0 = a.hi * y;
-  float p, pe;
-  two_prod(s0, s0, p, pe);
-  const float res = ((a.hi - p) - pe) + a.lo;
-  df s;
-  fast_two_sum(s0, 0.5f * y * res, s.hi, s.lo);
-  const df r2 = sub(a, mul(s, s));
-  return add(s, df{0.5f * y * r2.hi, 0.0f});
-}
-
 // herm() on a double-float table at q >= 0 (knot units): the interval from
 // the FP32 part of q settled by the sign of the double-float remainder, the
 // same clamps (at most the last interval, p at most 1), the value and the
@@ -367,7 +348,8 @@ __global__ void __launch_bounds__(128)
       epj[(size_t)ns * P.n + i] = u;  // ns <= k: the candidate there is consumed
       ++ns;
       df v, dv;
-      herm_df(E.fd + 2 * (size_t)E.map[type[j]] * E.nr, E.nr, mul(sqrt_df(r2), inv_dr), v, dv);
+      const df q = mul(df64::sqrt(r2, rsqrt_estimate(r2.hi)), inv_dr);
+      herm_df(E.fd + 2 * (size_t)E.map[type[j]] * E.nr, E.nr, q, v, dv);
       acc_add(rs.blk, v);
       if ((ns & 7) == 0) bsum_fold(rs);
     }
@@ -416,7 +398,7 @@ __global__ void __launch_bounds__(128)
     df dx, dy, dz;
     pair_e_df(P, rec, Bi, rh, rl, xi, x, j, u >> IDX_BITS, dx, dy, dz);
     const df r2 = dot3(dx, dy, dz, dx, dy, dz);
-    const df r = sqrt_df(r2);
+    const df r = df64::sqrt(r2, rsqrt_estimate(r2.hi));
     const df rinv = recip(r, rcp_estimate(r.hi));
     const df q = mul(r, inv_dr);
     const int b = E.map[type[j]];
