@@ -159,6 +159,15 @@ FORCES_PIPES = {"issue_active": 0.377, "fma_pipe": 0.298, "alu_pipe": 0.083, "fp
                 "top_stall": "long_scoreboard"}
 
 
+def step_bytes_8d(n_list=78, sweeps=3):
+    """Algorithmic HBM bytes of one atom-step by the hot-path scope's own
+    count (a stored full list of n_list entries per atom read by `sweeps`
+    list sweeps, 4 B each; x, v, type read over the passes, 156 B; xi, T_e
+    at the atom, rho, alpha, w, f_EPH, f_RNG, f and the deposition, 224 B):
+    1,316 B at n_list = 78 (the list with a 1 A skin) and 3 sweeps."""
+    return 4 * n_list * sweeps + 156 + 224
+
+
 def ranks_reduce(x, op, device):
     """x combined over the ranks of the process group ("max" for times, "sum"
     for throughputs of independent replicas); x itself without a group or
@@ -809,6 +818,13 @@ def main():
                              DENSITY_DRAM_OVER_ALGORITHMIC, DENSITY_PIPES),
         "roofline_forces": roofline("forces", "k_forces_df", forces_bytes(n, res["n_pairs"]),
                                     FORCES_DRAM_OVER_ALGORITHMIC, FORCES_PIPES),
+        # the whole step against HBM with the scope's own byte count per atom-step
+        "roofline_step": {"bound": "hbm", "bytes_per_atom_step": step_bytes_8d(),
+                          "achieved": step_bytes_8d() * n / (res["ms"] / args.steps / 1000.0) / 1e9,
+                          "peak": hbm, "unit": "GB/s",
+                          "frac": step_bytes_8d() * n / (res["ms"] / args.steps / 1000.0) / 1e9 / hbm,
+                          "note": "4 n_L P + 156 + 224 B per atom-step, n_L = 78, P = 3; the sweeps are bound "
+                                  "by issue and latency, not by these bytes"},
         "phases_ms": {k: round(v[0], 3) for k, v in res["phases"].items()},
         "clocks": res["clocks"],
         "pairs_per_atom": res["n_pairs"] / n,
