@@ -145,17 +145,17 @@ def forces_bytes(n_atoms, n_pairs):
 
 
 # DRAM bytes of one launch (dram__bytes_read.sum + dram__bytes_write.sum) over
-# the algorithmic bytes of that launch, from an ncu capture of the same
-# kernels on the 131,072-atom cascade (`bench.py --cells 32 --grid 26`, kept
+# the algorithmic bytes of that launch, from ncu captures of each kernel
+# alone on the 131,072-atom cascade (`bench.py --cells 32 --grid 26`, kept
 # lists, 42.0 pairs per atom, like the bench workload); the bench's traffic figure is this ratio times the algorithmic
 # bytes at its own size.  Under 1: part of a sweep's pair-cache writes is
 # still in L2 when it ends.
-DENSITY_DRAM_OVER_ALGORITHMIC = 0.860
+DENSITY_DRAM_OVER_ALGORITHMIC = 0.858
 FORCES_DRAM_OVER_ALGORITHMIC = 0.987
-# pipe and issue figures of the two sweeps (ncu, the same capture)
-DENSITY_PIPES = {"issue_active": 0.479, "fma_pipe": 0.348, "alu_pipe": 0.130, "fp64_pipe": 0.286,
+# pipe and issue figures of the two sweeps (ncu, the same captures)
+DENSITY_PIPES = {"issue_active": 0.469, "fma_pipe": 0.332, "alu_pipe": 0.144, "fp64_pipe": 0.294,
                  "top_stall": "long_scoreboard"}
-FORCES_PIPES = {"issue_active": 0.377, "fma_pipe": 0.298, "alu_pipe": 0.083, "fp64_pipe": 0.157,
+FORCES_PIPES = {"issue_active": 0.379, "fma_pipe": 0.298, "alu_pipe": 0.083, "fp64_pipe": 0.157,
                 "top_stall": "long_scoreboard"}
 
 
