@@ -240,6 +240,21 @@ def run_gpu(args, rank, world):
         out.update(ms=ms, phases=phases, launches=launches, n_pairs=n_pairs, clocks=clock, n=n,
                    rebuilds=fix.counter("wrap"), list_builds=fix.counter("build") - builds0, list_skin=fix.list_skin(),
                    skin_autotuned=tuned)
+        if not args.no_fp64_pairs:
+            # the same steps with the pair terms in FP64 (EPH_PAIRS_FP64), from
+            # the state reached: the rate of the FP64-throughout form
+            fix.set_pair_arithmetic(ephgb.PAIRS_FP64)
+            fix.step(3)
+            fix.synchronize()
+            k64 = max(1, min(args.steps, 50))
+            e0.record(stream)
+            fix.step(k64)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out.update(ms64=ranks_reduce(e0.elapsed_time(e1), "max", "cuda"), steps64=k64)
+            fix.set_pair_arithmetic(ephgb.PAIRS_DF64)
+            fix.step(2)
+            fix.synchronize()
         if args.no_e2e:
             return out
         # ------------------------------------------------ end to end (host)
@@ -729,6 +744,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="omit the end-to-end leg")
+    ap.add_argument("--no-fp64-pairs", action="store_true", help="omit the leg with FP64 pair terms")
     ap.add_argument("--no-batched", action="store_true", help="omit the batched-replicas leg")
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--no-adjoint", action="store_true", help="omit the adjoint leg")
@@ -832,6 +848,11 @@ def main():
         "list_skin_A": res["list_skin"][0] if res["list_skin"][1] else 0.0,
         "list_builds": res["list_builds"],  # in the timed steps
     }
+    if "ms64" in res:
+        line["fp64_pairs"] = {"value": job_value(world, n, res["steps64"], res["ms64"]), "unit": METRIC,
+                              "ms_per_step": res["ms64"] / res["steps64"], "steps": res["steps64"],
+                              "note": "the same workload with the pair terms in FP64 (EPH_PAIRS_FP64), "
+                                      "timed after the main steps from the state they reached"}
     if res.get("skin_autotuned") is not None:
         line["list_skin_autotuned"] = {"candidates_A": list(SKIN_CANDIDATES), "chosen_A": res["skin_autotuned"],
                                        "window_steps": args.autotune_steps}
