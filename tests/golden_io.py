@@ -22,6 +22,9 @@ REF_FILES = {
     "Example_4_Ni_model_4.beta": "Examples/Example_4/Ni_model_4.beta",
     "Example_4_struc_in.data": "Examples/Example_4/struc_in.data",  # 500 atoms with velocities
     "MD_Run_Ni.eam": "Tests/MD_Run/Ni.eam",  # the decks' eam/alloy potential (setfl)
+    # the LAMMPS run of that deck (fix print every 1000 steps: step, time, temp,
+    # mean T_e, the knock-on atom's x y z, pe, ke, E_e, its rho and beta)
+    "MD_Run_out.data": "Tests/MD_Run/Reference/out.data",
 }
 
 

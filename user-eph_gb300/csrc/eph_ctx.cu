@@ -262,7 +262,10 @@ void launch_density_f(eph_ctx *c, int xi_mode) {
   // and lane sums cost more than they hide: 32,000 atoms 71 -> 81 ms per 200
   // steps, so the one-lane sweep stays there)
   if constexpr (FAST) {
-    if (c->tpa > 1 && c->n < 16384) {
+    // not over the EAM engine's bins: they are sized for its cut-off, and a
+    // lane's share of 27 such bins can hold more candidates than its
+    // shared-memory column (the one-lane sweeps spill to the pair rows)
+    if (c->tpa > 1 && c->n < 16384 && !c->eam) {
 #define EPH_DENSITY_TPA(T)                                                                                         \
   k_density_tpa<MULTI, FUSE, T><<<nblocks((long)c->n * T), BLOCK, 0, c->stream>>>(                                  \
       c->P, c->x.p, c->mask.p, c->bin_count.p, c->bins.p, c->atom_bin.p, c->atom_off.p, c->xi.p, xi_mode, c->T0.p, \
