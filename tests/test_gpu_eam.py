@@ -5,9 +5,11 @@ perfect lattice, and energy conservation of plain NVE.  Two potentials: a
 generated Sutton-Chen Ni setfl (6 A cut-off) and the reference decks' own
 Tests/MD_Run/Ni.eam (10001-point tables, 6.5 A cut-off; kept under
 tests/golden/ref_inputs).  FAST mode sums the pair terms in double-float
-(the default) or in FP64; both are checked.  Parity with LAMMPS's
-pair_style eam/alloy itself is unpinned (LAMMPS is not available); the
-tables follow the same cubic Hermite scheme with five-point slopes."""
+(the default) or in FP64; both are checked.  LAMMPS itself is not available
+here: what ties the pair force to LAMMPS's pair_style eam/alloy is the
+reference's MD_Run deck against its LAMMPS output
+(tests/test_gpu_md_run_deck.py); the tables follow the same cubic Hermite
+scheme with five-point slopes."""
 import numpy as np
 import pytest
 
